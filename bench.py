@@ -1,0 +1,395 @@
+#!/usr/bin/env python3
+"""Benchmark of the SimulationCode.jl MD hot path on GB300 (libsimmd).
+
+Prints ONE JSON line.  A "step" is one MD time step of every particle of the
+workload (all replicas).  ``value`` = particle-steps/s with the state
+resident in HBM (device-timed with CUDA events on the library's stream);
+``e2e`` = the same metric through the C ABI with host buffers: upload of the
+ArrayStruct arrays from page-locked host memory, simmd_step, download of the
+state, all inside the timed region.
+
+    python bench.py [--workload c4] [--steps K] [--warmup W] [--gpus N]
+    python bench.py --impl reference ...   # the reference algorithm on the host cores
+
+Multi-GPU: replicas only (independent systems, no collective); each rank
+runs the full workload on its own GPU (weak scaling), max time over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+MEASURED_PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class Dist:
+    def __init__(self):
+        self.ws, self.rank, self.local = dist_env()
+        self.pg = None
+        if self.ws > 1:
+            import torch.distributed as dist
+            dist.init_process_group("gloo")
+            self.dist = dist
+
+    def barrier(self):
+        if self.ws > 1:
+            self.dist.barrier()
+
+    def max(self, x):
+        if self.ws == 1:
+            return x
+        import torch
+        t = torch.tensor([float(x)], dtype=torch.float64)
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.ws > 1:
+            self.dist.destroy_process_group()
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.th = threading.Thread(target=self._read, daemon=True)
+            self.th.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for k, n in enumerate(names):
+                if f[5 + k].lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def peaks():
+    try:
+        with open(MEASURED_PEAKS) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def force_bytes_per_launch(specs, stats):
+    """Algorithmic HBM bytes of one force-kernel launch: per particle its own
+    position record (FP64 x,y,z,D = 32 B, or the FP32 offset record 16 B), the
+    list count, original id and 4 B per list entry, the force write (8 B per
+    component) and, when the second half-kick is fused (Newtonian/Langevin),
+    the velocity read and write (16 B per component).  Neighbour positions
+    are gathered from L2 (cell-sorted layout) and not counted."""
+    total = 0
+    for s, st in zip(specs, stats):
+        own = 32 if s.precision == 0 else 16
+        per = own + 4 + 4 + 8 * s.dims
+        if s.dynamics != 2:
+            per += 16 * s.dims
+        total += s.N * per + 4 * int(st.list_entries)
+    return total
+
+
+def build_batch(specs, device, tpp):
+    from simulationcode_gb300.batch import ReplicaBatch
+    b = ReplicaBatch(device, tpp=tpp, graphs=True, graph_steps=16)
+    n = sum(s.N for s in specs)
+    b.reserve(n + 128 * len(specs), 4 * n // 8 + 64 * len(specs), len(specs) + 1, max(s.max_neighbors for s in specs))
+    ids = [b.add(s) for s in specs]
+    return b, ids
+
+
+def relax_specs(specs, device, steps=300, cap=0.05):
+    """Set-up relaxation on the GPU in FP64; returns relaxed positions."""
+    from simulationcode_gb300 import _lib
+    import copy
+    tmp = []
+    for s in specs:
+        t = copy.copy(s)
+        t.precision = _lib.FP64
+        tmp.append(t)
+    b, ids = build_batch(tmp, device, 1)
+    b.rebuild()
+    b.relax(steps, cap)
+    out = [b.state(i)[0] for i in ids]
+    b.close()
+    return out
+
+
+def cpu_baseline_port(specs, seconds=12.0):
+    """The oracle (serial C restatement of the reference) on a bounded sample
+    of the same workload: whole replicas, a few steps each."""
+    from oracle import build as ob, pyoracle as O
+    ob.build_oracle()
+    done_ps, t_used = 0, 0.0
+    used = []
+    for s in specs:
+        p = O.make_params(s.dims, s.potential, s.dynamics, s.N, s.box_size, s.force_cutoff2, s.skin,
+                          eps=s.lj_eps, sigma=s.lj_sigma, lj_rc=math.sqrt(s.force_cutoff2), zeta=s.b_zeta,
+                          berthier_rc=math.sqrt(s.force_cutoff2), kBT=s.kBT, gamma=s.gamma, dt=s.dt, m=s.m)
+        sysm = O.OracleSystem(p, s.r, s.D, v=s.v, force_cutoff=s.verlet_force_cutoff, maxK=s.max_neighbors * 2)
+        sysm.update_neighbor_lists()
+        t0 = time.perf_counter()
+        sysm.run(1, seed=s.seed)
+        t1 = time.perf_counter()
+        per = max(t1 - t0, 1e-6)
+        nsteps = int(max(1, min(200, (seconds - t_used) / per)))
+        t0 = time.perf_counter()
+        sysm.run(nsteps, seed=s.seed, step0=1)
+        dt = time.perf_counter() - t0
+        done_ps += s.N * nsteps
+        t_used += dt + per
+        used.append((s.N, s.dims, nsteps))
+        if t_used > seconds:
+            break
+    value = done_ps / max(t_used, 1e-9)
+    sample = "%d replica(s) of the workload, %d particle-steps (%s)" % (
+        len(used), done_ps, ", ".join("N=%d %dD x%d steps" % u for u in used[:4]) + ("..." if len(used) > 4 else ""))
+    return {"value": value, "unit": "particle-steps/s", "cores": 1, "kind": "port", "sample": sample}
+
+
+def run_reference(args, dist):
+    """--impl reference: the reference algorithm (the oracle port, a serial
+    restatement of the Julia routines; Julia itself is not available) on the
+    host cores, threads over replicas."""
+    from concurrent.futures import ThreadPoolExecutor
+    from simulationcode_gb300 import workloads as W
+    from oracle import build as ob, pyoracle as O
+    ob.build_oracle()
+    specs = W.WORKLOADS[args.workload](precision=0)
+    # the same seeded initial state; positions relaxed by the oracle's MC
+    # restatement of find_random_initial_configuration! (few sweeps)
+    systems = []
+    for s in specs:
+        p = O.make_params(s.dims, s.potential, s.dynamics, s.N, s.box_size, s.force_cutoff2, s.skin,
+                          eps=s.lj_eps, sigma=s.lj_sigma, lj_rc=math.sqrt(s.force_cutoff2), zeta=s.b_zeta,
+                          berthier_rc=math.sqrt(s.force_cutoff2), kBT=s.kBT, gamma=s.gamma, dt=s.dt, m=s.m)
+        r = s.r
+        if s.potential == O.POT_BERTHIER:
+            r, _ = O.random_initial_configuration(p, s.D, 3, max_disp=0.1, seed=s.seed, maxK=s.max_neighbors * 2,
+                                                  skin=0.6)
+        sysm = O.OracleSystem(p, r, s.D, v=s.v, force_cutoff=s.verlet_force_cutoff, maxK=s.max_neighbors * 2)
+        sysm.update_neighbor_lists()
+        systems.append((s, sysm))
+    cores = max(1, min(os.cpu_count() or 1, len(systems)))
+    pool = ThreadPoolExecutor(cores)
+    step_no = [0]
+
+    def one_step():
+        k = step_no[0]
+        list(pool.map(lambda t: t[1].run(1, seed=t[0].seed, step0=k), systems))
+        step_no[0] += 1
+
+    for _ in range(args.warmup):
+        one_step()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        one_step()
+    dt = time.perf_counter() - t0
+    n = sum(s.N for s, _ in systems)
+    value = n * args.steps / dt
+    line = {"metric": "particle-steps/s", "value": value, "unit": "particle-steps/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * dt / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "impl": "reference",
+            "config": {"workload": args.workload, "description": W.DESCRIPTIONS[args.workload],
+                       "particles": n, "replicas": len(systems), "parallelism": "threads over replicas"},
+            "cpu_baseline": {"value": value, "unit": "particle-steps/s", "cores": cores, "kind": "port",
+                             "sample": "the full workload, %d timed steps" % args.steps},
+            "e2e": {"value": value, "unit": "particle-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    pool.shutdown()
+    return line
+
+
+def run_gpu(args, dist):
+    from simulationcode_gb300 import _lib, build as lb, workloads as W
+    lb.build()
+    lib = _lib.load()
+    device = dist.local
+    prec = {"fp64": _lib.FP64, "fp32": _lib.FP32_SPLIT}[args.precision] if args.precision else None
+    specs = W.WORKLOADS[args.workload]() if prec is None else W.WORKLOADS[args.workload](precision=prec)
+    # set-up: relax random starts on the GPU (not timed)
+    if any(s.potential == _lib.POT_BERTHIER for s in specs):
+        rel = relax_specs(specs, device)
+        for s, r in zip(specs, rel):
+            s.r = r
+    batch, ids = build_batch(specs, device, args.tpp)
+    batch.rebuild()
+    batch.step(args.warmup)
+    st_before = [batch.stats(i) for i in ids]
+    dist.barrier()
+    clocks = ClockSampler(device)
+    clocks.start()
+    l0 = batch.launches()
+    batch.timer_start()
+    batch.step(args.steps)
+    ms = batch.timer_stop()
+    launches = batch.launches() - l0
+    clk = clocks.stop()
+    ms = dist.max(ms)
+    n = sum(s.N for s in specs)
+    value = n * args.steps / (ms / 1000.0)
+    st_after = [batch.stats(i) for i in ids]
+    rebuilds = sum(b.rebuilds - a.rebuilds for a, b in zip(st_before, st_after))
+
+    # force-kernel duration: CUDA events around every force launch of an
+    # instrumented pass of the same step loop (direct launches)
+    batch.profile(True)
+    batch.step(max(16, min(args.steps, 64)))
+    prof = batch.profile_get()
+    batch.profile(False)
+    force_ms = prof["force_ms"] / max(prof["force_n"], 1)
+    stats = [batch.stats(i) for i in ids]
+    fbytes = force_bytes_per_launch(specs, stats)
+    peak, peak_kind = peaks()
+    achieved = fbytes / (force_ms / 1000.0) / 1e9
+    traffic = None
+    tfile = os.path.join(ROOT, "profiles", "force_traffic_%s.json" % args.workload)
+    if os.path.exists(tfile):
+        try:
+            with open(tfile) as f:
+                traffic = json.load(f).get("dram_bytes_per_launch")
+        except Exception:
+            traffic = None
+
+    # e2e through the C ABI: host (page-locked) arrays -> device, K steps,
+    # device -> host, for every replica
+    host = []
+    h2d = d2h = 0
+    for s in specs:
+        r = np.ascontiguousarray(s.r, dtype=np.float64)
+        v = np.ascontiguousarray(s.v if s.v is not None else np.zeros_like(r))
+        D = np.ascontiguousarray(s.D, dtype=np.float64)
+        F = np.zeros_like(r)
+        outs = [np.zeros_like(r) for _ in range(3)]
+        for a in [r, v, D, F] + outs:
+            lib.simmd_host_register(C.c_void_p(a.ctypes.data), a.nbytes)
+        host.append((r, v, D, F, outs))
+        h2d += r.nbytes + D.nbytes + (v.nbytes if s.dynamics != 2 else 0)
+        d2h += r.nbytes + F.nbytes + (v.nbytes if s.dynamics != 2 else 0)
+    e2e_steps = args.steps
+    dist.barrier()
+    t0 = time.perf_counter()
+    for rid, s, (r, v, D, F, outs) in zip(ids, specs, host):
+        _lib.check(lib.simmd_upload_r(batch.ctx, rid, _lib.ptr(r), _lib.ptr(v) if s.dynamics != 2 else None,
+                                      None, _lib.ptr(D), None))
+    _lib.check(lib.simmd_step(batch.ctx, e2e_steps, None))
+    for rid, s, (r, v, D, F, outs) in zip(ids, specs, host):
+        _lib.check(lib.simmd_download_r(batch.ctx, rid, _lib.ptr(outs[0]),
+                                        _lib.ptr(outs[1]) if s.dynamics != 2 else None, _lib.ptr(outs[2]), None))
+    e2e_s = dist.max(time.perf_counter() - t0)
+    for (r, v, D, F, outs) in host:
+        for a in [r, v, D, F] + outs:
+            lib.simmd_host_unregister(C.c_void_p(a.ctypes.data))
+    e2e = {"value": n * e2e_steps / e2e_s, "unit": "particle-steps/s",
+           "h2d_bytes_per_step": h2d / e2e_steps, "d2h_bytes_per_step": d2h / e2e_steps,
+           "what": "simmd_upload_r (r, v, D from page-locked host) + simmd_step(K) + simmd_download_r (r, v, F) "
+                   "for every replica, wall clock"}
+
+    dtype = "f64" if all(s.precision == 0 for s in specs) else "f32-split (f32 pair math, f64 integration)"
+    line = {"metric": "particle-steps/s", "value": value, "unit": "particle-steps/s", "n_gpus": dist.ws,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": dtype, "data": "synthetic",
+            "config": {"workload": args.workload, "description": W.DESCRIPTIONS[args.workload], "particles": n,
+                       "replicas": len(specs), "threads_per_particle": args.tpp,
+                       "l2": "state larger than L2" if batch.device_bytes() > 129e6 else "state fits in L2 (no flush)",
+                       "parallelism": "replicas only" if dist.ws > 1 else "single GPU",
+                       "rebuilds_in_timed_region": rebuilds},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
+                         "kernel": "k_force", "force_ms_per_launch": force_ms,
+                         "alg_bytes_per_launch": fbytes},
+            "step_breakdown_ms": {k: prof[k] / max(prof["steps"], 1) for k in ("force_ms", "kick_ms", "rebuild_ms",
+                                                                               "update_ms")},
+            "e2e": e2e, "gpu_launches": int(launches), "clocks": clk}
+    if dist.rank == 0 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline_port(specs, seconds=args.cpu_seconds)
+    batch.close()
+    return line
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="c2", choices=["c1", "c2", "c3", "c4"])
+    ap.add_argument("--precision", default=None, choices=[None, "fp64", "fp32"])
+    ap.add_argument("--tpp", type=int, default=1)
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    dist = Dist()
+    if args.impl == "reference":
+        if dist.rank != 0:
+            dist.close()
+            return
+        line = run_reference(args, dist)
+    else:
+        line = run_gpu(args, dist)
+    if dist.rank == 0:
+        print(json.dumps(line), flush=True)
+    dist.close()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,210 @@
+/*
+ * simmd.h -- C ABI of libsimmd, the GB300 (sm_103a) molecular-dynamics hot
+ * path of SimulationCode.jl behind a plain C interface (Julia reaches it by
+ * ccall; Python by ctypes).  No CUDA, C++ or torch types cross this boundary:
+ * only plain pointers to host memory, sizes and an opaque context.
+ *
+ * Reference interfaces replaced (paths relative to the SimulationCode.jl
+ * project):
+ *   initialize_neighbor_struct(skin, L, rc, N, D, dims; maxneighbours=200)
+ *        src/DataStructs.jl:349-378            -> simmd_create
+ *   update_neighbor_lists!(arrays, parameters, output, neighborlist)
+ *        src/NeighborLists.jl:24-53            -> simmd_rebuild
+ *   calculate_new_forces!(arrays, parameters, neighborlist)
+ *        src/MD.jl:262-316                     -> simmd_forces
+ *   do_time_step(arrays, parameters, output, neighborlist, system)
+ *        src/MD.jl:429-471, 499-554            -> simmd_step (nsteps = 1)
+ *   the step loop of perform_molecular_dynamics!
+ *        src/MD.jl:704-715                     -> simmd_step (nsteps = N_steps)
+ *   calculate_full_energy / find_kinetic_energy
+ *        src/AuxiliaryFunctions.jl:22-34, 57-65 -> simmd_energy
+ *   compute_potential_energy!
+ *        src/AuxiliaryFunctions.jl:186-196     -> simmd_potential_energy_array
+ *   NeighborListStruct.neighbor_list_half / _full (layout only)
+ *        src/DataStructs.jl:243-257            -> simmd_export_pairs
+ *   OutputStruct.N_neighbor_list_rebuilds, steps_done
+ *        src/DataStructs.jl:291-315            -> simmd_stats
+ *
+ * Array layout: every per-particle vector array is the reference's
+ * ArrayStruct field reinterpreted as Float64, i.e. AoS dims x N, particle i's
+ * components at [i*dims + k] (Julia: reinterpret(reshape, Float64, r_array)).
+ * Lists are Julia's Array{Int64,2}(maxK, N): column-major, 1-based ids.
+ *
+ * Every call returns an int status (SIMMD_OK = 0); the Julia shim raises
+ * error() on nonzero, as the reference raises on neighbour overflow
+ * (BoundsError) or a bad dimension ("To be implemented").  Calls are
+ * blocking at the ABI level unless stated; one context per host thread.
+ */
+#ifndef SIMMD_H
+#define SIMMD_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum simmd_status {
+    SIMMD_OK = 0,
+    SIMMD_ERR_BAD_ARG = 1,            /* invalid parameter (dims not 2/3, N<1, ...) */
+    SIMMD_ERR_CUDA = 2,               /* CUDA runtime error (message: simmd_last_error) */
+    SIMMD_ERR_OOM = 3,                /* device allocation failed */
+    SIMMD_ERR_NEIGHBOR_OVERFLOW = 4,  /* a particle has more than max_neighbors entries */
+    SIMMD_ERR_NONFINITE = 5,          /* NaN/Inf position or displacement */
+    SIMMD_ERR_NOISE_RANGE = 6,        /* host noise array shorter than the steps taken */
+    SIMMD_ERR_BUDGET = 7,             /* replica does not fit the memory budget / capacity */
+    SIMMD_ERR_NOT_FOUND = 8,          /* unknown replica id */
+    SIMMD_ERR_NO_DEVICE = 9           /* no CUDA device */
+};
+
+enum { SIMMD_POT_LJ = 0, SIMMD_POT_BERTHIER = 1 };
+enum { SIMMD_NEWTONIAN = 0, SIMMD_LANGEVIN = 1, SIMMD_BROWNIAN = 2 };
+enum { SIMMD_FP64 = 0, SIMMD_FP32_SPLIT = 1 };
+
+/* ParameterStruct + System + potential scalars + neighbour-list skin
+ * (src/DataStructs.jl:10-87, 138-153, 244). */
+typedef struct simmd_params {
+    int32_t dims;                /* 2 or 3 (system.dims) */
+    int32_t potential;           /* SIMMD_POT_* (interaction_potential) */
+    int32_t dynamics;            /* SIMMD_NEWTONIAN / _LANGEVIN / _BROWNIAN (typeof(system)) */
+    int32_t precision;           /* SIMMD_FP64 (reference arithmetic) or SIMMD_FP32_SPLIT */
+    int64_t N;                   /* parameters.N */
+    double box_size;             /* parameters.box_size (cubic box) */
+    double force_cutoff2;        /* parameters.force_cutoff2 = rc^2 */
+    double skin;                 /* neighborlist.skin_distance */
+    double verlet_force_cutoff;  /* force_cutoff argument of initialize_neighbor_struct (rc) */
+    double lj_eps, lj_sigma, lj_Uc;          /* LJ(eps, sigma, rc) fields */
+    double b_c0, b_c2, b_c4, b_zeta;         /* Berthier fields */
+    double kBT, gamma, dt, m;                /* system fields (gamma unused for Newtonian) */
+    int32_t rescale_temperature; /* Newtonian.rescale_temperature */
+    int32_t max_neighbors;       /* maxneighbours (rows of the list); 0 -> 200 */
+    uint64_t seed;               /* Philox key of the production noise stream */
+} simmd_params;
+
+typedef struct simmd_stats {
+    int64_t steps_done;          /* time steps taken through simmd_step */
+    int64_t rebuilds;            /* neighbour-list rebuilds (N_neighbor_list_rebuilds) */
+    int64_t noise_draws;         /* Philox counter: random-force evaluations so far */
+    int32_t max_neighbors;       /* list rows allocated */
+    int32_t max_count;           /* largest list length seen since creation */
+    int32_t overflow;            /* sticky neighbour-overflow flag */
+    int32_t nonfinite;           /* sticky NaN/Inf flag */
+    double epot, virial, ekin;   /* last values from simmd_energy */
+    int64_t list_entries;        /* force-list entries (both directions) at the last rebuild */
+} simmd_stats;
+
+typedef struct simmd_ctx simmd_ctx;
+
+const char* simmd_version(void);
+const char* simmd_status_string(int status);
+const char* simmd_last_error(void);
+int simmd_device_count(int32_t* n);
+
+/* ---- single system (drop-in; replica 0 of the context) ------------------ */
+
+/* initialize_neighbor_struct: allocate device state for one system of N
+ * particles on the current CUDA device.  The list of maxneighbours rows is
+ * allocated as in the reference. */
+int simmd_create(const simmd_params* p, simmd_ctx** out);
+int simmd_destroy(simmd_ctx* ctx);
+
+/* Copy ArrayStruct fields to the device (r, D required; v, F, disp may be
+ * NULL = zeros).  The stale F is used by the first kick, as in the reference.
+ * Schedules a list rebuild before the next force evaluation. */
+int simmd_upload(simmd_ctx* ctx, const double* r, const double* v, const double* F,
+                 const double* D, const double* disp);
+/* Overwrite positions / velocities / forces / displacements in place (any
+ * pointer may be NULL), keeping the neighbour lists and the skin bookkeeping:
+ * the ArrayStruct fields a Julia caller edited between calls. */
+int simmd_set_state(simmd_ctx* ctx, const double* r, const double* v, const double* F,
+                    const double* disp);
+/* Copy the device state back (any pointer may be NULL). */
+int simmd_download(simmd_ctx* ctx, double* r, double* v, double* F, double* disp);
+
+/* update_neighbor_lists!: rebuild every replica's lists now (resets the
+ * displacements, counts a rebuild). */
+int simmd_rebuild(simmd_ctx* ctx);
+
+/* calculate_new_forces!: pair forces + random force (Langevin: -gamma v +
+ * sqrt(2 kBT gamma/dt) xi; Brownian: sqrt(2 kBT gamma/dt) xi).  noise: host
+ * array dims x N of N(0,1) deviates for this call (NULL: Philox stream).
+ * F_out (may be NULL) receives the forces. */
+int simmd_forces(simmd_ctx* ctx, const double* noise, double* F_out);
+
+/* do_time_step x nsteps for every replica of the context.  noise: NULL for
+ * the Philox stream, or (single-replica contexts) a host array
+ * [nsteps][N][dims] of N(0,1) deviates, the reference's random_displacement
+ * for each step. */
+int simmd_step(simmd_ctx* ctx, int64_t nsteps, const double* noise);
+
+/* Set-up relaxation (not a reference routine): nsteps of steepest descent
+ * r += F with each particle's move capped at max_disp, FP64, no noise, for
+ * every replica; removes the overlaps of random initial positions before
+ * dynamics (the role of find_random_initial_configuration!'s MC sweeps,
+ * src/InitialConfiguration.jl:43-114).  Velocities are kept; F holds the
+ * last relaxation forces. */
+int simmd_relax(simmd_ctx* ctx, int64_t nsteps, double max_disp);
+
+/* calculate_full_energy (epot), virial W = sum_pairs r_ij . F_ij, and
+ * find_kinetic_energy (ekin) of replica 0; any pointer may be NULL. */
+int simmd_energy(simmd_ctx* ctx, double* epot, double* virial, double* ekin);
+
+/* compute_potential_energy!: per-particle energy (half of the pair sum). */
+int simmd_potential_energy_array(simmd_ctx* ctx, double* e);
+
+/* Lists as of the last rebuild, reference layout (maxK, N) column-major,
+ * 1-based.  which = 0: the force ("half") list, each pair once, owner = the
+ * lower particle id; which = 1: the full Verlet-sphere list (requires
+ * simmd_set_full_list(ctx, 1) before the rebuild). */
+int simmd_export_pairs(simmd_ctx* ctx, int32_t which, int64_t maxK, int64_t* counts, int64_t* list);
+int simmd_set_full_list(simmd_ctx* ctx, int32_t enable);
+
+int simmd_stats_get(simmd_ctx* ctx, simmd_stats* out);
+
+/* ---- many replicas in one context (batching / serving) ------------------ */
+
+int simmd_engine_create(int32_t device, simmd_ctx** out);
+/* Pre-size slot, cell and replica capacity (no reallocation -- and no graph
+ * re-capture -- while replicas come and go inside it). */
+int simmd_reserve(simmd_ctx* ctx, int64_t slots, int64_t cells, int32_t replicas, int32_t max_neighbors);
+int simmd_add_replica(simmd_ctx* ctx, const simmd_params* p, const double* r, const double* v,
+                      const double* F, const double* D, int32_t* rep_out);
+int simmd_remove_replica(simmd_ctx* ctx, int32_t rep);
+int simmd_upload_r(simmd_ctx* ctx, int32_t rep, const double* r, const double* v, const double* F,
+                   const double* D, const double* disp);
+int simmd_download_r(simmd_ctx* ctx, int32_t rep, double* r, double* v, double* F, double* disp);
+int simmd_set_state_r(simmd_ctx* ctx, int32_t rep, const double* r, const double* v, const double* F,
+                      const double* disp);
+/* energies of every replica (one pass), then per replica */
+int simmd_energy_all(simmd_ctx* ctx);
+int simmd_stats_r(simmd_ctx* ctx, int32_t rep, simmd_stats* out);
+/* device bytes a replica of this shape needs (admission against a budget) */
+int64_t simmd_replica_bytes(const simmd_params* p, int32_t max_neighbors);
+
+/* ---- tuning, timing, plumbing ------------------------------------------ */
+
+/* threads per particle in the force pass (1, 2, 4), CUDA-graph capture of
+ * the step loop (0/1) and steps per captured graph. */
+int simmd_set_tuning(simmd_ctx* ctx, int32_t threads_per_particle, int32_t use_graphs, int32_t graph_steps);
+int simmd_sync(simmd_ctx* ctx);
+void* simmd_stream(simmd_ctx* ctx);          /* the context's cudaStream_t */
+int simmd_timer_start(simmd_ctx* ctx);       /* CUDA event on the context stream */
+int simmd_timer_stop(simmd_ctx* ctx, float* ms);
+int64_t simmd_launch_count(simmd_ctx* ctx);  /* kernels launched by this context */
+int64_t simmd_device_bytes(simmd_ctx* ctx);  /* device memory held */
+/* time the force pass alone: nrep launches, average ms per launch (CUDA
+ * events around the launches on the context stream) */
+int simmd_time_force(simmd_ctx* ctx, int32_t nrep, float* ms_per_launch);
+/* per-kernel CUDA-event timing of simmd_step (direct launches, events around
+ * each kernel group on the context stream).  out[6] = {force ms total, force
+ * launches, kick/drift ms, rebuild ms, Brownian-update ms, steps}. */
+int simmd_set_profile(simmd_ctx* ctx, int32_t enable);
+/* page-lock a caller's host array for fast transfers (cudaHostRegister) */
+int simmd_host_register(void* ptr, int64_t bytes);
+int simmd_host_unregister(void* ptr);
+int simmd_profile_get(simmd_ctx* ctx, double* out6);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,156 @@
+"""Many independent replicas in one libsimmd context (one stream, one slot
+space, one CUDA-graph step loop): the batched front end.
+
+Each replica is a full system (its own N, dims, potential, dynamics,
+precision, box and seed).  All replicas advance together by ``step``; every
+kernel launch covers all of them, and the per-replica results are
+bit-identical to running the replica alone (same slot layout inside the
+replica, per-replica reductions in a fixed order, noise keyed by the
+replica's seed and original particle ids).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import dataclasses
+from typing import Optional
+
+import numpy as np
+
+from . import _lib
+
+
+@dataclasses.dataclass
+class ReplicaSpec:
+    """One replica: the scalars of simmd_params plus its initial arrays."""
+    dims: int
+    potential: int
+    dynamics: int
+    N: int
+    box_size: float
+    force_cutoff2: float
+    skin: float
+    verlet_force_cutoff: float
+    r: np.ndarray
+    D: np.ndarray
+    v: Optional[np.ndarray] = None
+    precision: int = _lib.FP64
+    kBT: float = 0.1
+    gamma: float = 1.0
+    dt: float = 0.005
+    m: float = 1.0
+    lj_eps: float = 1.0
+    lj_sigma: float = 1.0
+    lj_Uc: float = 0.0
+    b_c0: float = 0.0
+    b_c2: float = 0.0
+    b_c4: float = 0.0
+    b_zeta: float = 0.2
+    rescale_temperature: bool = False
+    max_neighbors: int = 200
+    seed: int = 1
+
+    def params(self) -> _lib.Params:
+        p = _lib.Params()
+        for f in ("dims", "potential", "dynamics", "precision", "N", "box_size", "force_cutoff2", "skin",
+                  "verlet_force_cutoff", "lj_eps", "lj_sigma", "lj_Uc", "b_c0", "b_c2", "b_c4", "b_zeta", "kBT",
+                  "gamma", "dt", "m", "max_neighbors", "seed"):
+            setattr(p, f, getattr(self, f))
+        p.rescale_temperature = int(bool(self.rescale_temperature))
+        return p
+
+    def device_bytes(self) -> int:
+        p = self.params()
+        return int(_lib.load().simmd_replica_bytes(C.byref(p), self.max_neighbors))
+
+
+class ReplicaBatch:
+    """A libsimmd context holding many replicas."""
+
+    def __init__(self, device: int = 0, *, tpp: int = 1, graphs: bool = True, graph_steps: int = 16):
+        self.lib = _lib.load()
+        self.ctx = C.c_void_p()
+        _lib.check(self.lib.simmd_engine_create(device, C.byref(self.ctx)))
+        _lib.check(self.lib.simmd_set_tuning(self.ctx, tpp, int(graphs), graph_steps))
+        self.specs = {}
+
+    def reserve(self, slots: int, cells: int, replicas: int, max_neighbors: int = 200):
+        _lib.check(self.lib.simmd_reserve(self.ctx, slots, cells, replicas, max_neighbors))
+
+    def add(self, spec: ReplicaSpec) -> int:
+        p = spec.params()
+        r = _lib.f64(spec.r, (spec.N, spec.dims))
+        D = _lib.f64(spec.D, (spec.N,))
+        v = _lib.f64(spec.v, (spec.N, spec.dims)) if spec.v is not None else None
+        rid = C.c_int32()
+        _lib.check(self.lib.simmd_add_replica(self.ctx, C.byref(p), _lib.ptr(r), _lib.ptr(v), None, _lib.ptr(D),
+                                              C.byref(rid)))
+        self.specs[rid.value] = spec
+        return rid.value
+
+    def remove(self, rid: int):
+        _lib.check(self.lib.simmd_remove_replica(self.ctx, rid))
+        self.specs.pop(rid, None)
+
+    def rebuild(self):
+        _lib.check(self.lib.simmd_rebuild(self.ctx))
+
+    def relax(self, nsteps: int, max_disp: float):
+        _lib.check(self.lib.simmd_relax(self.ctx, nsteps, max_disp))
+
+    def step(self, nsteps: int):
+        _lib.check(self.lib.simmd_step(self.ctx, int(nsteps), None))
+
+    def step_async_status(self, nsteps: int) -> int:
+        """step, returning the status instead of raising (serving loop)."""
+        return int(self.lib.simmd_step(self.ctx, int(nsteps), None))
+
+    def state(self, rid: int):
+        s = self.specs[rid]
+        r = np.zeros((s.N, s.dims))
+        v = np.zeros((s.N, s.dims))
+        F = np.zeros((s.N, s.dims))
+        _lib.check(self.lib.simmd_download_r(self.ctx, rid, _lib.ptr(r), _lib.ptr(v), _lib.ptr(F), None))
+        return r, v, F
+
+    def energies(self):
+        _lib.check(self.lib.simmd_energy_all(self.ctx))
+        return {rid: self.stats(rid) for rid in self.specs}
+
+    def stats(self, rid: int) -> _lib.Stats:
+        st = _lib.Stats()
+        _lib.check(self.lib.simmd_stats_r(self.ctx, rid, C.byref(st)))
+        return st
+
+    def launches(self) -> int:
+        return int(self.lib.simmd_launch_count(self.ctx))
+
+    def device_bytes(self) -> int:
+        return int(self.lib.simmd_device_bytes(self.ctx))
+
+    def timer_start(self):
+        _lib.check(self.lib.simmd_timer_start(self.ctx))
+
+    def timer_stop(self) -> float:
+        ms = C.c_float()
+        _lib.check(self.lib.simmd_timer_stop(self.ctx, C.byref(ms)))
+        return ms.value
+
+    def profile(self, enable: bool):
+        _lib.check(self.lib.simmd_set_profile(self.ctx, int(enable)))
+
+    def profile_get(self):
+        out = np.zeros(6)
+        _lib.check(self.lib.simmd_profile_get(self.ctx, _lib.ptr(out)))
+        return dict(force_ms=out[0], force_n=int(out[1]), kick_ms=out[2], rebuild_ms=out[3], update_ms=out[4],
+                    steps=int(out[5]))
+
+    def set_tuning(self, tpp: int, graphs: bool = True, graph_steps: int = 16):
+        _lib.check(self.lib.simmd_set_tuning(self.ctx, tpp, int(graphs), graph_steps))
+
+    def close(self):
+        if self.ctx:
+            self.lib.simmd_destroy(self.ctx)
+            self.ctx = None
+
+    def __del__(self):
+        self.close()

@@ -1,0 +1,1341 @@
+// engine.cu -- host runtime of libsimmd and its C ABI (include/simmd.h).
+//
+// One context = one CUDA device + one stream + a slot space shared by any
+// number of replicas (independent systems).  The host keeps the replica
+// table (slot / cell ranges from first-fit free lists), launches the kernels
+// of k_neighbor.cu, k_force.cu and k_integrate.cu in the order of the
+// reference's do_time_step, captures the step loop in a CUDA graph, and
+// turns device status flags into the ABI's status codes.
+//
+// Step sequence (all replicas of the context advance together):
+//   Newtonian/Langevin (src/MD.jl:499-554): kick1+drift -> rebuild if the
+//     skin trigger fired -> forces + random force + kick2 (+COM sum)
+//     [-> kinetic energy / rescale factor when rescale_temperature]
+//   Brownian (src/MD.jl:429-471 as intended): forces + random force (+mean
+//     force) -> position update -> rebuild if the skin trigger fired
+// The COM velocity is subtracted lazily at the next kick1 or by a finalize
+// pass at the end of each simmd_step call.
+#include "../../include/simmd.h"
+#include "simmd_internal.cuh"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+namespace simmd {
+void launch_rebuild_impl(const Batch& b, const LaunchCfg& lc, unsigned* nbr_full, int* ncnt_full, int Kfull);
+void launch_export_impl(const Batch& b, const LaunchCfg& lc, int rep, const RepDesc& hd, const unsigned* lst,
+                        const int* cnt, int T, long long* counts, long long* list, long long maxK, int half_only,
+                        int* overflow);
+void launch_force_impl(const Batch& b, const LaunchCfg& lc, int mode, int grid, double* epp);
+int force_blocks_per_sm(int T, int mode);
+void launch_kick_drift_impl(const Batch& b, const LaunchCfg& lc);
+void launch_brownian_update_impl(const Batch& b, const LaunchCfg& lc);
+void launch_rescale_impl(const Batch& b, const LaunchCfg& lc);
+void launch_kinetic_impl(const Batch& b, const LaunchCfg& lc);
+void launch_finalize_impl(const Batch& b, const LaunchCfg& lc);
+void launch_load_aos_impl(const Batch& b, const LaunchCfg& lc, int rep, const RepDesc& hd, const double* r,
+                          const double* v, const double* F, const double* D, const double* disp);
+void launch_store_aos_impl(const Batch& b, const LaunchCfg& lc, int rep, const RepDesc& hd, double* r,
+                           double* v, double* F, double* disp, const double* epp_src, double* epp);
+void launch_set_state_impl(const Batch& b, const LaunchCfg& lc, int rep, const RepDesc& hd, const double* r,
+                           const double* v, const double* F, const double* disp);
+}  // namespace simmd
+
+using namespace simmd;
+
+static thread_local std::string g_last_error;
+
+static int set_err(int code, const std::string& msg)
+{
+    g_last_error = msg;
+    return code;
+}
+
+#define CK(call)                                                                                   \
+    do {                                                                                           \
+        cudaError_t e_ = (call);                                                                   \
+        if (e_ != cudaSuccess)                                                                     \
+            return set_err(e_ == cudaErrorMemoryAllocation ? SIMMD_ERR_OOM : SIMMD_ERR_CUDA,       \
+                           std::string(#call) + ": " + cudaGetErrorString(e_));                  \
+    } while (0)
+
+struct Range {
+    long long start, len;
+};
+
+struct HostRep {
+    bool active = false;
+    simmd_params p{};
+    RepDesc d{};
+    long long steps_done = 0;
+    long long noise_draws = 0;
+    bool pending_rebuild = false;
+};
+
+struct ProfileAcc {
+    double force_ms = 0, kick_ms = 0, rebuild_ms = 0, update_ms = 0;
+    long long force_n = 0, steps = 0;
+};
+
+struct simmd_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    cudaEvent_t pev[8] = {};
+    int sm_count = 1;
+    long long S_cap = 0;
+    long long C_cap = 0;
+    int R_cap = 0;
+    int K = 0;
+    int T = 1;
+    int use_graphs = 1;
+    int graph_steps = 16;
+    int keep_full = 0;
+    int Kfull = 0;
+    int profile = 0;
+    ProfileAcc prof;
+    std::vector<HostRep> reps;
+    std::vector<Range> free_slots, free_cells;
+    Slots s{};
+    unsigned* nbr_full = nullptr;
+    int* ncnt_full = nullptr;
+    double* epp = nullptr;
+    RepDesc* d_desc = nullptr;
+    RepState* d_state = nullptr;
+    int* d_tile_rep = nullptr;
+    double* d_tile_part = nullptr;
+    int* d_queue = nullptr;
+    std::vector<int> h_tile_rep;
+    std::vector<RepState> h_state;
+    double* d_stage = nullptr;  // AoS staging, 5 arrays of stage_cap doubles
+    long long stage_cap = 0;
+    double* d_noise = nullptr;
+    long long noise_cap = 0;
+    long long bytes = 0;
+    long long launches = 0;
+    long long max_count_seen = 0;
+    // graph cache
+    cudaGraphExec_t gexec = nullptr;
+    int gkey = -1;
+    long long g_launches_per_replay = 0;
+};
+
+// ---------------------------------------------------------------------------
+// allocation helpers
+// ---------------------------------------------------------------------------
+template <typename Tp>
+static int dalloc(simmd_ctx* c, Tp** p, size_t count)
+{
+    *p = nullptr;
+    if (count == 0) return SIMMD_OK;
+    cudaError_t e = cudaMalloc((void**)p, count * sizeof(Tp));
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        *p = nullptr;
+        return set_err(SIMMD_ERR_OOM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+    }
+    c->bytes += (long long)(count * sizeof(Tp));
+    return SIMMD_OK;
+}
+
+template <typename Tp>
+static void dfree(simmd_ctx* c, Tp** p, size_t count)
+{
+    if (*p) {
+        cudaFree(*p);
+        c->bytes -= (long long)(count * sizeof(Tp));
+    }
+    *p = nullptr;
+}
+
+#define TRY(x)                        \
+    do {                              \
+        int st_ = (x);                \
+        if (st_ != SIMMD_OK) return st_; \
+    } while (0)
+
+static void invalidate_graph(simmd_ctx* c)
+{
+    if (c->gexec) cudaGraphExecDestroy(c->gexec);
+    c->gexec = nullptr;
+    c->gkey = -1;
+}
+
+// grow a per-slot array preserving [0, old)
+template <typename Tp>
+static int grow_keep(simmd_ctx* c, Tp** p, long long old_n, long long new_n)
+{
+    Tp* np = nullptr;
+    TRY(dalloc(c, &np, (size_t)new_n));
+    CK(cudaMemsetAsync(np, 0, (size_t)new_n * sizeof(Tp), c->stream));
+    if (*p && old_n > 0) CK(cudaMemcpyAsync(np, *p, (size_t)old_n * sizeof(Tp), cudaMemcpyDeviceToDevice, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    dfree(c, p, (size_t)old_n);
+    *p = np;
+    return SIMMD_OK;
+}
+
+template <typename Tp>
+static int grow_fresh(simmd_ctx* c, Tp** p, long long old_n, long long new_n)
+{
+    CK(cudaStreamSynchronize(c->stream));
+    dfree(c, p, (size_t)old_n);
+    TRY(dalloc(c, p, (size_t)new_n));
+    CK(cudaMemsetAsync(*p, 0, (size_t)new_n * sizeof(Tp), c->stream));
+    return SIMMD_OK;
+}
+
+static int force_rebuild_all(simmd_ctx* c)
+{
+    for (size_t r = 0; r < c->reps.size(); r++)
+        if (c->reps[r].active) c->reps[r].pending_rebuild = true;
+    return SIMMD_OK;
+}
+
+// (re)size everything that depends on slot capacity S, list rows K, T
+static int ensure_capacity(simmd_ctx* c, long long S_need, long long C_need, int R_need, int K_need)
+{
+    S_need = (S_need + TILE - 1) / TILE * TILE;
+    if (K_need < 1) K_need = 1;
+    K_need = (K_need + c->T - 1) / c->T * c->T;
+    bool grow_s = S_need > c->S_cap;
+    bool grow_c = C_need > c->C_cap;
+    bool grow_r = R_need > c->R_cap;
+    bool grow_k = K_need > c->K;
+    if (!grow_s && !grow_c && !grow_r && !grow_k) return SIMMD_OK;
+    invalidate_graph(c);
+    long long S_old = c->S_cap, S_new = grow_s ? std::max(S_need, S_old + S_old / 2) : S_old;
+    S_new = (S_new + TILE - 1) / TILE * TILE;
+    if (grow_s) {
+        Slots& s = c->s;
+        TRY(grow_keep(c, &s.posD, S_old, S_new));
+        TRY(grow_keep(c, &s.vx, S_old, S_new));
+        TRY(grow_keep(c, &s.vy, S_old, S_new));
+        TRY(grow_keep(c, &s.vz, S_old, S_new));
+        TRY(grow_keep(c, &s.fx, S_old, S_new));
+        TRY(grow_keep(c, &s.fy, S_old, S_new));
+        TRY(grow_keep(c, &s.fz, S_old, S_new));
+        TRY(grow_keep(c, &s.ux, S_old, S_new));
+        TRY(grow_keep(c, &s.uy, S_old, S_new));
+        TRY(grow_keep(c, &s.uz, S_old, S_new));
+        TRY(grow_keep(c, &s.off, S_old, S_new));
+        TRY(grow_keep(c, &s.cellc, S_old, S_new));
+        TRY(grow_keep(c, &s.orig, S_old, S_new));
+        TRY(grow_fresh(c, &s.ncnt, S_old, S_new));
+        TRY(grow_fresh(c, &s.bin_cell, S_old, S_new));
+        TRY(grow_fresh(c, &s.bin_rank, S_old, S_new));
+        TRY(grow_fresh(c, &s.src, S_old, S_new));
+        TRY(grow_fresh(c, &s.t_posD, S_old, S_new));
+        TRY(grow_fresh(c, &s.t_vx, S_old, S_new));
+        TRY(grow_fresh(c, &s.t_vy, S_old, S_new));
+        TRY(grow_fresh(c, &s.t_vz, S_old, S_new));
+        TRY(grow_fresh(c, &s.t_fx, S_old, S_new));
+        TRY(grow_fresh(c, &s.t_fy, S_old, S_new));
+        TRY(grow_fresh(c, &s.t_fz, S_old, S_new));
+        TRY(grow_fresh(c, &s.t_orig, S_old, S_new));
+        TRY(grow_fresh(c, &c->epp, S_old, S_new));
+        long long nt_old = S_old / TILE, nt_new = S_new / TILE;
+        TRY(grow_fresh(c, &c->d_tile_part, nt_old * NPART, nt_new * NPART));
+        TRY(grow_keep(c, &c->d_tile_rep, nt_old, nt_new));
+        c->h_tile_rep.resize((size_t)nt_new, -1);
+        CK(cudaMemcpyAsync(c->d_tile_rep, c->h_tile_rep.data(), sizeof(int) * nt_new, cudaMemcpyHostToDevice,
+                           c->stream));
+        // free-list: the new tail
+        c->free_slots.push_back({S_old, S_new - S_old});
+        c->S_cap = S_new;
+    }
+    int K_new = grow_k ? K_need : c->K;
+    if (grow_s || grow_k) {
+        dfree(c, &c->s.nbr, (size_t)S_old * (size_t)c->K);
+        TRY(dalloc(c, &c->s.nbr, (size_t)c->S_cap * (size_t)K_new));
+        c->K = K_new;
+        if (c->keep_full) {
+            dfree(c, &c->nbr_full, (size_t)S_old * (size_t)c->Kfull);
+            dfree(c, &c->ncnt_full, (size_t)S_old);
+            c->Kfull = std::max(c->K, c->Kfull);
+            TRY(dalloc(c, &c->nbr_full, (size_t)c->S_cap * (size_t)c->Kfull));
+            TRY(dalloc(c, &c->ncnt_full, (size_t)c->S_cap));
+        }
+        force_rebuild_all(c);
+    }
+    if (grow_c) {
+        long long C_old = c->C_cap, C_new = std::max(C_need, C_old + C_old / 2);
+        TRY(grow_fresh(c, &c->s.cell_count, C_old, C_new));
+        TRY(grow_fresh(c, &c->s.cell_start, C_old, C_new));
+        c->free_cells.push_back({C_old, C_new - C_old});
+        c->C_cap = C_new;
+        force_rebuild_all(c);
+    }
+    if (grow_r) {
+        int R_old = c->R_cap, R_new = std::max(R_need, R_old + R_old / 2 + 1);
+        TRY(grow_keep(c, &c->d_desc, R_old, R_new));
+        TRY(grow_keep(c, &c->d_state, R_old, R_new));
+        c->reps.resize(R_new);
+        c->h_state.resize(R_new);
+        c->R_cap = R_new;
+    }
+    // merge adjacent free ranges
+    for (auto* fl : {&c->free_slots, &c->free_cells}) {
+        std::sort(fl->begin(), fl->end(), [](const Range& a, const Range& b) { return a.start < b.start; });
+        std::vector<Range> m;
+        for (auto& r : *fl) {
+            if (r.len <= 0) continue;
+            if (!m.empty() && m.back().start + m.back().len == r.start) m.back().len += r.len;
+            else m.push_back(r);
+        }
+        *fl = m;
+    }
+    return SIMMD_OK;
+}
+
+static bool take_range(std::vector<Range>& fl, long long len, long long* start)
+{
+    for (size_t k = 0; k < fl.size(); k++) {
+        if (fl[k].len >= len) {
+            *start = fl[k].start;
+            fl[k].start += len;
+            fl[k].len -= len;
+            if (fl[k].len == 0) fl.erase(fl.begin() + (long)k);
+            return true;
+        }
+    }
+    return false;
+}
+
+static void give_range(std::vector<Range>& fl, long long start, long long len)
+{
+    fl.push_back({start, len});
+    std::sort(fl.begin(), fl.end(), [](const Range& a, const Range& b) { return a.start < b.start; });
+    std::vector<Range> m;
+    for (auto& r : fl) {
+        if (!m.empty() && m.back().start + m.back().len == r.start) m.back().len += r.len;
+        else m.push_back(r);
+    }
+    fl = m;
+}
+
+static Batch make_batch(simmd_ctx* c)
+{
+    Batch b{};
+    b.desc = c->d_desc;
+    b.state = c->d_state;
+    b.tile_rep = c->d_tile_rep;
+    b.ntiles = (int)(c->S_cap / TILE);
+    b.nreps = c->R_cap;
+    b.S = c->S_cap;
+    b.K = c->K;
+    b.tpp = c->T;
+    b.s = c->s;
+    b.tile_part = c->d_tile_part;
+    b.queue = c->d_queue;
+    return b;
+}
+
+static LaunchCfg make_lc(simmd_ctx* c, int mode)
+{
+    LaunchCfg lc{};
+    lc.stream = c->stream;
+    long long nt = c->S_cap / TILE;
+    lc.grid_stream = (int)std::max(1LL, std::min(nt, (long long)c->sm_count * 16));
+    lc.grid_force = c->sm_count * force_blocks_per_sm(c->T, mode);
+    lc.launches = &c->launches;
+    return lc;
+}
+
+// ---------------------------------------------------------------------------
+// replica descriptors
+// ---------------------------------------------------------------------------
+static int validate(const simmd_params* p)
+{
+    if (!p) return set_err(SIMMD_ERR_BAD_ARG, "params is NULL");
+    if (p->dims != 2 && p->dims != 3) return set_err(SIMMD_ERR_BAD_ARG, "dims must be 2 or 3 (To be implemented)");
+    if (p->N < 1 || p->N > (1LL << 24)) return set_err(SIMMD_ERR_BAD_ARG, "N out of range [1, 2^24]");
+    if (p->potential != SIMMD_POT_LJ && p->potential != SIMMD_POT_BERTHIER)
+        return set_err(SIMMD_ERR_BAD_ARG, "unknown potential");
+    if (p->dynamics < SIMMD_NEWTONIAN || p->dynamics > SIMMD_BROWNIAN)
+        return set_err(SIMMD_ERR_BAD_ARG, "unknown dynamics");
+    if (p->precision != SIMMD_FP64 && p->precision != SIMMD_FP32_SPLIT)
+        return set_err(SIMMD_ERR_BAD_ARG, "unknown precision");
+    if (!(p->box_size > 0) || !(p->force_cutoff2 > 0) || !(p->skin >= 0) || !(p->dt > 0))
+        return set_err(SIMMD_ERR_BAD_ARG, "box_size, force_cutoff2, dt must be > 0 and skin >= 0");
+    if (p->dynamics != SIMMD_NEWTONIAN && !(p->gamma > 0)) return set_err(SIMMD_ERR_BAD_ARG, "gamma must be > 0");
+    if (p->dynamics != SIMMD_BROWNIAN && !(p->m > 0)) return set_err(SIMMD_ERR_BAD_ARG, "m must be > 0");
+    return SIMMD_OK;
+}
+
+static int fill_desc(const simmd_params* p, const double* D, RepDesc& d)
+{
+    double smax = D[0];
+    for (long long i = 1; i < p->N; i++) smax = std::max(smax, D[i]);
+    if (!(smax > 0)) return set_err(SIMMD_ERR_BAD_ARG, "diameters must be positive");
+    double rc_v = p->verlet_force_cutoff > 0 ? p->verlet_force_cutoff : std::sqrt(p->force_cutoff2);
+    double rv = p->skin + rc_v * smax;  // verlet_sphere_size, src/DataStructs.jl:351-352
+    double L = p->box_size;
+    if (!(rv < 0.5 * L)) return set_err(SIMMD_ERR_BAD_ARG, "Verlet sphere (skin + rc*max(D)) must be < box/2");
+    long long nc = (long long)std::floor(L / rv);
+    if (nc < 3) nc = 1;
+    if (nc > MAX_CELLS_AXIS) nc = MAX_CELLS_AXIS;
+    memset(&d, 0, sizeof(d));
+    d.n = (int)p->N;
+    d.npad = (int)((p->N + TILE - 1) / TILE * TILE);
+    d.ntiles = d.npad / TILE;
+    d.dims = p->dims;
+    d.pot = p->potential;
+    d.dyn = p->dynamics;
+    d.prec = p->precision;
+    d.nc = (int)nc;
+    d.ncell = (int)(p->dims == 3 ? nc * nc * nc : nc * nc);
+    d.rescale = (p->dynamics == SIMMD_NEWTONIAN && p->rescale_temperature) ? 1 : 0;
+    d.noise_mode = NOISE_PHILOX;
+    d.active = 1;
+    d.L = L;
+    d.halfL = L * 0.5;
+    d.cs = L / (double)nc;
+    d.inv_cs = (double)nc / L;
+    d.rc2 = p->force_cutoff2;
+    d.rcut = std::sqrt(p->force_cutoff2);
+    d.skin = p->skin;
+    d.rv2 = rv * rv;
+    double h = p->skin / 2.0;
+    d.skin_half2 = h * h;
+    d.sigma2 = p->lj_sigma * p->lj_sigma;
+    d.sigma4 = d.sigma2 * d.sigma2;
+    d.lj_cut2 = (p->dims == 3) ? d.rc2 * d.sigma2 : d.rc2 * d.sigma4;
+    d.eps = p->lj_eps;
+    d.Uc = p->lj_Uc;
+    d.c0 = p->b_c0;
+    d.c2 = p->b_c2;
+    d.c4 = p->b_c4;
+    d.zeta = p->b_zeta;
+    d.kBT = p->kBT;
+    d.gamma = p->gamma;
+    d.dt = p->dt;
+    d.m = p->m;
+    d.noise_factor = (p->dynamics == SIMMD_NEWTONIAN) ? 0.0 : std::sqrt(2.0 * p->kBT * p->gamma / p->dt);
+    d.dt_over_gamma = (p->dynamics == SIMMD_BROWNIAN) ? p->dt / p->gamma : 0.0;
+    d.two_m = 2.0 * p->m;
+    d.m_half = p->m / 2.0;
+    d.Lf = (float)L;
+    d.halfLf = (float)(L * 0.5);
+    d.csf = (float)d.cs;
+    d.rc2f = (float)d.rc2;
+    d.rcutf = (float)d.rcut;
+    d.skinf = (float)d.skin;
+    d.sigma2f = (float)d.sigma2;
+    d.sigma4f = (float)d.sigma4;
+    d.cut2f = (float)d.lj_cut2;
+    d.epsf = (float)d.eps;
+    d.Ucf = (float)d.Uc;
+    d.c0f = (float)d.c0;
+    d.c2f = (float)d.c2;
+    d.c4f = (float)d.c4;
+    d.zetaf = (float)d.zeta;
+    d.seed = p->seed;
+    return SIMMD_OK;
+}
+
+static int push_desc(simmd_ctx* c, int r)
+{
+    CK(cudaMemcpyAsync(c->d_desc + r, &c->reps[r].d, sizeof(RepDesc), cudaMemcpyHostToDevice, c->stream));
+    return SIMMD_OK;
+}
+
+static int set_tiles(simmd_ctx* c, int r, int value)
+{
+    const RepDesc& d = c->reps[r].d;
+    for (int t = 0; t < d.ntiles; t++) c->h_tile_rep[d.tile0 + t] = value;
+    CK(cudaMemcpyAsync(c->d_tile_rep + d.tile0, c->h_tile_rep.data() + d.tile0, sizeof(int) * d.ntiles,
+                       cudaMemcpyHostToDevice, c->stream));
+    return SIMMD_OK;
+}
+
+static int ensure_stage(simmd_ctx* c, long long n)
+{
+    if (n <= c->stage_cap) return SIMMD_OK;
+    CK(cudaStreamSynchronize(c->stream));
+    dfree(c, &c->d_stage, (size_t)(5 * c->stage_cap));
+    long long cap = std::max(n, c->stage_cap * 2);
+    TRY(dalloc(c, &c->d_stage, (size_t)(5 * cap)));
+    c->stage_cap = cap;
+    return SIMMD_OK;
+}
+
+static int reset_state(simmd_ctx* c, int r, bool keep_counters)
+{
+    RepState st{};
+    if (keep_counters) {
+        CK(cudaMemcpyAsync(&st, c->d_state + r, sizeof(RepState), cudaMemcpyDeviceToHost, c->stream));
+        CK(cudaStreamSynchronize(c->stream));
+    }
+    long long step = keep_counters ? st.step : 0, rb = keep_counters ? st.rebuilds : 0;
+    int mc = keep_counters ? st.maxcount : 0;
+    memset(&st, 0, sizeof(st));
+    st.step = step;
+    st.rebuilds = rb;
+    st.maxcount = mc;
+    st.vscale = 1.0;
+    st.force_rebuild = 1;
+    CK(cudaMemcpyAsync(c->d_state + r, &st, sizeof(RepState), cudaMemcpyHostToDevice, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    c->h_state[r] = st;
+    c->reps[r].pending_rebuild = true;
+    return SIMMD_OK;
+}
+
+static int upload_rep(simmd_ctx* c, int r, const double* rr, const double* v, const double* F, const double* D,
+                      const double* disp)
+{
+    HostRep& h = c->reps[r];
+    const long long nd = h.p.N * h.p.dims;
+    TRY(ensure_stage(c, std::max<long long>(nd, (long long)h.p.N)));
+    double* st = c->d_stage;
+    double *dr = st, *dv = st + c->stage_cap, *dF = st + 2 * c->stage_cap, *dD = st + 3 * c->stage_cap,
+           *du = st + 4 * c->stage_cap;
+    CK(cudaMemcpyAsync(dr, rr, sizeof(double) * nd, cudaMemcpyHostToDevice, c->stream));
+    if (v) CK(cudaMemcpyAsync(dv, v, sizeof(double) * nd, cudaMemcpyHostToDevice, c->stream));
+    if (F) CK(cudaMemcpyAsync(dF, F, sizeof(double) * nd, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(dD, D, sizeof(double) * h.p.N, cudaMemcpyHostToDevice, c->stream));
+    if (disp) CK(cudaMemcpyAsync(du, disp, sizeof(double) * nd, cudaMemcpyHostToDevice, c->stream));
+    Batch b = make_batch(c);
+    LaunchCfg lc = make_lc(c, FMODE_STEP);
+    launch_load_aos_impl(b, lc, r, h.d, dr, v ? dv : nullptr, F ? dF : nullptr, dD, disp ? du : nullptr);
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(c->stream));
+    return SIMMD_OK;
+}
+
+static int add_replica(simmd_ctx* c, const simmd_params* p, const double* r, const double* v, const double* F,
+                       const double* D, int* out)
+{
+    TRY(validate(p));
+    if (!r || !D) return set_err(SIMMD_ERR_BAD_ARG, "r and D are required");
+    RepDesc d;
+    TRY(fill_desc(p, D, d));
+    int K_need = p->max_neighbors > 0 ? p->max_neighbors : 200;
+    // find a replica id
+    int rid = -1;
+    for (int k = 0; k < c->R_cap; k++)
+        if (!c->reps[k].active) { rid = k; break; }
+    int R_need = rid < 0 ? c->R_cap + 1 : c->R_cap;
+    long long start = 0, cstart = 0;
+    bool have_s = take_range(c->free_slots, d.npad, &start);
+    bool have_c = take_range(c->free_cells, d.ncell + 1, &cstart);
+    if (have_s) give_range(c->free_slots, start, d.npad);
+    if (have_c) give_range(c->free_cells, cstart, d.ncell + 1);
+    long long S_need = have_s ? c->S_cap : c->S_cap + d.npad;
+    long long C_need = have_c ? c->C_cap : c->C_cap + d.ncell + 1;
+    TRY(ensure_capacity(c, S_need, C_need, R_need, std::max(K_need, c->K)));
+    if (rid < 0)
+        for (int k = 0; k < c->R_cap; k++)
+            if (!c->reps[k].active) { rid = k; break; }
+    if (!take_range(c->free_slots, d.npad, &start)) return set_err(SIMMD_ERR_BUDGET, "slot allocation failed");
+    if (!take_range(c->free_cells, d.ncell + 1, &cstart)) {
+        give_range(c->free_slots, start, d.npad);
+        return set_err(SIMMD_ERR_BUDGET, "cell allocation failed");
+    }
+    d.slot0 = start;
+    d.tile0 = (int)(start / TILE);
+    d.cell0 = (int)cstart;
+    HostRep& h = c->reps[rid];
+    h = HostRep();
+    h.active = true;
+    h.p = *p;
+    h.d = d;
+    TRY(push_desc(c, rid));
+    TRY(reset_state(c, rid, false));
+    TRY(upload_rep(c, rid, r, v, F, D, nullptr));
+    TRY(set_tiles(c, rid, rid));
+    CK(cudaStreamSynchronize(c->stream));
+    *out = rid;
+    return SIMMD_OK;
+}
+
+static int remove_replica(simmd_ctx* c, int rid)
+{
+    if (rid < 0 || rid >= c->R_cap || !c->reps[rid].active) return set_err(SIMMD_ERR_NOT_FOUND, "no such replica");
+    HostRep& h = c->reps[rid];
+    TRY(set_tiles(c, rid, -1));
+    h.d.active = 0;
+    TRY(push_desc(c, rid));
+    give_range(c->free_slots, h.d.slot0, h.d.npad);
+    give_range(c->free_cells, h.d.cell0, h.d.ncell + 1);
+    h.active = false;
+    CK(cudaStreamSynchronize(c->stream));
+    return SIMMD_OK;
+}
+
+// ---------------------------------------------------------------------------
+// step sequencing
+// ---------------------------------------------------------------------------
+struct Mix {
+    bool nl = false, br = false, rescale = false, noise = false;
+};
+
+static Mix batch_mix(simmd_ctx* c)
+{
+    Mix m;
+    for (auto& h : c->reps) {
+        if (!h.active) continue;
+        if (h.p.dynamics == SIMMD_BROWNIAN) m.br = true;
+        else m.nl = true;
+        if (h.d.rescale) m.rescale = true;
+        if (h.p.dynamics != SIMMD_NEWTONIAN) m.noise = true;
+    }
+    return m;
+}
+
+static void rebuild_launch(simmd_ctx* c, const Batch& b, const LaunchCfg& lc)
+{
+    launch_rebuild_impl(b, lc, c->keep_full ? c->nbr_full : nullptr, c->keep_full ? c->ncnt_full : nullptr,
+                        c->Kfull);
+}
+
+static void enqueue_step(simmd_ctx* c, const Batch& b, const LaunchCfg& lc, const Mix& m, int fmode)
+{
+    const bool prof = c->profile != 0;
+    if (m.nl) {
+        if (prof) cudaEventRecord(c->pev[0], c->stream);
+        launch_kick_drift_impl(b, lc);
+        if (prof) cudaEventRecord(c->pev[1], c->stream);
+        rebuild_launch(c, b, lc);
+        if (prof) cudaEventRecord(c->pev[2], c->stream);
+    }
+    if (prof) cudaEventRecord(c->pev[3], c->stream);
+    launch_force_impl(b, lc, fmode, lc.grid_force, nullptr);
+    if (prof) cudaEventRecord(c->pev[4], c->stream);
+    if (m.rescale) launch_rescale_impl(b, lc);
+    if (m.br) {
+        if (prof) cudaEventRecord(c->pev[5], c->stream);
+        launch_brownian_update_impl(b, lc);
+        if (prof) cudaEventRecord(c->pev[6], c->stream);
+        rebuild_launch(c, b, lc);
+        if (prof) cudaEventRecord(c->pev[7], c->stream);
+    }
+    if (prof) {
+        cudaStreamSynchronize(c->stream);
+        float ms = 0;
+        if (m.nl) {
+            cudaEventElapsedTime(&ms, c->pev[0], c->pev[1]);
+            c->prof.kick_ms += ms;
+            cudaEventElapsedTime(&ms, c->pev[1], c->pev[2]);
+            c->prof.rebuild_ms += ms;
+        }
+        cudaEventElapsedTime(&ms, c->pev[3], c->pev[4]);
+        c->prof.force_ms += ms;
+        c->prof.force_n += 1;
+        if (m.br) {
+            cudaEventElapsedTime(&ms, c->pev[5], c->pev[6]);
+            c->prof.update_ms += ms;
+            cudaEventElapsedTime(&ms, c->pev[6], c->pev[7]);
+            c->prof.rebuild_ms += ms;
+        }
+        c->prof.steps += 1;
+    }
+}
+
+static int pending_rebuilds(simmd_ctx* c)
+{
+    bool any = false;
+    for (int r = 0; r < c->R_cap; r++) {
+        HostRep& h = c->reps[r];
+        if (h.active && h.pending_rebuild) {
+            int one = 1;
+            CK(cudaMemcpyAsync(&c->d_state[r].force_rebuild, &one, sizeof(int), cudaMemcpyHostToDevice, c->stream));
+            h.pending_rebuild = false;
+            any = true;
+        }
+    }
+    if (any) {
+        Batch b = make_batch(c);
+        LaunchCfg lc = make_lc(c, FMODE_STEP);
+        rebuild_launch(c, b, lc);
+        CK(cudaGetLastError());
+    }
+    return SIMMD_OK;
+}
+
+static int read_states(simmd_ctx* c)
+{
+    CK(cudaMemcpyAsync(c->h_state.data(), c->d_state, sizeof(RepState) * c->R_cap, cudaMemcpyDeviceToHost,
+                       c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    int st = SIMMD_OK;
+    for (int r = 0; r < c->R_cap; r++) {
+        if (!c->reps[r].active) continue;
+        const RepState& s = c->h_state[r];
+        c->max_count_seen = std::max<long long>(c->max_count_seen, s.maxcount);
+        if (s.overflow && st == SIMMD_OK)
+            st = set_err(SIMMD_ERR_NEIGHBOR_OVERFLOW, "neighbour list overflow: raise max_neighbors");
+        if (s.nonfinite && st == SIMMD_OK) st = set_err(SIMMD_ERR_NONFINITE, "non-finite position or displacement");
+        if (s.noise_range_error && st == SIMMD_OK) st = set_err(SIMMD_ERR_NOISE_RANGE, "host noise array too short");
+    }
+    return st;
+}
+
+static int graph_key(const Mix& m, int fmode) { return (m.nl ? 1 : 0) | (m.br ? 2 : 0) | (m.rescale ? 4 : 0) | (fmode << 3); }
+
+static int run_steps(simmd_ctx* c, long long nsteps, const double* noise)
+{
+    if (nsteps < 0) return set_err(SIMMD_ERR_BAD_ARG, "nsteps < 0");
+    int nact = 0, single = -1;
+    for (int r = 0; r < c->R_cap; r++)
+        if (c->reps[r].active) { nact++; single = r; }
+    if (nact == 0) return SIMMD_OK;
+    TRY(pending_rebuilds(c));
+    Mix m = batch_mix(c);
+    Batch b = make_batch(c);
+    const int fmode = FMODE_STEP;
+    LaunchCfg lc = make_lc(c, fmode);
+    if (noise && m.noise) {
+        if (nact != 1) return set_err(SIMMD_ERR_BAD_ARG, "host noise requires a single-replica context");
+        HostRep& h = c->reps[single];
+        long long nd = nsteps * h.p.N * h.p.dims;
+        if (nd > c->noise_cap) {
+            CK(cudaStreamSynchronize(c->stream));
+            dfree(c, &c->d_noise, (size_t)c->noise_cap);
+            TRY(dalloc(c, &c->d_noise, (size_t)nd));
+            c->noise_cap = nd;
+        }
+        CK(cudaMemcpyAsync(c->d_noise, noise, sizeof(double) * nd, cudaMemcpyHostToDevice, c->stream));
+        CK(cudaMemcpyAsync(&c->h_state[single], c->d_state + single, sizeof(RepState), cudaMemcpyDeviceToHost,
+                           c->stream));
+        CK(cudaStreamSynchronize(c->stream));
+        h.d.noise_mode = NOISE_HOST;
+        h.d.host_noise = c->d_noise;
+        h.d.noise_step0 = c->h_state[single].step;
+        h.d.noise_nsteps = (int)nsteps;
+        TRY(push_desc(c, single));
+        for (long long s = 0; s < nsteps; s++) enqueue_step(c, b, lc, m, fmode);
+        CK(cudaGetLastError());
+        h.d.noise_mode = NOISE_PHILOX;
+        h.d.host_noise = nullptr;
+        TRY(push_desc(c, single));
+    } else if (c->use_graphs && !c->profile && nsteps >= c->graph_steps) {
+        int key = graph_key(m, fmode);
+        if (!c->gexec || c->gkey != key) {
+            invalidate_graph(c);
+            cudaGraph_t g;
+            long long l0 = c->launches;
+            CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+            for (int s = 0; s < c->graph_steps; s++) enqueue_step(c, b, lc, m, fmode);
+            cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+            c->g_launches_per_replay = c->launches - l0;
+            c->launches = l0;
+            CK(e);
+            e = cudaGraphInstantiate(&c->gexec, g, 0);
+            cudaGraphDestroy(g);
+            CK(e);
+            c->gkey = key;
+        }
+        long long reps = nsteps / c->graph_steps;
+        for (long long k = 0; k < reps; k++) {
+            CK(cudaGraphLaunch(c->gexec, c->stream));
+            c->launches += c->g_launches_per_replay;
+        }
+        for (long long s = reps * c->graph_steps; s < nsteps; s++) enqueue_step(c, b, lc, m, fmode);
+        CK(cudaGetLastError());
+    } else {
+        for (long long s = 0; s < nsteps; s++) enqueue_step(c, b, lc, m, fmode);
+        CK(cudaGetLastError());
+    }
+    if (m.nl) launch_finalize_impl(b, lc);
+    CK(cudaGetLastError());
+    for (int r = 0; r < c->R_cap; r++)
+        if (c->reps[r].active) c->reps[r].steps_done += nsteps;
+    return read_states(c);
+}
+
+// ---------------------------------------------------------------------------
+// C ABI
+// ---------------------------------------------------------------------------
+extern "C" {
+
+const char* simmd_version(void) { return "simmd 0.1.0 (sm_103a)"; }
+
+const char* simmd_status_string(int status)
+{
+    switch (status) {
+        case SIMMD_OK: return "ok";
+        case SIMMD_ERR_BAD_ARG: return "bad argument";
+        case SIMMD_ERR_CUDA: return "CUDA error";
+        case SIMMD_ERR_OOM: return "out of device memory";
+        case SIMMD_ERR_NEIGHBOR_OVERFLOW: return "neighbour list overflow";
+        case SIMMD_ERR_NONFINITE: return "non-finite state";
+        case SIMMD_ERR_NOISE_RANGE: return "noise array too short";
+        case SIMMD_ERR_BUDGET: return "capacity or budget exceeded";
+        case SIMMD_ERR_NOT_FOUND: return "replica not found";
+        case SIMMD_ERR_NO_DEVICE: return "no CUDA device";
+        default: return "unknown status";
+    }
+}
+
+const char* simmd_last_error(void) { return g_last_error.c_str(); }
+
+int simmd_device_count(int32_t* n)
+{
+    int k = 0;
+    cudaError_t e = cudaGetDeviceCount(&k);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        k = 0;
+    }
+    if (n) *n = k;
+    return SIMMD_OK;
+}
+
+int simmd_engine_create(int32_t device, simmd_ctx** out)
+{
+    if (!out) return set_err(SIMMD_ERR_BAD_ARG, "out is NULL");
+    *out = nullptr;
+    int nd = 0;
+    if (cudaGetDeviceCount(&nd) != cudaSuccess || nd == 0) {
+        cudaGetLastError();
+        return set_err(SIMMD_ERR_NO_DEVICE, "no CUDA device");
+    }
+    if (device < 0 || device >= nd) return set_err(SIMMD_ERR_BAD_ARG, "bad device index");
+    CK(cudaSetDevice(device));
+    simmd_ctx* c = new simmd_ctx();
+    c->device = device;
+    cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, device);
+    if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreate(&c->ev0) != cudaSuccess || cudaEventCreate(&c->ev1) != cudaSuccess) {
+        delete c;
+        return set_err(SIMMD_ERR_CUDA, "stream/event creation failed");
+    }
+    for (auto& e : c->pev) cudaEventCreate(&e);
+    int st = dalloc(c, &c->d_queue, 4);
+    if (st == SIMMD_OK) st = cudaMemsetAsync(c->d_queue, 0, 4 * sizeof(int), c->stream) == cudaSuccess ? 0 : SIMMD_ERR_CUDA;
+    if (st != SIMMD_OK) {
+        delete c;
+        return st;
+    }
+    *out = c;
+    return SIMMD_OK;
+}
+
+static void destroy_ctx(simmd_ctx* c)
+{
+    cudaSetDevice(c->device);
+    cudaStreamSynchronize(c->stream);
+    invalidate_graph(c);
+    Slots& s = c->s;
+    void* ptrs[] = {s.posD, s.vx, s.vy, s.vz, s.fx, s.fy, s.fz, s.ux, s.uy, s.uz, s.off, s.cellc, s.orig, s.nbr,
+                    s.ncnt, s.bin_cell, s.bin_rank, s.src, s.t_posD, s.t_vx, s.t_vy, s.t_vz, s.t_fx, s.t_fy,
+                    s.t_fz, s.t_orig, s.cell_count, s.cell_start, c->nbr_full, c->ncnt_full, c->epp, c->d_desc,
+                    c->d_state, c->d_tile_rep, c->d_tile_part, c->d_queue, c->d_stage, c->d_noise};
+    for (void* p : ptrs)
+        if (p) cudaFree(p);
+    cudaEventDestroy(c->ev0);
+    cudaEventDestroy(c->ev1);
+    for (auto& e : c->pev) cudaEventDestroy(e);
+    cudaStreamDestroy(c->stream);
+    delete c;
+}
+
+int simmd_destroy(simmd_ctx* ctx)
+{
+    if (ctx) destroy_ctx(ctx);
+    return SIMMD_OK;
+}
+
+int simmd_create(const simmd_params* p, simmd_ctx** out)
+{
+    TRY(validate(p));
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaGetLastError();
+    TRY(simmd_engine_create(dev, out));
+    simmd_ctx* c = *out;
+    // reserve the single system's shape; data arrive with simmd_upload
+    RepDesc d;
+    std::vector<double> ones((size_t)p->N, p->potential == SIMMD_POT_LJ ? p->lj_sigma : 1.0);
+    int st = fill_desc(p, ones.data(), d);
+    if (st == SIMMD_OK) st = ensure_capacity(c, d.npad, (long long)d.ncell * 8 + 64, 1,
+                                             p->max_neighbors > 0 ? p->max_neighbors : 200);
+    if (st != SIMMD_OK) {
+        destroy_ctx(c);
+        *out = nullptr;
+        return st;
+    }
+    c->reps[0].p = *p;  // placeholder until upload (inactive)
+    return SIMMD_OK;
+}
+
+int simmd_upload_r(simmd_ctx* c, int32_t rep, const double* r, const double* v, const double* F, const double* D,
+                   const double* disp)
+{
+    if (!c || !r || !D) return set_err(SIMMD_ERR_BAD_ARG, "NULL argument");
+    CK(cudaSetDevice(c->device));
+    if (rep < 0 || rep >= c->R_cap) return set_err(SIMMD_ERR_NOT_FOUND, "no such replica");
+    HostRep& h = c->reps[rep];
+    if (!h.active) {
+        // first upload of a simmd_create context: becomes replica 0
+        simmd_params p = h.p;
+        int rid = -1;
+        TRY(add_replica(c, &p, r, v, F, D, &rid));
+        if (rid != rep) return set_err(SIMMD_ERR_NOT_FOUND, "replica id mismatch");
+        if (disp) TRY(upload_rep(c, rid, r, v, F, D, disp));
+        return SIMMD_OK;
+    }
+    // the Verlet radius depends on max(D): refresh the descriptor and cells
+    RepDesc d;
+    TRY(fill_desc(&h.p, D, d));
+    if (d.ncell != h.d.ncell) {
+        give_range(c->free_cells, h.d.cell0, h.d.ncell + 1);
+        long long cstart;
+        if (!take_range(c->free_cells, d.ncell + 1, &cstart)) {
+            TRY(ensure_capacity(c, c->S_cap, c->C_cap + d.ncell + 1, c->R_cap, c->K));
+            if (!take_range(c->free_cells, d.ncell + 1, &cstart)) return set_err(SIMMD_ERR_BUDGET, "cells");
+        }
+        d.cell0 = (int)cstart;
+    } else {
+        d.cell0 = h.d.cell0;
+    }
+    d.slot0 = h.d.slot0;
+    d.tile0 = h.d.tile0;
+    h.d = d;
+    TRY(push_desc(c, rep));
+    TRY(reset_state(c, rep, true));
+    return upload_rep(c, rep, r, v, F, D, disp);
+}
+
+int simmd_upload(simmd_ctx* c, const double* r, const double* v, const double* F, const double* D,
+                 const double* disp)
+{
+    return simmd_upload_r(c, 0, r, v, F, D, disp);
+}
+
+int simmd_download_r(simmd_ctx* c, int32_t rep, double* r, double* v, double* F, double* disp)
+{
+    if (!c) return set_err(SIMMD_ERR_BAD_ARG, "NULL context");
+    CK(cudaSetDevice(c->device));
+    if (rep < 0 || rep >= c->R_cap || !c->reps[rep].active) return set_err(SIMMD_ERR_NOT_FOUND, "no such replica");
+    HostRep& h = c->reps[rep];
+    const long long nd = h.p.N * h.p.dims;
+    TRY(ensure_stage(c, std::max<long long>(nd, (long long)h.p.N)));
+    double* st = c->d_stage;
+    double *dr = st, *dv = st + c->stage_cap, *dF = st + 2 * c->stage_cap, *du = st + 4 * c->stage_cap;
+    Batch b = make_batch(c);
+    LaunchCfg lc = make_lc(c, FMODE_STEP);
+    launch_store_aos_impl(b, lc, rep, h.d, r ? dr : nullptr, v ? dv : nullptr, F ? dF : nullptr,
+                          disp ? du : nullptr, nullptr, nullptr);
+    CK(cudaGetLastError());
+    if (r) CK(cudaMemcpyAsync(r, dr, sizeof(double) * nd, cudaMemcpyDeviceToHost, c->stream));
+    if (v) CK(cudaMemcpyAsync(v, dv, sizeof(double) * nd, cudaMemcpyDeviceToHost, c->stream));
+    if (F) CK(cudaMemcpyAsync(F, dF, sizeof(double) * nd, cudaMemcpyDeviceToHost, c->stream));
+    if (disp) CK(cudaMemcpyAsync(disp, du, sizeof(double) * nd, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return SIMMD_OK;
+}
+
+int simmd_set_state_r(simmd_ctx* c, int32_t rep, const double* r, const double* v, const double* F,
+                      const double* disp)
+{
+    if (!c) return set_err(SIMMD_ERR_BAD_ARG, "NULL context");
+    CK(cudaSetDevice(c->device));
+    if (rep < 0 || rep >= c->R_cap || !c->reps[rep].active) return set_err(SIMMD_ERR_NOT_FOUND, "no such replica");
+    HostRep& h = c->reps[rep];
+    const long long nd = h.p.N * h.p.dims;
+    TRY(ensure_stage(c, std::max<long long>(nd, (long long)h.p.N)));
+    double* st = c->d_stage;
+    double *dr = st, *dv = st + c->stage_cap, *dF = st + 2 * c->stage_cap, *du = st + 4 * c->stage_cap;
+    if (r) CK(cudaMemcpyAsync(dr, r, sizeof(double) * nd, cudaMemcpyHostToDevice, c->stream));
+    if (v) CK(cudaMemcpyAsync(dv, v, sizeof(double) * nd, cudaMemcpyHostToDevice, c->stream));
+    if (F) CK(cudaMemcpyAsync(dF, F, sizeof(double) * nd, cudaMemcpyHostToDevice, c->stream));
+    if (disp) CK(cudaMemcpyAsync(du, disp, sizeof(double) * nd, cudaMemcpyHostToDevice, c->stream));
+    Batch b = make_batch(c);
+    LaunchCfg lc = make_lc(c, FMODE_STEP);
+    launch_set_state_impl(b, lc, rep, h.d, r ? dr : nullptr, v ? dv : nullptr, F ? dF : nullptr, disp ? du : nullptr);
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(c->stream));
+    return SIMMD_OK;
+}
+
+int simmd_set_state(simmd_ctx* c, const double* r, const double* v, const double* F, const double* disp)
+{
+    return simmd_set_state_r(c, 0, r, v, F, disp);
+}
+
+int simmd_download(simmd_ctx* c, double* r, double* v, double* F, double* disp)
+{
+    return simmd_download_r(c, 0, r, v, F, disp);
+}
+
+int simmd_rebuild(simmd_ctx* c)
+{
+    if (!c) return set_err(SIMMD_ERR_BAD_ARG, "NULL context");
+    CK(cudaSetDevice(c->device));
+    for (int r = 0; r < c->R_cap; r++)
+        if (c->reps[r].active) c->reps[r].pending_rebuild = true;
+    TRY(pending_rebuilds(c));
+    return read_states(c);
+}
+
+int simmd_set_full_list(simmd_ctx* c, int32_t enable)
+{
+    if (!c) return set_err(SIMMD_ERR_BAD_ARG, "NULL context");
+    CK(cudaSetDevice(c->device));
+    if (enable && !c->keep_full) {
+        c->Kfull = c->K;
+        TRY(dalloc(c, &c->nbr_full, (size_t)c->S_cap * (size_t)c->Kfull));
+        TRY(dalloc(c, &c->ncnt_full, (size_t)c->S_cap));
+        CK(cudaMemsetAsync(c->ncnt_full, 0, sizeof(int) * c->S_cap, c->stream));
+        c->keep_full = 1;
+        invalidate_graph(c);
+    } else if (!enable && c->keep_full) {
+        CK(cudaStreamSynchronize(c->stream));
+        dfree(c, &c->nbr_full, (size_t)c->S_cap * (size_t)c->Kfull);
+        dfree(c, &c->ncnt_full, (size_t)c->S_cap);
+        c->keep_full = 0;
+        invalidate_graph(c);
+    }
+    return SIMMD_OK;
+}
+
+int simmd_forces(simmd_ctx* c, const double* noise, double* F_out)
+{
+    if (!c) return set_err(SIMMD_ERR_BAD_ARG, "NULL context");
+    CK(cudaSetDevice(c->device));
+    TRY(pending_rebuilds(c));
+    Batch b = make_batch(c);
+    LaunchCfg lc = make_lc(c, FMODE_FORCES);
+    Mix m = batch_mix(c);
+    int single = -1, nact = 0;
+    for (int r = 0; r < c->R_cap; r++)
+        if (c->reps[r].active) { nact++; single = r; }
+    if (nact == 0) return set_err(SIMMD_ERR_NOT_FOUND, "no replica uploaded");
+    if (noise && m.noise) {
+        if (nact != 1) return set_err(SIMMD_ERR_BAD_ARG, "host noise requires a single-replica context");
+        HostRep& h = c->reps[single];
+        long long nd = h.p.N * h.p.dims;
+        if (nd > c->noise_cap) {
+            CK(cudaStreamSynchronize(c->stream));
+            dfree(c, &c->d_noise, (size_t)c->noise_cap);
+            TRY(dalloc(c, &c->d_noise, (size_t)nd));
+            c->noise_cap = nd;
+        }
+        CK(cudaMemcpyAsync(c->d_noise, noise, sizeof(double) * nd, cudaMemcpyHostToDevice, c->stream));
+        CK(cudaMemcpyAsync(&c->h_state[single], c->d_state + single, sizeof(RepState), cudaMemcpyDeviceToHost,
+                           c->stream));
+        CK(cudaStreamSynchronize(c->stream));
+        h.d.noise_mode = NOISE_HOST;
+        h.d.host_noise = c->d_noise;
+        h.d.noise_step0 = c->h_state[single].step;
+        h.d.noise_nsteps = 1;
+        TRY(push_desc(c, single));
+        launch_force_impl(b, lc, FMODE_FORCES, lc.grid_force, nullptr);
+        h.d.noise_mode = NOISE_PHILOX;
+        h.d.host_noise = nullptr;
+        TRY(push_desc(c, single));
+    } else {
+        launch_force_impl(b, lc, FMODE_FORCES, lc.grid_force, nullptr);
+    }
+    CK(cudaGetLastError());
+    TRY(read_states(c));
+    if (F_out) return simmd_download_r(c, single, nullptr, nullptr, F_out, nullptr);
+    return SIMMD_OK;
+}
+
+int simmd_step(simmd_ctx* c, int64_t nsteps, const double* noise)
+{
+    if (!c) return set_err(SIMMD_ERR_BAD_ARG, "NULL context");
+    CK(cudaSetDevice(c->device));
+    return run_steps(c, nsteps, noise);
+}
+
+int simmd_energy_all(simmd_ctx* c)
+{
+    if (!c) return set_err(SIMMD_ERR_BAD_ARG, "NULL context");
+    CK(cudaSetDevice(c->device));
+    TRY(pending_rebuilds(c));
+    Batch b = make_batch(c);
+    LaunchCfg lc = make_lc(c, FMODE_ENERGY);
+    launch_force_impl(b, lc, FMODE_ENERGY, lc.grid_force, c->epp);
+    launch_kinetic_impl(b, lc);
+    CK(cudaGetLastError());
+    return read_states(c);
+}
+
+int simmd_energy(simmd_ctx* c, double* epot, double* virial, double* ekin)
+{
+    TRY(simmd_energy_all(c));
+    int r0 = -1;
+    for (int r = 0; r < c->R_cap; r++)
+        if (c->reps[r].active) { r0 = r; break; }
+    if (r0 < 0) return set_err(SIMMD_ERR_NOT_FOUND, "no replica");
+    const RepState& s = c->h_state[r0];
+    if (epot) *epot = s.epot;
+    if (virial) *virial = s.virial;
+    if (ekin) *ekin = c->reps[r0].p.dynamics == SIMMD_BROWNIAN ? 0.0 : s.ekin;
+    return SIMMD_OK;
+}
+
+int simmd_potential_energy_array(simmd_ctx* c, double* e)
+{
+    if (!c || !e) return set_err(SIMMD_ERR_BAD_ARG, "NULL argument");
+    TRY(simmd_energy_all(c));
+    HostRep& h = c->reps[0];
+    if (!h.active) return set_err(SIMMD_ERR_NOT_FOUND, "no replica");
+    TRY(ensure_stage(c, h.p.N * h.p.dims));
+    Batch b = make_batch(c);
+    LaunchCfg lc = make_lc(c, FMODE_STEP);
+    launch_store_aos_impl(b, lc, 0, h.d, nullptr, nullptr, nullptr, nullptr, c->epp, c->d_stage);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(e, c->d_stage, sizeof(double) * h.p.N, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return SIMMD_OK;
+}
+
+int simmd_export_pairs(simmd_ctx* c, int32_t which, int64_t maxK, int64_t* counts, int64_t* list)
+{
+    if (!c || !counts || !list || maxK < 1) return set_err(SIMMD_ERR_BAD_ARG, "bad argument");
+    CK(cudaSetDevice(c->device));
+    HostRep& h = c->reps[0];
+    if (!h.active) return set_err(SIMMD_ERR_NOT_FOUND, "no replica");
+    if (which == 1 && !c->keep_full) return set_err(SIMMD_ERR_BAD_ARG, "full list not kept: simmd_set_full_list");
+    TRY(pending_rebuilds(c));
+    long long N = h.p.N;
+    long long *dcnt = nullptr, *dlist = nullptr;
+    int* dovf = nullptr;
+    TRY(dalloc(c, &dcnt, (size_t)N));
+    TRY(dalloc(c, &dlist, (size_t)(N * maxK)));
+    TRY(dalloc(c, &dovf, 1));
+    CK(cudaMemsetAsync(dovf, 0, sizeof(int), c->stream));
+    CK(cudaMemsetAsync(dlist, 0, sizeof(long long) * N * maxK, c->stream));
+    Batch b = make_batch(c);
+    LaunchCfg lc = make_lc(c, FMODE_STEP);
+    if (which == 0) launch_export_impl(b, lc, 0, h.d, c->s.nbr, c->s.ncnt, c->T, dcnt, dlist, maxK, 1, dovf);
+    else launch_export_impl(b, lc, 0, h.d, c->nbr_full, c->ncnt_full, 1, dcnt, dlist, maxK, 0, dovf);
+    CK(cudaGetLastError());
+    int ovf = 0;
+    CK(cudaMemcpyAsync(counts, dcnt, sizeof(long long) * N, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemcpyAsync(list, dlist, sizeof(long long) * N * maxK, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemcpyAsync(&ovf, dovf, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    dfree(c, &dcnt, (size_t)N);
+    dfree(c, &dlist, (size_t)(N * maxK));
+    dfree(c, &dovf, 1);
+    if (ovf) return set_err(SIMMD_ERR_NEIGHBOR_OVERFLOW, "export maxK too small");
+    return SIMMD_OK;
+}
+
+static void fill_stats(simmd_ctx* c, int r, simmd_stats* out)
+{
+    const RepState& s = c->h_state[r];
+    memset(out, 0, sizeof(*out));
+    out->steps_done = c->reps[r].steps_done;
+    out->rebuilds = s.rebuilds;
+    out->noise_draws = s.step;
+    out->max_neighbors = c->K;
+    out->max_count = s.maxcount;
+    out->overflow = s.overflow;
+    out->nonfinite = s.nonfinite;
+    out->epot = s.epot;
+    out->virial = s.virial;
+    out->ekin = s.ekin;
+    out->list_entries = s.list_entries;
+}
+
+int simmd_stats_r(simmd_ctx* c, int32_t rep, simmd_stats* out)
+{
+    if (!c || !out) return set_err(SIMMD_ERR_BAD_ARG, "NULL argument");
+    CK(cudaSetDevice(c->device));
+    if (rep < 0 || rep >= c->R_cap || !c->reps[rep].active) return set_err(SIMMD_ERR_NOT_FOUND, "no such replica");
+    CK(cudaMemcpyAsync(&c->h_state[rep], c->d_state + rep, sizeof(RepState), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    fill_stats(c, rep, out);
+    return SIMMD_OK;
+}
+
+int simmd_stats_get(simmd_ctx* c, simmd_stats* out) { return simmd_stats_r(c, 0, out); }
+
+int simmd_reserve(simmd_ctx* c, int64_t slots, int64_t cells, int32_t replicas, int32_t max_neighbors)
+{
+    if (!c) return set_err(SIMMD_ERR_BAD_ARG, "NULL context");
+    CK(cudaSetDevice(c->device));
+    return ensure_capacity(c, std::max<long long>(slots, c->S_cap), std::max<long long>(cells, c->C_cap),
+                           std::max<int>(replicas, c->R_cap), std::max<int>(max_neighbors, c->K));
+}
+
+int simmd_add_replica(simmd_ctx* c, const simmd_params* p, const double* r, const double* v, const double* F,
+                      const double* D, int32_t* rep_out)
+{
+    if (!c || !rep_out) return set_err(SIMMD_ERR_BAD_ARG, "NULL argument");
+    CK(cudaSetDevice(c->device));
+    int rid = -1;
+    TRY(add_replica(c, p, r, v, F, D, &rid));
+    *rep_out = rid;
+    return SIMMD_OK;
+}
+
+int simmd_remove_replica(simmd_ctx* c, int32_t rep)
+{
+    if (!c) return set_err(SIMMD_ERR_BAD_ARG, "NULL context");
+    CK(cudaSetDevice(c->device));
+    return remove_replica(c, rep);
+}
+
+int64_t simmd_replica_bytes(const simmd_params* p, int32_t max_neighbors)
+{
+    if (!p || p->N < 1) return 0;
+    long long npad = (p->N + TILE - 1) / TILE * TILE;
+    long long K = max_neighbors > 0 ? max_neighbors : 200;
+    // per slot: posD 32 + v,F,u 72 + off 16 + cellc/orig/ncnt 12 + scratch (bin x3 12, t_posD 32,
+    // t_v/t_F 48, t_orig 4) + epp 8 + list 4K
+    long long per = 32 + 72 + 16 + 12 + 12 + 32 + 48 + 4 + 8 + 4 * K;
+    long long cells = npad;  // upper bound of cells actually used
+    return npad * per + cells * 8 + 4096;
+}
+
+int simmd_set_tuning(simmd_ctx* c, int32_t tpp, int32_t use_graphs, int32_t graph_steps)
+{
+    if (!c) return set_err(SIMMD_ERR_BAD_ARG, "NULL context");
+    if (tpp != 1 && tpp != 2 && tpp != 4) return set_err(SIMMD_ERR_BAD_ARG, "tpp must be 1, 2 or 4");
+    CK(cudaSetDevice(c->device));
+    if (tpp != c->T) {
+        CK(cudaStreamSynchronize(c->stream));
+        c->T = tpp;
+        int K = (c->K + tpp - 1) / tpp * tpp;
+        if (K != c->K) {
+            dfree(c, &c->s.nbr, (size_t)c->S_cap * (size_t)c->K);
+            TRY(dalloc(c, &c->s.nbr, (size_t)c->S_cap * (size_t)K));
+            c->K = K;
+        }
+        force_rebuild_all(c);
+        invalidate_graph(c);
+    }
+    c->use_graphs = use_graphs ? 1 : 0;
+    if (graph_steps > 0 && graph_steps != c->graph_steps) {
+        c->graph_steps = graph_steps;
+        invalidate_graph(c);
+    }
+    return SIMMD_OK;
+}
+
+int simmd_sync(simmd_ctx* c)
+{
+    if (!c) return set_err(SIMMD_ERR_BAD_ARG, "NULL context");
+    CK(cudaStreamSynchronize(c->stream));
+    return SIMMD_OK;
+}
+
+void* simmd_stream(simmd_ctx* c) { return c ? (void*)c->stream : nullptr; }
+
+int simmd_timer_start(simmd_ctx* c)
+{
+    if (!c) return set_err(SIMMD_ERR_BAD_ARG, "NULL context");
+    CK(cudaEventRecord(c->ev0, c->stream));
+    return SIMMD_OK;
+}
+
+int simmd_timer_stop(simmd_ctx* c, float* ms)
+{
+    if (!c || !ms) return set_err(SIMMD_ERR_BAD_ARG, "NULL argument");
+    CK(cudaEventRecord(c->ev1, c->stream));
+    CK(cudaEventSynchronize(c->ev1));
+    CK(cudaEventElapsedTime(ms, c->ev0, c->ev1));
+    return SIMMD_OK;
+}
+
+int64_t simmd_launch_count(simmd_ctx* c) { return c ? c->launches : 0; }
+int64_t simmd_device_bytes(simmd_ctx* c) { return c ? c->bytes : 0; }
+
+int simmd_time_force(simmd_ctx* c, int32_t nrep, float* ms_per_launch)
+{
+    if (!c || !ms_per_launch || nrep < 1) return set_err(SIMMD_ERR_BAD_ARG, "bad argument");
+    CK(cudaSetDevice(c->device));
+    TRY(pending_rebuilds(c));
+    Batch b = make_batch(c);
+    LaunchCfg lc = make_lc(c, FMODE_ENERGY);
+    CK(cudaEventRecord(c->ev0, c->stream));
+    for (int k = 0; k < nrep; k++) launch_force_impl(b, lc, FMODE_ENERGY, lc.grid_force, nullptr);
+    CK(cudaEventRecord(c->ev1, c->stream));
+    CK(cudaEventSynchronize(c->ev1));
+    float ms = 0;
+    CK(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
+    *ms_per_launch = ms / (float)nrep;
+    return SIMMD_OK;
+}
+
+int simmd_relax(simmd_ctx* c, int64_t nsteps, double max_disp)
+{
+    if (!c || nsteps < 0 || !(max_disp > 0)) return set_err(SIMMD_ERR_BAD_ARG, "bad argument");
+    CK(cudaSetDevice(c->device));
+    TRY(pending_rebuilds(c));
+    std::vector<RepDesc> saved;
+    for (int r = 0; r < c->R_cap; r++) {
+        saved.push_back(c->reps[r].d);
+        if (!c->reps[r].active) continue;
+        RepDesc& d = c->reps[r].d;
+        d.dyn = DYN_BROWNIAN;
+        d.dt_over_gamma = 1.0;
+        d.relax_cap = max_disp;
+        d.prec = PREC_FP64;
+        TRY(push_desc(c, r));
+    }
+    Batch b = make_batch(c);
+    LaunchCfg lc = make_lc(c, FMODE_STEP);
+    Mix m;
+    m.br = true;
+    for (long long s = 0; s < nsteps; s++) enqueue_step(c, b, lc, m, FMODE_STEP);
+    CK(cudaGetLastError());
+    for (int r = 0; r < c->R_cap; r++) {
+        if (!c->reps[r].active) continue;
+        c->reps[r].d = saved[r];
+        TRY(push_desc(c, r));
+        c->reps[r].pending_rebuild = true;  // FP32 offsets / lists for the restored mode
+    }
+    // the relaxation's mean-force state must not leak into the dynamics
+    TRY(read_states(c));
+    for (int r = 0; r < c->R_cap; r++) {
+        if (!c->reps[r].active) continue;
+        RepState& st = c->h_state[r];
+        st.fmean[0] = st.fmean[1] = st.fmean[2] = 0.0;
+        st.vmean[0] = st.vmean[1] = st.vmean[2] = 0.0;
+        st.vscale = 1.0;
+        st.nonfinite = 0;
+        CK(cudaMemcpyAsync(c->d_state + r, &st, sizeof(RepState), cudaMemcpyHostToDevice, c->stream));
+    }
+    CK(cudaStreamSynchronize(c->stream));
+    return SIMMD_OK;
+}
+
+int simmd_host_register(void* ptr, int64_t bytes)
+{
+    if (!ptr || bytes <= 0) return set_err(SIMMD_ERR_BAD_ARG, "bad argument");
+    CK(cudaHostRegister(ptr, (size_t)bytes, cudaHostRegisterDefault));
+    return SIMMD_OK;
+}
+
+int simmd_host_unregister(void* ptr)
+{
+    if (!ptr) return set_err(SIMMD_ERR_BAD_ARG, "bad argument");
+    CK(cudaHostUnregister(ptr));
+    return SIMMD_OK;
+}
+
+int simmd_set_profile(simmd_ctx* c, int32_t enable)
+{
+    if (!c) return set_err(SIMMD_ERR_BAD_ARG, "NULL context");
+    c->profile = enable ? 1 : 0;
+    c->prof = ProfileAcc();
+    return SIMMD_OK;
+}
+
+int simmd_profile_get(simmd_ctx* c, double* out6)
+{
+    if (!c || !out6) return set_err(SIMMD_ERR_BAD_ARG, "NULL argument");
+    out6[0] = c->prof.force_ms;
+    out6[1] = (double)c->prof.force_n;
+    out6[2] = c->prof.kick_ms;
+    out6[3] = c->prof.rebuild_ms;
+    out6[4] = c->prof.update_ms;
+    out6[5] = (double)c->prof.steps;
+    return SIMMD_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,386 @@
+// k_integrate.cu -- O(N) streaming kernels of the time step and the host <->
+// slot-layout transfers.
+//
+// Reference (SimulationCode.jl):
+//   kick1 / drift / wrap / displacement  src/MD.jl:510-522
+//   skin trigger max|disp|^2 > (skin/2)^2 src/MD.jl:523-525 (one atomicMax per warp)
+//   centre-of-mass removal               src/MD.jl:532-542 (applied lazily: the vmean
+//                                        computed by the force pass is subtracted at the
+//                                        start of the next kick1, or by finalize)
+//   temperature rescale                  src/MD.jl:543-553, 391-402
+//   Brownian update (as intended)        src/MD.jl:444-470
+//   find_kinetic_energy                  src/AuxiliaryFunctions.jl:57-65
+// All FP64 arithmetic uses explicit round-to-nearest intrinsics in the
+// reference's operation order.
+#include "simmd_internal.cuh"
+#include "simmd_reduce.cuh"
+
+namespace simmd {
+
+__device__ __forceinline__ float cell_offset_dyn(double x, int c, const RepDesc& d)
+{
+    if (d.nc == 1) return (float)x;
+    double o = x - (double)c * d.cs;
+    o = (o > d.halfL) ? o - d.L : o;
+    o = (o < -d.halfL) ? o + d.L : o;
+    return (float)o;
+}
+
+// r += dr with the reference wrap rnew - floor(rnew/L)*L, displacement update,
+// FP32 offset refresh; returns |disp|^2
+__device__ __forceinline__ double drift_slot(const Batch& b, const RepDesc& d, long long i, double drx,
+                                             double dry, double drz)
+{
+    const Slots& S = b.s;
+    double ux = dadd(S.ux[i], drx), uy = dadd(S.uy[i], dry), uz = 0.0;
+    double u2 = dadd(dmul(ux, ux), dmul(uy, uy));
+    S.ux[i] = ux;
+    S.uy[i] = uy;
+    if (d.dims == 3) {
+        uz = dadd(S.uz[i], drz);
+        u2 = dadd(u2, dmul(uz, uz));
+        S.uz[i] = uz;
+    }
+    double4_32a p = S.posD[i];
+    double x = dadd(p.x, drx);
+    x = dsub(x, dmul(floor(ddiv(x, d.L)), d.L));
+    double y = dadd(p.y, dry);
+    y = dsub(y, dmul(floor(ddiv(y, d.L)), d.L));
+    double z = p.z;
+    if (d.dims == 3) {
+        z = dadd(p.z, drz);
+        z = dsub(z, dmul(floor(ddiv(z, d.L)), d.L));
+    }
+    S.posD[i] = make_double4_32a(x, y, z, p.w);
+    if (d.prec == PREC_FP32) {
+        int c = S.cellc[i];
+        S.off[i] = make_float4(cell_offset_dyn(x, c & 1023, d), cell_offset_dyn(y, (c >> 10) & 1023, d),
+                               d.dims == 3 ? cell_offset_dyn(z, (c >> 20) & 1023, d) : 0.0f, (float)p.w);
+    }
+    return u2;
+}
+
+__device__ __forceinline__ void warp_max_to_state(double u2, RepState& st)
+{
+    unsigned long long bits = (unsigned long long)__double_as_longlong(u2);
+    if (!(u2 == u2) || isinf(u2)) {
+        st.nonfinite = 1;
+        bits = 0x7ff0000000000000ull;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        unsigned long long y = __shfl_xor_sync(0xffffffffu, bits, o);
+        bits = y > bits ? y : bits;
+    }
+    if ((threadIdx.x & 31) == 0) atomicMax(&st.maxdisp2, bits);
+}
+
+// kick1 + drift for Newtonian / Langevin replicas (src/MD.jl:510-522)
+__global__ void k_kick_drift(Batch b)
+{
+    for (int t = blockIdx.x; t < b.ntiles; t += gridDim.x) {
+        int r = b.tile_rep[t];
+        if (r < 0) continue;
+        const RepDesc& d = b.desc[r];
+        if (d.dyn == DYN_BROWNIAN) continue;
+        RepState& st = b.state[r];
+        long long i = (long long)t * TILE + threadIdx.x;
+        double u2 = 0.0;
+        if (i < d.slot0 + d.n) {
+            const Slots& S = b.s;
+            const double vs = st.vscale;
+            double vx = dmul(dsub(S.vx[i], st.vmean[0]), vs);
+            double vy = dmul(dsub(S.vy[i], st.vmean[1]), vs);
+            vx = dadd(vx, ddiv(dmul(d.dt, S.fx[i]), d.two_m));
+            vy = dadd(vy, ddiv(dmul(d.dt, S.fy[i]), d.two_m));
+            S.vx[i] = vx;
+            S.vy[i] = vy;
+            double vz = 0.0;
+            if (d.dims == 3) {
+                vz = dmul(dsub(S.vz[i], st.vmean[2]), vs);
+                vz = dadd(vz, ddiv(dmul(d.dt, S.fz[i]), d.two_m));
+                S.vz[i] = vz;
+            }
+            u2 = drift_slot(b, d, i, dmul(d.dt, vx), dmul(d.dt, vy), dmul(d.dt, vz));
+        }
+        warp_max_to_state(u2, st);
+    }
+}
+
+// Brownian position update (src/MD.jl:444-467 as intended): F -= <F>,
+// dr = (dt/gamma) F, displacement, wrap
+__global__ void k_brownian_update(Batch b)
+{
+    for (int t = blockIdx.x; t < b.ntiles; t += gridDim.x) {
+        int r = b.tile_rep[t];
+        if (r < 0) continue;
+        const RepDesc& d = b.desc[r];
+        if (d.dyn != DYN_BROWNIAN) continue;
+        RepState& st = b.state[r];
+        long long i = (long long)t * TILE + threadIdx.x;
+        double u2 = 0.0;
+        if (i < d.slot0 + d.n) {
+            const Slots& S = b.s;
+            double Fx = dsub(S.fx[i], st.fmean[0]);
+            double Fy = dsub(S.fy[i], st.fmean[1]);
+            S.fx[i] = Fx;
+            S.fy[i] = Fy;
+            double Fz = 0.0;
+            if (d.dims == 3) {
+                Fz = dsub(S.fz[i], st.fmean[2]);
+                S.fz[i] = Fz;
+            }
+            double drx = dmul(d.dt_over_gamma, Fx), dry = dmul(d.dt_over_gamma, Fy),
+                   drz = dmul(d.dt_over_gamma, Fz);
+            if (d.relax_cap > 0.0) {  // set-up relaxation: |dr| <= relax_cap per particle
+                double m = fmax(fabs(drx), fmax(fabs(dry), fabs(drz)));
+                if (m > 0.0) {
+                    double qx = drx / m, qy = dry / m, qz = drz / m;
+                    double len = m * sqrt(qx * qx + qy * qy + qz * qz);
+                    if (!(len <= d.relax_cap)) {
+                        double sc = d.relax_cap / len;
+                        drx = isfinite(sc) ? drx * sc : 0.0;
+                        dry = isfinite(sc) ? dry * sc : 0.0;
+                        drz = isfinite(sc) ? drz * sc : 0.0;
+                        if (!isfinite(len)) {
+                            drx = qx * d.relax_cap;
+                            dry = qy * d.relax_cap;
+                            drz = qz * d.relax_cap;
+                        }
+                    }
+                }
+            }
+            u2 = drift_slot(b, d, i, drx, dry, drz);
+        }
+        warp_max_to_state(u2, st);
+    }
+}
+
+// kinetic energy of (v - vmean) with the pending COM removal applied, and
+// (rescale mode) the velocity rescale factor sqrt(kBT / kBT_current)
+template <bool RESCALE_ONLY>
+__global__ void k_kinetic(Batch b)
+{
+    __shared__ double s_part[32];
+    __shared__ int s_flag;
+    for (int t = blockIdx.x; t < b.ntiles; t += gridDim.x) {
+        int r = b.tile_rep[t];
+        if (r < 0) continue;
+        const RepDesc& d = b.desc[r];
+        if (d.dyn == DYN_BROWNIAN) continue;
+        if (RESCALE_ONLY && !d.rescale) continue;
+        RepState& st = b.state[r];
+        long long i = (long long)t * TILE + threadIdx.x;
+        double v[1] = {0.0};
+        if (i < d.slot0 + d.n) {
+            const Slots& S = b.s;
+            double vx = dsub(S.vx[i], st.vmean[0]), vy = dsub(S.vy[i], st.vmean[1]);
+            double s = dadd(dmul(vx, vx), dmul(vy, vy));
+            if (d.dims == 3) {
+                double vz = dsub(S.vz[i], st.vmean[2]);
+                s = dadd(s, dmul(vz, vz));
+            }
+            v[0] = s;
+        }
+        double out[1];
+        if (tile_reduce<1>(b, t, d, st, v, out, s_part, &s_flag) && threadIdx.x == 0) {
+            double ekin = dmul(out[0], d.m_half);
+            if (RESCALE_ONLY) {
+                double kbt = ddiv(dmul(2.0, ekin), (double)(d.dims * d.n));
+                st.vscale = __dsqrt_rn(ddiv(d.kBT, kbt));
+            } else {
+                st.ekin = ekin;
+            }
+        }
+    }
+}
+
+// apply the pending COM removal / rescale (end of a batch of steps)
+__global__ void k_finalize(Batch b)
+{
+    __shared__ double s_part[32];
+    __shared__ int s_flag;
+    for (int t = blockIdx.x; t < b.ntiles; t += gridDim.x) {
+        int r = b.tile_rep[t];
+        if (r < 0) continue;
+        const RepDesc& d = b.desc[r];
+        if (d.dyn == DYN_BROWNIAN) continue;
+        RepState& st = b.state[r];
+        long long i = (long long)t * TILE + threadIdx.x;
+        if (i < d.slot0 + d.n) {
+            const Slots& S = b.s;
+            const double vs = st.vscale;
+            S.vx[i] = dmul(dsub(S.vx[i], st.vmean[0]), vs);
+            S.vy[i] = dmul(dsub(S.vy[i], st.vmean[1]), vs);
+            if (d.dims == 3) S.vz[i] = dmul(dsub(S.vz[i], st.vmean[2]), vs);
+        }
+        double v[1] = {0.0}, out[1];
+        if (tile_reduce<1>(b, t, d, st, v, out, s_part, &s_flag) && threadIdx.x == 0) {
+            st.vmean[0] = st.vmean[1] = st.vmean[2] = 0.0;
+            st.vscale = 1.0;
+        }
+    }
+}
+
+void launch_kick_drift_impl(const Batch& b, const LaunchCfg& lc)
+{
+    k_kick_drift<<<lc.grid_stream, TILE, 0, lc.stream>>>(b);
+    if (lc.launches) *lc.launches += 1;
+}
+void launch_brownian_update_impl(const Batch& b, const LaunchCfg& lc)
+{
+    k_brownian_update<<<lc.grid_stream, TILE, 0, lc.stream>>>(b);
+    if (lc.launches) *lc.launches += 1;
+}
+void launch_rescale_impl(const Batch& b, const LaunchCfg& lc)
+{
+    k_kinetic<true><<<lc.grid_stream, TILE, 0, lc.stream>>>(b);
+    if (lc.launches) *lc.launches += 1;
+}
+void launch_kinetic_impl(const Batch& b, const LaunchCfg& lc)
+{
+    k_kinetic<false><<<lc.grid_stream, TILE, 0, lc.stream>>>(b);
+    if (lc.launches) *lc.launches += 1;
+}
+void launch_finalize_impl(const Batch& b, const LaunchCfg& lc)
+{
+    k_finalize<<<lc.grid_stream, TILE, 0, lc.stream>>>(b);
+    if (lc.launches) *lc.launches += 1;
+}
+
+// ---------------------------------------------------------------------------
+// host layout (AoS dims x N, original order) <-> slots
+// ---------------------------------------------------------------------------
+__global__ void k_load_aos(Batch b, int rep, const double* r, const double* v, const double* F,
+                           const double* D, const double* disp)
+{
+    const RepDesc& d = b.desc[rep];
+    long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= d.npad) return;
+    long long s = d.slot0 + k;
+    Slots& S = b.s;
+    const int dm = d.dims;
+    if (k < d.n) {
+        double x = r[k * dm], y = r[k * dm + 1], z = dm == 3 ? r[k * dm + 2] : 0.0;
+        S.posD[s] = make_double4_32a(x, y, z, D[k]);
+        S.vx[s] = v ? v[k * dm] : 0.0;
+        S.vy[s] = v ? v[k * dm + 1] : 0.0;
+        S.vz[s] = (v && dm == 3) ? v[k * dm + 2] : 0.0;
+        S.fx[s] = F ? F[k * dm] : 0.0;
+        S.fy[s] = F ? F[k * dm + 1] : 0.0;
+        S.fz[s] = (F && dm == 3) ? F[k * dm + 2] : 0.0;
+        S.ux[s] = disp ? disp[k * dm] : 0.0;
+        S.uy[s] = disp ? disp[k * dm + 1] : 0.0;
+        S.uz[s] = (disp && dm == 3) ? disp[k * dm + 2] : 0.0;
+        S.orig[s] = (int)k;
+    } else {
+        S.posD[s] = make_double4_32a(0.0, 0.0, 0.0, 0.0);
+        S.vx[s] = S.vy[s] = S.vz[s] = 0.0;
+        S.fx[s] = S.fy[s] = S.fz[s] = 0.0;
+        S.ux[s] = S.uy[s] = S.uz[s] = 0.0;
+        S.orig[s] = -1;
+    }
+    S.ncnt[s] = 0;
+    S.cellc[s] = 0;
+    S.off[s] = make_float4(0.f, 0.f, 0.f, 0.f);
+}
+
+__global__ void k_store_aos(Batch b, int rep, double* r, double* v, double* F, double* disp,
+                            const double* epp_src, double* epp)
+{
+    const RepDesc& d = b.desc[rep];
+    long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= d.n) return;
+    long long s = d.slot0 + k;
+    const Slots& S = b.s;
+    int o = S.orig[s];
+    const int dm = d.dims;
+    double4_32a p = S.posD[s];
+    if (r) {
+        r[o * dm] = p.x;
+        r[o * dm + 1] = p.y;
+        if (dm == 3) r[o * dm + 2] = p.z;
+    }
+    if (v) {
+        v[o * dm] = S.vx[s];
+        v[o * dm + 1] = S.vy[s];
+        if (dm == 3) v[o * dm + 2] = S.vz[s];
+    }
+    if (F) {
+        F[o * dm] = S.fx[s];
+        F[o * dm + 1] = S.fy[s];
+        if (dm == 3) F[o * dm + 2] = S.fz[s];
+    }
+    if (disp) {
+        disp[o * dm] = S.ux[s];
+        disp[o * dm + 1] = S.uy[s];
+        if (dm == 3) disp[o * dm + 2] = S.uz[s];
+    }
+    if (epp && epp_src) epp[o] = epp_src[s];
+}
+
+// host arrays (original order) -> current slot order; lists and cells kept
+__global__ void k_set_state(Batch b, int rep, const double* r, const double* v, const double* F,
+                            const double* disp)
+{
+    const RepDesc& d = b.desc[rep];
+    long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= d.n) return;
+    long long s = d.slot0 + k;
+    Slots& S = b.s;
+    const int o = S.orig[s];
+    const int dm = d.dims;
+    if (r) {
+        double4_32a p = S.posD[s];
+        p.x = r[o * dm];
+        p.y = r[o * dm + 1];
+        if (dm == 3) p.z = r[o * dm + 2];
+        S.posD[s] = p;
+        if (d.prec == PREC_FP32) {
+            int c = S.cellc[s];
+            S.off[s] = make_float4(cell_offset_dyn(p.x, c & 1023, d), cell_offset_dyn(p.y, (c >> 10) & 1023, d),
+                                   dm == 3 ? cell_offset_dyn(p.z, (c >> 20) & 1023, d) : 0.0f, (float)p.w);
+        }
+    }
+    if (v) {
+        S.vx[s] = v[o * dm];
+        S.vy[s] = v[o * dm + 1];
+        if (dm == 3) S.vz[s] = v[o * dm + 2];
+    }
+    if (F) {
+        S.fx[s] = F[o * dm];
+        S.fy[s] = F[o * dm + 1];
+        if (dm == 3) S.fz[s] = F[o * dm + 2];
+    }
+    if (disp) {
+        S.ux[s] = disp[o * dm];
+        S.uy[s] = disp[o * dm + 1];
+        if (dm == 3) S.uz[s] = disp[o * dm + 2];
+    }
+}
+
+void launch_set_state_impl(const Batch& b, const LaunchCfg& lc, int rep, const RepDesc& hd, const double* r,
+                           const double* v, const double* F, const double* disp)
+{
+    int blocks = (hd.n + 127) / 128;
+    if (blocks > 0) k_set_state<<<blocks, 128, 0, lc.stream>>>(b, rep, r, v, F, disp);
+    if (lc.launches) *lc.launches += 1;
+}
+
+void launch_load_aos_impl(const Batch& b, const LaunchCfg& lc, int rep, const RepDesc& hd, const double* r,
+                          const double* v, const double* F, const double* D, const double* disp)
+{
+    int blocks = (hd.npad + 127) / 128;
+    k_load_aos<<<blocks, 128, 0, lc.stream>>>(b, rep, r, v, F, D, disp);
+    if (lc.launches) *lc.launches += 1;
+}
+
+void launch_store_aos_impl(const Batch& b, const LaunchCfg& lc, int rep, const RepDesc& hd, double* r,
+                           double* v, double* F, double* disp, const double* epp_src, double* epp)
+{
+    int blocks = (hd.n + 127) / 128;
+    if (blocks > 0) k_store_aos<<<blocks, 128, 0, lc.stream>>>(b, rep, r, v, F, disp, epp_src, epp);
+    if (lc.launches) *lc.launches += 1;
+}
+
+}  // namespace simmd

@@ -1,0 +1,410 @@
+// k_neighbor.cu -- neighbour-list rebuild (update_neighbor_lists!,
+// src/NeighborLists.jl:24-104 of SimulationCode.jl) for every replica whose
+// skin trigger fired or whose rebuild was requested by the host.
+//
+// Sequence (each kernel covers all replicas and skips those not rebuilding):
+//   zero      cell counters of the replica
+//   bin       cell of each particle (FP64 position / cell size), rank in the
+//             cell by atomicAdd
+//   scan      one block per replica: exclusive scan of the counts -> starts
+//   scatter   new slot = start[cell] + rank  (src[new] = old slot)
+//   cellsort  each cell's slots ordered by original particle id, so the
+//             layout (and every later sum) is deterministic and independent
+//             of the other replicas in the batch
+//   gather    particle state to the new order (staging), displacement := 0,
+//             packed cell coordinates and FP32 cell-relative offsets
+//   build     per particle, the 27 (3D) / 9 (2D) stencil cells; an FP32
+//             prefilter on the offsets, then the exact FP64 test of the
+//             reference: d2 <= verlet^2 (the pair enumeration radius) and
+//             d2 < (sqrt(rc2)*mean_d + skin)^2 (add_pair!'s half-list test),
+//             d2 from dx - round(dx/L)*L in the reference's operation order.
+//             The list stores each pair in both directions (no atomics in
+//             the force pass); staging copied back to the main arrays.
+//   done      reset displacement max / request flag, count the rebuild.
+#include "simmd_internal.cuh"
+
+namespace simmd {
+
+__device__ __forceinline__ int pack_cell(int cx, int cy, int cz) { return cx | (cy << 10) | (cz << 20); }
+
+__global__ void k_rb_zero(Batch b)
+{
+    for (int t = blockIdx.x; t < b.ntiles; t += gridDim.x) {
+        int r = b.tile_rep[t];
+        if (r < 0) continue;
+        const RepDesc& d = b.desc[r];
+        if (!need_rebuild(b.state[r], d)) continue;
+        int tl = t - d.tile0;
+        for (int c = tl * TILE + threadIdx.x; c < d.ncell + 1; c += d.ntiles * TILE)
+            b.s.cell_count[d.cell0 + c] = 0;
+    }
+}
+
+__global__ void k_rb_bin(Batch b)
+{
+    for (int t = blockIdx.x; t < b.ntiles; t += gridDim.x) {
+        int r = b.tile_rep[t];
+        if (r < 0) continue;
+        const RepDesc& d = b.desc[r];
+        if (!need_rebuild(b.state[r], d)) continue;
+        long long s = (long long)t * TILE + threadIdx.x;
+        if (s >= d.slot0 + d.n) continue;
+        double4_32a p = b.s.posD[s];
+        int nc = d.nc;
+        int c[3] = {0, 0, 0};
+        double x[3] = {p.x, p.y, p.z};
+        bool finite = isfinite(p.x) && isfinite(p.y) && isfinite(p.z);
+        if (!finite) b.state[r].nonfinite = 1;
+        if (nc > 1 && finite) {
+            for (int k = 0; k < d.dims; k++) {
+                int ci = (int)floor(x[k] * d.inv_cs);
+                ci = ci < 0 ? 0 : (ci >= nc ? nc - 1 : ci);
+                c[k] = ci;
+            }
+        }
+        int lin = c[0] + nc * (c[1] + nc * c[2]);
+        b.s.bin_cell[s] = lin;
+        b.s.bin_rank[s] = atomicAdd(&b.s.cell_count[d.cell0 + lin], 1);
+    }
+}
+
+// one block per replica; blockDim 1024
+__global__ void k_rb_scan(Batch b)
+{
+    int r = blockIdx.x;
+    if (r >= b.nreps) return;
+    const RepDesc& d = b.desc[r];
+    if (!d.active || !need_rebuild(b.state[r], d)) return;
+    __shared__ int warp_sums[32];
+    const int nthr = blockDim.x;
+    const int nc = d.ncell;
+    const int per = (nc + nthr - 1) / nthr;
+    const int lo = threadIdx.x * per;
+    const int hi = min(lo + per, nc);
+    const int* cnt = b.s.cell_count + d.cell0;
+    int local = 0;
+    for (int c = lo; c < hi; c++) local += cnt[c];
+    // block exclusive scan of the per-thread totals
+    int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    int incl = local;
+    for (int o = 1; o < 32; o <<= 1) {
+        int y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += y;
+    }
+    if (lane == 31) warp_sums[w] = incl;
+    __syncthreads();
+    if (w == 0) {
+        int nw = nthr >> 5;
+        int v = lane < nw ? warp_sums[lane] : 0;
+        int inc = v;
+        for (int o = 1; o < 32; o <<= 1) {
+            int y = __shfl_up_sync(0xffffffffu, inc, o);
+            if (lane >= o) inc += y;
+        }
+        if (lane < nw) warp_sums[lane] = inc - v;
+    }
+    __syncthreads();
+    int run = (int)d.slot0 + warp_sums[w] + incl - local;
+    int* start = b.s.cell_start + d.cell0;
+    for (int c = lo; c < hi; c++) {
+        start[c] = run;
+        run += cnt[c];
+    }
+    if (threadIdx.x == 0) {
+        start[nc] = (int)(d.slot0 + d.n);
+        b.state[r].list_entries = 0;
+    }
+}
+
+__global__ void k_rb_scatter(Batch b)
+{
+    for (int t = blockIdx.x; t < b.ntiles; t += gridDim.x) {
+        int r = b.tile_rep[t];
+        if (r < 0) continue;
+        const RepDesc& d = b.desc[r];
+        if (!need_rebuild(b.state[r], d)) continue;
+        long long s = (long long)t * TILE + threadIdx.x;
+        if (s >= d.slot0 + d.n) continue;
+        int nw = b.s.cell_start[d.cell0 + b.s.bin_cell[s]] + b.s.bin_rank[s];
+        b.s.src[nw] = (int)s;
+    }
+}
+
+__global__ void k_rb_cellsort(Batch b)
+{
+    for (int t = blockIdx.x; t < b.ntiles; t += gridDim.x) {
+        int r = b.tile_rep[t];
+        if (r < 0) continue;
+        const RepDesc& d = b.desc[r];
+        if (!need_rebuild(b.state[r], d)) continue;
+        int tl = t - d.tile0;
+        for (int c = tl * TILE + threadIdx.x; c < d.ncell; c += d.ntiles * TILE) {
+            int a = b.s.cell_start[d.cell0 + c], e = b.s.cell_start[d.cell0 + c + 1];
+            int* src = b.s.src;
+            for (int k = a + 1; k < e; k++) {  // insertion sort by original id
+                int sv = src[k];
+                int key = b.s.orig[sv];
+                int m = k - 1;
+                while (m >= a && b.s.orig[src[m]] > key) {
+                    src[m + 1] = src[m];
+                    m--;
+                }
+                src[m + 1] = sv;
+            }
+        }
+    }
+}
+
+// FP32 cell-relative offset of coordinate x in cell c (nc >= 3), continuous
+// across the periodic wrap; for a single-cell axis the wrapped x itself
+__device__ __forceinline__ float cell_offset(double x, int c, const RepDesc& d)
+{
+    if (d.nc == 1) return (float)x;
+    double o = x - (double)c * d.cs;
+    o = (o > d.halfL) ? o - d.L : o;
+    o = (o < -d.halfL) ? o + d.L : o;
+    return (float)o;
+}
+
+__global__ void k_rb_gather(Batch b)
+{
+    for (int t = blockIdx.x; t < b.ntiles; t += gridDim.x) {
+        int r = b.tile_rep[t];
+        if (r < 0) continue;
+        const RepDesc& d = b.desc[r];
+        if (!need_rebuild(b.state[r], d)) continue;
+        long long nw = (long long)t * TILE + threadIdx.x;
+        Slots& S = b.s;
+        S.ux[nw] = 0.0;
+        S.uy[nw] = 0.0;
+        S.uz[nw] = 0.0;
+        if (nw < d.slot0 + d.n) {
+            int s = S.src[nw];
+            double4_32a p = S.posD[s];
+            S.t_posD[nw] = p;
+            S.t_vx[nw] = S.vx[s];
+            S.t_vy[nw] = S.vy[s];
+            S.t_vz[nw] = S.vz[s];
+            S.t_fx[nw] = S.fx[s];
+            S.t_fy[nw] = S.fy[s];
+            S.t_fz[nw] = S.fz[s];
+            S.t_orig[nw] = S.orig[s];
+            int lin = S.bin_cell[s];
+            int nc = d.nc;
+            int cx = lin % nc, cy = (lin / nc) % nc, cz = lin / (nc * nc);
+            S.cellc[nw] = pack_cell(cx, cy, cz);
+            S.off[nw] = make_float4(cell_offset(p.x, cx, d), cell_offset(p.y, cy, d),
+                                    d.dims == 3 ? cell_offset(p.z, cz, d) : 0.0f, (float)p.w);
+        } else {
+            S.t_posD[nw] = make_double4_32a(0.0, 0.0, 0.0, 0.0);
+            S.t_vx[nw] = S.t_vy[nw] = S.t_vz[nw] = 0.0;
+            S.t_fx[nw] = S.t_fy[nw] = S.t_fz[nw] = 0.0;
+            S.t_orig[nw] = -1;
+            S.cellc[nw] = 0;
+            S.off[nw] = make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+    }
+}
+
+// mean pair diameter of find_mean_D (src/InteractionPotential.jl:5-11), exact
+__device__ __forceinline__ double mean_d_f64(const RepDesc& d, double Di, double Dj)
+{
+    if (d.pot == POT_LJ) return d.sigma2;
+    return dmul(dmul(dadd(Di, Dj), 0.5), dsub(1.0, dmul(d.zeta, fabs(dsub(Di, Dj)))));
+}
+
+template <int DIM, bool FULL>
+__device__ void build_particle(const Batch& b, const RepDesc& d, RepState& st, long long i,
+                               unsigned* nbr_full, int* ncnt_full, int Kfull)
+{
+    const Slots& S = b.s;
+    const double4_32a pi = S.t_posD[i];
+    const float4 oi = S.off[i];
+    const int ci = S.cellc[i];
+    const int cx = ci & 1023, cy = (ci >> 10) & 1023, cz = (ci >> 20) & 1023;
+    const int nc = d.nc;
+    const int rng = (nc >= 3) ? 1 : 0;
+    const long long halfLb = __double_as_longlong(d.halfL);
+    const float csf = d.csf;
+    const float pre_r = (d.pot == POT_LJ) ? d.rcutf * d.sigma2f + d.skinf
+                                          : d.rcutf * 1.0f + d.skinf;  // scaled by mean_d below
+    const float rvf = (float)sqrt(d.rv2) + 1e-3f;
+    int cnt = 0, cntf = 0;
+    const int K = b.K, T = b.tpp;
+    const long long SS = b.S;
+    const int zr = (DIM == 3) ? rng : 0;
+    for (int oz = -zr; oz <= zr; oz++) {
+        int z = (DIM == 3) ? (cz + oz + nc) % nc : 0;
+        for (int oy = -rng; oy <= rng; oy++) {
+            int y = (cy + oy + nc) % nc;
+            for (int ox = -rng; ox <= rng; ox++) {
+                int x = (cx + ox + nc) % nc;
+                int lin = x + nc * (y + nc * z);
+                int a = S.cell_start[d.cell0 + lin], e = S.cell_start[d.cell0 + lin + 1];
+                unsigned code = (unsigned)(1 - ox) | ((unsigned)(1 - oy) << 2) |
+                                ((unsigned)(DIM == 3 ? 1 - oz : 1) << 4);
+                float shx = (float)(-ox) * csf, shy = (float)(-oy) * csf, shz = (float)(-oz) * csf;
+                for (int j = a; j < e; j++) {
+                    if (j == i) continue;
+                    float4 oj = S.off[j];
+                    float dxf = min_image_f32(oi.x - oj.x + shx, d.halfLf, d.Lf);
+                    float dyf = min_image_f32(oi.y - oj.y + shy, d.halfLf, d.Lf);
+                    float d2f = dxf * dxf + dyf * dyf;
+                    if (DIM == 3) {
+                        float dzf = min_image_f32(oi.z - oj.z + shz, d.halfLf, d.Lf);
+                        d2f += dzf * dzf;
+                    }
+                    float lim;
+                    if (FULL) {
+                        lim = rvf;
+                    } else if (d.pot == POT_LJ) {
+                        lim = pre_r + 1e-3f;
+                    } else {
+                        float mdf = (oi.w + oj.w) * 0.5f * (1.0f - d.zetaf * fabsf(oi.w - oj.w));
+                        lim = d.rcutf * mdf + d.skinf + 1e-3f;
+                    }
+                    if (d2f > lim * lim) continue;
+                    // exact FP64 test in the reference's operation order
+                    double4_32a pj = S.t_posD[j];
+                    double ddx = min_image_f64(dsub(pi.x, pj.x), halfLb, d.L);
+                    double ddy = min_image_f64(dsub(pi.y, pj.y), halfLb, d.L);
+                    double d2 = dadd(dmul(ddx, ddx), dmul(ddy, ddy));
+                    if (DIM == 3) {
+                        double ddz = min_image_f64(dsub(pi.z, pj.z), halfLb, d.L);
+                        d2 = dadd(d2, dmul(ddz, ddz));
+                    }
+                    if (!(d2 <= d.rv2)) continue;
+                    if (FULL) {
+                        if (cntf < Kfull) nbr_full[(size_t)cntf * SS + i] = (unsigned)j;
+                        cntf++;
+                    }
+                    double tt = dadd(dmul(d.rcut, mean_d_f64(d, pi.w, pj.w)), d.skin);
+                    if (d2 < dmul(tt, tt)) {
+                        if (cnt < K) S.nbr[nbr_addr(cnt, i, T, SS)] = (unsigned)j | (code << IDX_BITS);
+                        cnt++;
+                    }
+                }
+            }
+        }
+    }
+    if (cnt > K) st.overflow = 1;
+    S.ncnt[i] = min(cnt, K);
+    if (FULL) {
+        if (cntf > Kfull) st.overflow = 1;
+        ncnt_full[i] = min(cntf, Kfull);
+    }
+    atomicMax(&st.maxcount, cnt);
+    atomicAdd((unsigned long long*)&st.list_entries, (unsigned long long)min(cnt, K));
+}
+
+__global__ void k_rb_build(Batch b, unsigned* nbr_full, int* ncnt_full, int Kfull)
+{
+    for (int t = blockIdx.x; t < b.ntiles; t += gridDim.x) {
+        int r = b.tile_rep[t];
+        if (r < 0) continue;
+        const RepDesc& d = b.desc[r];
+        RepState& st = b.state[r];
+        if (!need_rebuild(st, d)) continue;
+        long long i = (long long)t * TILE + threadIdx.x;
+        Slots& S = b.s;
+        if (i < d.slot0 + d.n) {
+            if (d.dims == 3) {
+                if (nbr_full) build_particle<3, true>(b, d, st, i, nbr_full, ncnt_full, Kfull);
+                else build_particle<3, false>(b, d, st, i, nbr_full, ncnt_full, Kfull);
+            } else {
+                if (nbr_full) build_particle<2, true>(b, d, st, i, nbr_full, ncnt_full, Kfull);
+                else build_particle<2, false>(b, d, st, i, nbr_full, ncnt_full, Kfull);
+            }
+        } else {
+            S.ncnt[i] = 0;
+            if (nbr_full) ncnt_full[i] = 0;
+        }
+    }
+}
+
+// copy the staged (re-ordered) state back; separate kernel because the build
+// reads neighbours' staged positions
+__global__ void k_rb_copyback(Batch b)
+{
+    for (int t = blockIdx.x; t < b.ntiles; t += gridDim.x) {
+        int r = b.tile_rep[t];
+        if (r < 0) continue;
+        const RepDesc& d = b.desc[r];
+        if (!need_rebuild(b.state[r], d)) continue;
+        long long i = (long long)t * TILE + threadIdx.x;
+        Slots& S = b.s;
+        S.posD[i] = S.t_posD[i];
+        S.vx[i] = S.t_vx[i];
+        S.vy[i] = S.t_vy[i];
+        S.vz[i] = S.t_vz[i];
+        S.fx[i] = S.t_fx[i];
+        S.fy[i] = S.t_fy[i];
+        S.fz[i] = S.t_fz[i];
+        S.orig[i] = S.t_orig[i];
+    }
+}
+
+__global__ void k_rb_done(Batch b)
+{
+    int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= b.nreps) return;
+    const RepDesc& d = b.desc[r];
+    RepState& st = b.state[r];
+    if (!d.active || !need_rebuild(st, d)) return;
+    st.maxdisp2 = 0ull;
+    st.force_rebuild = 0;
+    st.rebuilds += 1;
+}
+
+void launch_rebuild_impl(const Batch& b, const LaunchCfg& lc, unsigned* nbr_full, int* ncnt_full, int Kfull)
+{
+    int g = lc.grid_stream;
+    k_rb_zero<<<g, TILE, 0, lc.stream>>>(b);
+    k_rb_bin<<<g, TILE, 0, lc.stream>>>(b);
+    k_rb_scan<<<b.nreps, 1024, 0, lc.stream>>>(b);
+    k_rb_scatter<<<g, TILE, 0, lc.stream>>>(b);
+    k_rb_cellsort<<<g, TILE, 0, lc.stream>>>(b);
+    k_rb_gather<<<g, TILE, 0, lc.stream>>>(b);
+    k_rb_build<<<g, TILE, 0, lc.stream>>>(b, nbr_full, ncnt_full, Kfull);
+    k_rb_copyback<<<g, TILE, 0, lc.stream>>>(b);
+    k_rb_done<<<(b.nreps + 127) / 128, 128, 0, lc.stream>>>(b);
+    if (lc.launches) *lc.launches += 9;
+}
+
+// ---------------------------------------------------------------------------
+// export of the lists in the reference layout: column-major (maxK, N),
+// 1-based ids, counts per particle.  half_only: the force list, each pair
+// once (owner = lower original id); otherwise the full Verlet list.
+// ---------------------------------------------------------------------------
+__global__ void k_export(Batch b, int rep, const unsigned* lst, const int* cnt, int rowstride_T,
+                         long long* counts, long long* list, long long maxK, int half_only,
+                         int* overflow)
+{
+    const RepDesc& d = b.desc[rep];
+    long long s = d.slot0 + (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= d.slot0 + d.n) return;
+    int oi = b.s.orig[s];
+    int n = cnt[s];
+    long long k = 0;
+    for (int q = 0; q < n; q++) {
+        unsigned e = half_only ? lst[nbr_addr(q, s, rowstride_T, b.S)] : lst[(size_t)q * b.S + s];
+        int oj = b.s.orig[e & IDX_MASK];
+        if (half_only && oj < oi) continue;
+        if (k < maxK) list[k + maxK * (long long)oi] = (long long)oj + 1;
+        else *overflow = 1;
+        k++;
+    }
+    counts[oi] = k;
+}
+
+void launch_export_impl(const Batch& b, const LaunchCfg& lc, int rep, const RepDesc& hd,
+                        const unsigned* lst, const int* cnt, int T, long long* counts, long long* list,
+                        long long maxK, int half_only, int* overflow)
+{
+    int blocks = (hd.n + 127) / 128;
+    if (blocks > 0)
+        k_export<<<blocks, 128, 0, lc.stream>>>(b, rep, lst, cnt, T, counts, list, maxK, half_only, overflow);
+    if (lc.launches) *lc.launches += 1;
+}
+
+}  // namespace simmd

@@ -1,0 +1,222 @@
+// simmd_internal.cuh -- device-side data model of libsimmd.
+//
+// Layout in HBM (one engine = one CUDA stream, many replicas):
+//   * a flat SLOT space; replica r owns slots [slot0, slot0 + npad), npad a
+//     multiple of TILE; slots hold particles in cell-sorted order after each
+//     rebuild, padding slots (orig < 0) never appear in a cell or a list;
+//   * per-slot SoA FP64 arrays v, F, displacement; an AoS double4_32a (x,y,z,D)
+//     gathered by neighbours; an AoS float4 of cell-relative FP32 offsets
+//     (split-precision path); packed rebuild-time cell coordinates; the
+//     original particle id;
+//   * a padded ELL neighbour list nbr[(n/T)*(S*T) + slot*T + n%T] (T = threads
+//     per particle) holding the slot of j in the low 26 bits and, for the
+//     split-precision path, the cell offset of j relative to i in the top 6;
+//   * per-replica descriptors (read-only) and states (flags, counters,
+//     reductions), a tile -> replica table and per-tile partial sums.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace simmd {
+
+constexpr int TILE = 128;                       // slots per tile (work unit)
+constexpr int IDX_BITS = 26;
+constexpr unsigned IDX_MASK = (1u << IDX_BITS) - 1u;
+constexpr int MAX_CELLS_AXIS = 1023;
+constexpr int NPART = 8;                        // doubles of partial sums per tile
+
+enum { POT_LJ = 0, POT_BERTHIER = 1 };
+enum { DYN_NEWTONIAN = 0, DYN_LANGEVIN = 1, DYN_BROWNIAN = 2 };
+enum { PREC_FP64 = 0, PREC_FP32 = 1 };
+enum { NOISE_PHILOX = 0, NOISE_HOST = 1 };
+
+struct RepDesc {
+    long long slot0;
+    int n, npad;
+    int tile0, ntiles;
+    int cell0, ncell;          // cells [cell0, cell0+ncell) + pad cell + end marker
+    int dims, pot, dyn, prec;
+    int nc;                    // cells per axis (1 or >= 3); cubic box
+    int rescale;
+    int noise_mode;
+    int active;
+    double L, halfL, cs, inv_cs;
+    double rc2, rcut, skin, rv2, skin_half2;
+    double sigma2, sigma4, lj_cut2, eps, Uc, c0, c2, c4, zeta;
+    double kBT, gamma, dt, m, noise_factor, dt_over_gamma, two_m, m_half;
+    double relax_cap;          // > 0: capped steepest descent (set-up relaxation), no noise
+    float Lf, halfLf, csf, rc2f, rcutf, skinf, sigma2f, sigma4f, cut2f, epsf, Ucf, c0f, c2f, c4f, zetaf;
+    unsigned long long seed;
+    const double* host_noise;  // [noise_nsteps][n][dims], original order
+    long long noise_step0;
+    int noise_nsteps;
+    int pad_;
+};
+
+struct RepState {
+    unsigned long long maxdisp2;  // bits of the max |disp|^2 (non-negative double)
+    int force_rebuild;
+    int overflow;
+    int nonfinite;
+    int done_count;
+    int maxcount;
+    int noise_range_error;
+    long long step;               // noise draws so far (Philox counter)
+    long long rebuilds;
+    long long list_entries;       // total list length at the last rebuild
+    double vmean[3];              // pending centre-of-mass velocity (Newtonian/Langevin)
+    double fmean[3];              // mean force (Brownian)
+    double vscale;                // pending velocity rescale factor
+    double epot, virial, ekin;
+    double fmax;
+};
+
+struct Slots {
+    double4_32a* posD;                // x, y, z, D
+    double *vx, *vy, *vz;
+    double *fx, *fy, *fz;
+    double *ux, *uy, *uz;         // displacement since the last rebuild
+    float4* off;                  // split precision: cell-relative offsets, D
+    int* cellc;                   // packed rebuild-time cell coords (10 bits each)
+    int* orig;                    // original id, -1 for padding
+    unsigned* nbr;                // ELL neighbour list
+    int* ncnt;                    // neighbours per slot
+    // rebuild scratch
+    int* bin_cell;
+    int* bin_rank;
+    int* src;
+    double4_32a* t_posD;
+    double *t_vx, *t_vy, *t_vz, *t_fx, *t_fy, *t_fz;
+    int* t_orig;
+    int* cell_count;              // per cell (+ pad cell)
+    int* cell_start;              // per cell (+ pad cell + end)
+};
+
+struct Batch {
+    const RepDesc* desc;
+    RepState* state;
+    const int* tile_rep;          // tile -> replica (-1: unused)
+    int ntiles;                   // tiles in the slot space
+    int nreps;                    // replica table size
+    long long S;                  // slot capacity
+    int K;                        // list rows
+    int tpp;                      // threads per particle (list interleave)
+    Slots s;
+    double* tile_part;            // [ntiles][NPART]
+    int* queue;                   // work-queue heads [4]
+};
+
+// ---------------------------------------------------------------------------
+// exact FP64 helpers: explicit round-to-nearest intrinsics, never contracted
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double dmul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double dadd(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double dsub(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ double ddiv(double a, double b) { return __ddiv_rn(a, b); }
+__device__ __forceinline__ double drcp(double a) { return __drcp_rn(a); }
+
+// dx - round(dx/L)*L for |dx| < L, decided on the bit pattern (integer pipe):
+// identical to the reference whenever |dx| is not within an ulp of L/2, i.e.
+// for every pair closer than L/2.
+__device__ __forceinline__ double min_image_f64(double dx, long long halfL_bits, double L)
+{
+    long long b = __double_as_longlong(dx);
+    long long a = b & 0x7fffffffffffffffLL;
+    double sh = (a > halfL_bits) ? ((b < 0) ? -L : L) : 0.0;
+    return dsub(dx, sh);
+}
+
+__device__ __forceinline__ float min_image_f32(float dx, float halfL, float L)
+{
+    dx = (dx > halfL) ? dx - L : dx;
+    dx = (dx < -halfL) ? dx + L : dx;
+    return dx;
+}
+
+__device__ __forceinline__ bool need_rebuild(const RepState& st, const RepDesc& d)
+{
+    return st.force_rebuild || (__longlong_as_double((long long)st.maxdisp2) > d.skin_half2);
+}
+
+__device__ __forceinline__ size_t nbr_addr(int n, long long slot, int T, long long S)
+{
+    return (size_t)(n / T) * (size_t)(S * T) + (size_t)slot * T + (size_t)(n % T);
+}
+
+// ---------------------------------------------------------------------------
+// Philox4x32-10 (Salmon et al., SC'11) and Box-Muller normals
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint4 philox4x32_10(uint4 c, uint2 k)
+{
+#pragma unroll
+    for (int r = 0; r < 10; r++) {
+        unsigned hi0 = __umulhi(0xD2511F53u, c.x), lo0 = 0xD2511F53u * c.x;
+        unsigned hi1 = __umulhi(0xCD9E8D57u, c.z), lo1 = 0xCD9E8D57u * c.z;
+        c = make_uint4(hi1 ^ c.y ^ k.x, lo1, hi0 ^ c.w ^ k.y, lo0);
+        k.x += 0x9E3779B9u;
+        k.y += 0xBB67AE85u;
+    }
+    return c;
+}
+
+// two N(0,1) deviates for (seed, step, particle, pair); FP64 version matches
+// the oracle's orc_philox_normals to a few ulp
+__device__ __forceinline__ void normal_pair_f64(unsigned long long seed, long long step, int particle,
+                                                int pair, double& z0, double& z1)
+{
+    uint4 o = philox4x32_10(make_uint4((unsigned)particle, (unsigned)pair, (unsigned)step,
+                                       (unsigned)((unsigned long long)step >> 32)),
+                            make_uint2((unsigned)seed, (unsigned)(seed >> 32)));
+    unsigned long long a = ((unsigned long long)o.x << 21) | (o.y >> 11);
+    unsigned long long b = ((unsigned long long)o.z << 21) | (o.w >> 11);
+    double u = ((double)a + 1.0) * 0x1.0p-53;
+    double w = (double)b * 0x1.0p-53;
+    double rad = sqrt(-2.0 * log(u));
+    double s, c;
+    sincospi(2.0 * w, &s, &c);
+    z0 = rad * c;
+    z1 = rad * s;
+}
+
+// FP32 deviates (split-precision path): 24-bit uniforms, |z| <= 5.8
+__device__ __forceinline__ void normal_pair_f32(unsigned long long seed, long long step, int particle,
+                                                int pair, float& z0, float& z1)
+{
+    uint4 o = philox4x32_10(make_uint4((unsigned)particle, (unsigned)pair, (unsigned)step,
+                                       (unsigned)((unsigned long long)step >> 32)),
+                            make_uint2((unsigned)seed, (unsigned)(seed >> 32)));
+    float u = ((float)(o.x >> 8) + 1.0f) * 0x1.0p-24f;
+    float w = (float)(o.z >> 8) * 0x1.0p-24f;
+    float rad = sqrtf(-2.0f * logf(u));
+    float s, c;
+    sincospif(2.0f * w, &s, &c);
+    z0 = rad * c;
+    z1 = rad * s;
+}
+
+// ---------------------------------------------------------------------------
+// kernel launchers (host side, defined in the .cu files)
+// ---------------------------------------------------------------------------
+struct LaunchCfg {
+    cudaStream_t stream;
+    int grid_stream;      // blocks for streaming kernels
+    int grid_force;       // blocks for the persistent force kernel
+    long long* launches;  // launch counter
+};
+
+void launch_load_aos(const Batch& b, const LaunchCfg& lc, int rep, const RepDesc& hd, const double* r,
+                     const double* v, const double* F, const double* D, const double* disp);
+void launch_store_aos(const Batch& b, const LaunchCfg& lc, int rep, const RepDesc& hd, double* r,
+                      double* v, double* F, double* disp, double* epp);
+void launch_rebuild(const Batch& b, const LaunchCfg& lc, int full_list_mode);
+void launch_kick_drift(const Batch& b, const LaunchCfg& lc, int has_rescale);
+void launch_force(const Batch& b, const LaunchCfg& lc, int mode);
+void launch_brownian_update(const Batch& b, const LaunchCfg& lc);
+void launch_finalize(const Batch& b, const LaunchCfg& lc, int has_rescale);
+void launch_kinetic(const Batch& b, const LaunchCfg& lc);
+void launch_export_list(const Batch& b, const LaunchCfg& lc, int rep, const RepDesc& hd,
+                        long long* counts, long long* list, long long maxK, int half_only);
+
+enum { FMODE_STEP = 0, FMODE_FORCES = 1, FMODE_ENERGY = 2, FMODE_STEP_ENERGY = 3 };
+
+}  // namespace simmd

@@ -1,0 +1,116 @@
+"""Seeded synthetic workloads with the shapes, sizes and value distributions of
+the reference's MD configurations (no dataset is involved):
+
+  c1  3D LJ (eps = sigma = 1, rc = 2.5), N = 1000, rho = 1 (L = 10), 10^3
+      simple-cubic lattice + uniform jitter +-0.05, Gaussian v at kBT = 0.1
+      with zero momentum, Newtonian velocity Verlet dt = 0.01, skin 0.3
+  c2  3D polydisperse soft spheres (Berthier), N = 32768, rho = 1.02,
+      Langevin gamma = 1, kBT = 0.1, dt = 0.005, skin 0.3
+  c3  the c2 system at N = 2^20, Newtonian NVE, dt = 0.005
+  c4  512 replicas, N log-uniform in [500, 16384], half 2D / half 3D,
+      Berthier at rho = 1.02, Brownian mobility 1, kBT = 0.1, dt = 1e-3,
+      skin 0.3
+Berthier diameters: regular inverse-CDF quantiles of P(D) ~ D^-3 with
+sigma_ratio 2.219 (support [0.7253, 1.6095]), shuffled
+(generate_diameters!, src/InitialConfiguration.jl:1-11); positions seeded
+uniform random, then relaxed on the GPU by simmd_relax (capped steepest
+descent) in place of the reference's MC sweeps at kBT = 10.
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+from . import _lib
+from .batch import ReplicaSpec
+from .structs import Berthier, LJ
+
+
+def berthier_diameters(N, rng, sigma_ratio=2.219):
+    A = 1 / 2 + 1 / (sigma_ratio - 1)
+    smin = (1 + sigma_ratio) / (2 * sigma_ratio)
+    P = np.linspace(1 / (2 * N), 1 - 1 / (2 * N), N)
+    return rng.permutation(np.sqrt(1 / (smin ** -2 - 2 * P / A)))
+
+
+def gaussian_velocities(N, dims, kBT, m, rng):
+    v = rng.standard_normal((N, dims)) * math.sqrt(kBT / m)
+    return v - v.mean(0)
+
+
+def berthier_spec(N, dims, dynamics, rng, *, rho=1.02, skin=0.3, kBT=0.1, gamma=1.0, dt=0.005,
+                  precision=_lib.FP64, seed=1, max_neighbors=None):
+    U = Berthier()
+    L = (N / rho) ** (1.0 / dims)
+    D = berthier_diameters(N, rng)
+    r = rng.uniform(0.0, L, (N, dims))
+    v = gaussian_velocities(N, dims, kBT, 1.0, rng) if dynamics != _lib.BROWNIAN else None
+    if max_neighbors is None:
+        max_neighbors = 64 if dims == 3 else 32
+    return ReplicaSpec(dims=dims, potential=_lib.POT_BERTHIER, dynamics=dynamics, N=N, box_size=L,
+                       force_cutoff2=U.rc ** 2, skin=skin, verlet_force_cutoff=U.rc, r=r, D=D, v=v,
+                       precision=precision, kBT=kBT, gamma=gamma, dt=dt, b_c0=U.c0, b_c2=U.c2, b_c4=U.c4,
+                       b_zeta=U.zeta, max_neighbors=max_neighbors, seed=seed)
+
+
+def lj_spec(N, dims, dynamics, rng, *, rho=1.0, skin=0.3, kBT=0.1, gamma=1.0, dt=0.01, precision=_lib.FP64,
+            seed=1, lattice=True, max_neighbors=None):
+    U = LJ(1.0, 1.0, 2.5)
+    L = (N / rho) ** (1.0 / dims)
+    n = int(round(N ** (1.0 / dims)))
+    if lattice and n ** dims == N:
+        a = L / n
+        g = np.stack(np.meshgrid(*([np.arange(n)] * dims), indexing="ij"), -1).reshape(-1, dims)
+        r = np.mod((g + 0.5) * a + rng.uniform(-0.05, 0.05, (N, dims)), L)
+    else:
+        r = rng.uniform(0.0, L, (N, dims))
+    v = gaussian_velocities(N, dims, kBT, 1.0, rng) if dynamics != _lib.BROWNIAN else None
+    if max_neighbors is None:
+        max_neighbors = 128 if dims == 3 else 48
+    return ReplicaSpec(dims=dims, potential=_lib.POT_LJ, dynamics=dynamics, N=N, box_size=L, force_cutoff2=6.25,
+                       skin=skin, verlet_force_cutoff=2.5, r=r, D=np.ones(N), v=v, precision=precision, kBT=kBT,
+                       gamma=gamma, dt=dt, lj_eps=1.0, lj_sigma=1.0, lj_Uc=U.Uc, max_neighbors=max_neighbors,
+                       seed=seed)
+
+
+def c1(precision=_lib.FP64, seed=1):
+    rng = np.random.default_rng(seed)
+    return [lj_spec(1000, 3, _lib.NEWTONIAN, rng, dt=0.01, precision=precision, seed=seed)]
+
+
+def c2(precision=_lib.FP64, seed=2):
+    rng = np.random.default_rng(seed)
+    return [berthier_spec(32768, 3, _lib.LANGEVIN, rng, dt=0.005, precision=precision, seed=seed)]
+
+
+def c3(precision=_lib.FP64, seed=3):
+    rng = np.random.default_rng(seed)
+    return [berthier_spec(1 << 20, 3, _lib.NEWTONIAN, rng, dt=0.005, precision=precision, seed=seed)]
+
+
+def c4_sizes(nrep=512, seed=4, lo=500, hi=16384):
+    rng = np.random.default_rng(seed)
+    return np.floor(np.exp(rng.uniform(math.log(lo), math.log(hi), nrep))).astype(int)
+
+
+def c4(precision=_lib.FP32_SPLIT, seed=4, nrep=512):
+    sizes = c4_sizes(nrep, seed)
+    specs = []
+    for k, N in enumerate(sizes):
+        rng = np.random.default_rng(seed * 100003 + k)
+        dims = 2 if k % 2 == 0 else 3
+        specs.append(berthier_spec(int(N), dims, _lib.BROWNIAN, rng, dt=1e-3, precision=precision,
+                                   seed=seed * 1000 + k))
+    return specs
+
+
+WORKLOADS = {"c1": c1, "c2": c2, "c3": c3, "c4": c4}
+
+DESCRIPTIONS = {
+    "c1": "3D LJ N=1000 rho=1 lattice, Newtonian dt=0.01, skin 0.3",
+    "c2": "3D polydisperse soft spheres N=32768 rho=1.02, Langevin gamma=1 kBT=0.1 dt=0.005, skin 0.3",
+    "c3": "3D polydisperse soft spheres N=1048576 rho=1.02, Newtonian NVE dt=0.005, skin 0.3",
+    "c4": "512 replicas, N log-uniform [500,16384], half 2D/half 3D polydisperse soft spheres rho=1.02, "
+          "Brownian mu=1 kBT=0.1 dt=1e-3, skin 0.3",
+}

@@ -1,0 +1,58 @@
+"""Seeded synthetic systems shared by the oracle and GPU tests.
+
+Shapes and value distributions follow the reference's workloads: LJ at
+rho = 1 on a jittered simple-cubic lattice (eps = sigma = 1, rc = 2.5) and
+polydisperse Berthier soft spheres (D ~ P(D) ∝ D^-3 on [0.7253, 1.6095],
+zeta = 0.2, rc = 1.25) at rho = 1.02 relaxed by the oracle's restatement of
+find_random_initial_configuration! (MC at kBT = 10).
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+from oracle import pyoracle as O
+
+
+def lattice_positions(N, dims, L, jitter, rng):
+    n = int(round(N ** (1.0 / dims)))
+    assert n ** dims == N
+    a = L / n
+    g = np.stack(np.meshgrid(*([np.arange(n)] * dims), indexing="ij"), -1).reshape(-1, dims).astype(float)
+    r = (g + 0.5) * a + rng.uniform(-jitter, jitter, (N, dims))
+    return np.mod(r, L)
+
+
+def make_case(pot, dims, dyn, N, *, rho=None, skin=0.3, seed=0, mc_sweeps=40, dt=None, kBT=0.1, gamma=1.0,
+              jitter=0.05, vel=True):
+    """Returns (oracle params, r, v, D, force_cutoff) for a seeded system."""
+    rng = np.random.default_rng(seed)
+    if pot == O.POT_LJ:
+        rho = 1.0 if rho is None else rho
+        L = (N / rho) ** (1.0 / dims)
+        rc = 2.5
+        D = np.ones(N)
+        p = O.make_params(dims, O.POT_LJ, dyn, N, L, rc * rc, skin, eps=1.0, sigma=1.0, lj_rc=rc, kBT=kBT,
+                          gamma=gamma, dt=dt or 0.005)
+        n = int(round(N ** (1.0 / dims)))
+        if n ** dims == N:
+            r = lattice_positions(N, dims, L, jitter, rng)
+        else:
+            r = rng.uniform(0, L, (N, dims))
+    else:
+        rho = 1.02 if rho is None else rho
+        L = (N / rho) ** (1.0 / dims)
+        rc = 1.25
+        D = O.generate_diameters_berthier(N, 2.219, seed + 11)
+        p = O.make_params(dims, O.POT_BERTHIER, dyn, N, L, rc * rc, skin, zeta=0.2, berthier_rc=rc, kBT=kBT,
+                          gamma=gamma, dt=dt or 0.005)
+        if mc_sweeps > 0:
+            r, _ = O.random_initial_configuration(p, D, mc_sweeps, max_disp=0.1, seed=seed + 5, skin=0.6)
+        else:
+            r = rng.uniform(0, L, (N, dims))
+    v = None
+    if vel and dyn != O.BROWNIAN:
+        v = rng.standard_normal((N, dims)) * math.sqrt(kBT)
+        v -= v.mean(0)
+    return p, r, v, D, rc
