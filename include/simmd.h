@@ -181,6 +181,28 @@ int simmd_stats_r(simmd_ctx* ctx, int32_t rep, simmd_stats* out);
 /* device bytes a replica of this shape needs (admission against a budget) */
 int64_t simmd_replica_bytes(const simmd_params* p, int32_t max_neighbors);
 
+/* ---- energy without device allocation ----------------------------------- */
+
+/* No counterpart in the reference.  For callers that must not allocate
+ * device memory -- e.g. a Julia program whose GPU memory belongs to
+ * CUDA.jl's pool, a host enforcing its own device-memory budget, or a loop
+ * that cannot afford an allocation's latency or implicit synchronisation.
+ * Computes, on the caller's stream (NULL: the default stream) and without
+ * any cudaMalloc/cudaFree, out[0] = the potential energy of
+ * calculate_full_energy, out[1] = the virial W = sum_pairs r_ij . F_ij and
+ * out[2] = the number of invalid list entries skipped, from DEVICE arrays the
+ * caller owns: r (dims x N AoS), D (N), the full neighbour list as in the
+ * reference (counts[N], list[maxK*N] column-major, 1-based) and out[3].
+ * Scratch is a fixed array inside the library, shared by every call on a
+ * GPU: N must be <= SIMMD_NOALLOC_MAX_N (else SIMMD_ERR_BUDGET), and calls
+ * that run concurrently on the same GPU race.  The first call on a device
+ * performs a one-time symbol lookup; make it before any stream capture.
+ * Asynchronous: synchronise the stream before reading out. */
+#define SIMMD_NOALLOC_MAX_N 1048576
+int simmd_energy_virial_noalloc(const simmd_params* p, const double* r, const double* D,
+                                const int64_t* counts, const int64_t* list, int64_t maxK,
+                                double* out, void* stream);
+
 /* ---- tuning, timing, plumbing ------------------------------------------ */
 
 /* threads per particle in the force pass (1, 2, 4), CUDA-graph capture of

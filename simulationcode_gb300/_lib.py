@@ -98,6 +98,7 @@ SIGNATURES = {
     "simmd_relax": (C.c_int, [_vp, C.c_int64, C.c_double]),
     "simmd_host_register": (C.c_int, [_vp, C.c_int64]),
     "simmd_host_unregister": (C.c_int, [_vp]),
+    "simmd_energy_virial_noalloc": (C.c_int, [_P(Params), _vp, _vp, _vp, _vp, C.c_int64, _vp, _vp]),
     "simmd_profile_get": (C.c_int, [_vp, _vp]),
 }
 
