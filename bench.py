@@ -79,20 +79,32 @@ class ClockSampler:
         self.gpu = gpu_index
         self.proc = None
         self.lines = []
+        self.t0 = self.t1 = None
 
     def start(self):
+        """start sampling and wait for the first sample (the sampler's own
+        start-up stays outside the timed region)"""
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
                                           "--format=csv,noheader,nounits", "-lms", "100"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.th = threading.Thread(target=self._read, daemon=True)
             self.th.start()
+            t = time.time()
+            while not self.lines and time.time() - t < 10:
+                time.sleep(0.05)
         except Exception:
             self.proc = None
 
     def _read(self):
         for line in self.proc.stdout:
-            self.lines.append(line.strip())
+            self.lines.append((time.time(), line.strip()))
+
+    def mark(self, begin):
+        if begin:
+            self.t0 = time.time()
+        else:
+            self.t1 = time.time()
 
     def stop(self):
         if self.proc is None:
@@ -104,7 +116,12 @@ class ClockSampler:
             self.proc.kill()
         sm, smax, reasons = [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ln in self.lines:
+        lines = self.lines
+        if self.t0 is not None and self.t1 is not None:
+            inside = [x for x in lines if self.t0 - 0.15 <= x[0] <= self.t1 + 0.15]
+            if inside:
+                lines = inside
+        for _, ln in lines:
             f = [x.strip() for x in ln.split(",")]
             if len(f) < 9:
                 continue
@@ -155,7 +172,7 @@ def build_batch(specs, device, tpp):
     return b, ids
 
 
-def relax_specs(specs, device, steps=300, cap=0.05):
+def relax_specs(specs, device, steps=300, step_size=1e-3, cap=0.05):
     """Set-up relaxation on the GPU in FP64; returns relaxed positions."""
     from simulationcode_gb300 import _lib
     import copy
@@ -166,10 +183,73 @@ def relax_specs(specs, device, steps=300, cap=0.05):
         tmp.append(t)
     b, ids = build_batch(tmp, device, 1)
     b.rebuild()
-    b.relax(steps, cap)
+    b.relax(steps, step_size, cap)
     out = [b.state(i)[0] for i in ids]
+    fmax = max(float(np.abs(b.state(i)[2]).max()) for i in ids[:64])
+    print("relaxed: max |F| over the first replicas %.3g" % fmax, file=sys.stderr, flush=True)
+    relax_launches[0] += b.launches()
     b.close()
     return out
+
+
+relax_launches = [0]
+
+
+def plain_fp64_one_at_a_time(specs, device, steps=32):
+    """The plain FP64 path run one replica at a time: a context per replica,
+    device-timed steps summed over replicas."""
+    import copy
+    from simulationcode_gb300 import _lib
+    from simulationcode_gb300.batch import ReplicaBatch
+    tot_ps, tot_ms = 0, 0.0
+    for s in specs:
+        t = copy.copy(s)
+        t.precision = _lib.FP64
+        b = ReplicaBatch(device, tpp=1, graphs=True, graph_steps=16)
+        b.add(t)
+        b.rebuild()
+        b.step(3)
+        b.timer_start()
+        b.step(steps)
+        tot_ms += b.timer_stop()
+        tot_ps += t.N * steps
+        b.close()
+    return {"value": tot_ps / (tot_ms / 1000.0), "unit": "particle-steps/s", "steps_per_replica": steps,
+            "replicas": len(specs)}
+
+
+def split_precision_error(specs, device, nsample=16):
+    """FP32-split vs FP64 on the same configurations (pair forces, Newtonian
+    copies so no noise enters): force relative RMS and |dE|/N."""
+    import copy
+    from simulationcode_gb300 import _lib
+    from simulationcode_gb300.batch import ReplicaBatch
+    sample = specs[:nsample]
+    num = den = 0.0
+    de = 0.0
+    n = 0
+    res = {}
+    for prec in (_lib.FP64, _lib.FP32_SPLIT):
+        b = ReplicaBatch(device)
+        ids = []
+        for s in sample:
+            t = copy.copy(s)
+            t.precision = prec
+            t.dynamics = _lib.NEWTONIAN
+            t.v = np.zeros_like(s.r)
+            ids.append(b.add(t))
+        b.rebuild()
+        _lib.check(b.lib.simmd_forces(b.ctx, None, None))
+        en = b.energies()
+        res[prec] = [(b.state(i)[2], en[i].epot) for i in ids]
+        b.close()
+    for (f64, e64), (f32, e32), s in zip(res[_lib.FP64], res[_lib.FP32_SPLIT], sample):
+        num += float(((f32 - f64) ** 2).sum())
+        den += float((f64 ** 2).sum())
+        de += abs(e32 - e64)
+        n += s.N
+    return {"force_rel_rms": math.sqrt(num / den), "energy_abs_per_particle": de / n,
+            "replicas_sampled": len(sample)}
 
 
 def cpu_baseline_port(specs, seconds=12.0):
@@ -265,21 +345,27 @@ def run_gpu(args, dist):
     prec = {"fp64": _lib.FP64, "fp32": _lib.FP32_SPLIT}[args.precision] if args.precision else None
     specs = W.WORKLOADS[args.workload]() if prec is None else W.WORKLOADS[args.workload](precision=prec)
     # set-up: relax random starts on the GPU (not timed)
-    if any(s.potential == _lib.POT_BERTHIER for s in specs):
-        rel = relax_specs(specs, device)
+    if any(s.potential == _lib.POT_BERTHIER for s in specs) and args.relax_steps > 0:
+        rel = relax_specs(specs, device, steps=args.relax_steps)
         for s, r in zip(specs, rel):
             s.r = r
     batch, ids = build_batch(specs, device, args.tpp)
     batch.rebuild()
     batch.step(args.warmup)
     st_before = [batch.stats(i) for i in ids]
-    dist.barrier()
+    # kernel launches of this process before the timed region (for ncu -s)
+    print("LAUNCHES_BEFORE_TIMED=%d FORCE_LAUNCHES_BEFORE_TIMED=%d BUILD_LAUNCHES_BEFORE_TIMED=%d" % (
+        relax_launches[0] + batch.launches(), args.relax_steps + args.warmup, args.relax_steps + 2 + args.warmup),
+        file=sys.stderr, flush=True)
     clocks = ClockSampler(device)
     clocks.start()
+    dist.barrier()
     l0 = batch.launches()
+    clocks.mark(True)
     batch.timer_start()
     batch.step(args.steps)
     ms = batch.timer_stop()
+    clocks.mark(False)
     launches = batch.launches() - l0
     clk = clocks.stop()
     ms = dist.max(ms)
@@ -290,10 +376,14 @@ def run_gpu(args, dist):
 
     # force-kernel duration: CUDA events around every force launch of an
     # instrumented pass of the same step loop (direct launches)
-    batch.profile(True)
-    batch.step(max(16, min(args.steps, 64)))
-    prof = batch.profile_get()
-    batch.profile(False)
+    if args.no_profile_pass:
+        prof = {"force_ms": float("nan"), "force_n": 1, "kick_ms": 0.0, "rebuild_ms": 0.0, "update_ms": 0.0,
+                "steps": 1}
+    else:
+        batch.profile(True)
+        batch.step(max(16, min(args.steps, 64)))
+        prof = batch.profile_get()
+        batch.profile(False)
     force_ms = prof["force_ms"] / max(prof["force_n"], 1)
     stats = [batch.stats(i) for i in ids]
     fbytes = force_bytes_per_launch(specs, stats)
@@ -325,11 +415,14 @@ def run_gpu(args, dist):
         d2h += r.nbytes + F.nbytes + (v.nbytes if s.dynamics != 2 else 0)
     e2e_steps = args.steps
     dist.barrier()
+    if args.no_e2e:
+        e2e_steps = 0
     t0 = time.perf_counter()
     for rid, s, (r, v, D, F, outs) in zip(ids, specs, host):
         _lib.check(lib.simmd_upload_r(batch.ctx, rid, _lib.ptr(r), _lib.ptr(v) if s.dynamics != 2 else None,
                                       None, _lib.ptr(D), None))
-    _lib.check(lib.simmd_step(batch.ctx, e2e_steps, None))
+    if e2e_steps:
+        _lib.check(lib.simmd_step(batch.ctx, e2e_steps, None))
     for rid, s, (r, v, D, F, outs) in zip(ids, specs, host):
         _lib.check(lib.simmd_download_r(batch.ctx, rid, _lib.ptr(outs[0]),
                                         _lib.ptr(outs[1]) if s.dynamics != 2 else None, _lib.ptr(outs[2]), None))
@@ -337,18 +430,23 @@ def run_gpu(args, dist):
     for (r, v, D, F, outs) in host:
         for a in [r, v, D, F] + outs:
             lib.simmd_host_unregister(C.c_void_p(a.ctypes.data))
+    e2e_steps = max(e2e_steps, 1)
     e2e = {"value": n * e2e_steps / e2e_s, "unit": "particle-steps/s",
            "h2d_bytes_per_step": h2d / e2e_steps, "d2h_bytes_per_step": d2h / e2e_steps,
            "what": "simmd_upload_r (r, v, D from page-locked host) + simmd_step(K) + simmd_download_r (r, v, F) "
                    "for every replica, wall clock"}
 
+    # bytes streamed per step: force launch + positions, velocities, forces,
+    # displacements of the integrator pass
+    step_bytes = fbytes + sum(s.N * 8 * s.dims * 6 for s in specs)
     dtype = "f64" if all(s.precision == 0 for s in specs) else "f32-split (f32 pair math, f64 integration)"
     line = {"metric": "particle-steps/s", "value": value, "unit": "particle-steps/s", "n_gpus": dist.ws,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": dtype, "data": "synthetic",
             "config": {"workload": args.workload, "description": W.DESCRIPTIONS[args.workload], "particles": n,
                        "replicas": len(specs), "threads_per_particle": args.tpp,
-                       "l2": "state larger than L2" if batch.device_bytes() > 129e6 else "state fits in L2 (no flush)",
+                       "l2": ("state larger than L2 (%.0f MB streamed per step)" % (step_bytes / 1e6))
+                             if step_bytes > 129e6 else "state fits in L2 (%.0f MB; no flush)" % (step_bytes / 1e6),
                        "parallelism": "replicas only" if dist.ws > 1 else "single GPU",
                        "rebuilds_in_timed_region": rebuilds},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
@@ -358,9 +456,14 @@ def run_gpu(args, dist):
             "step_breakdown_ms": {k: prof[k] / max(prof["steps"], 1) for k in ("force_ms", "kick_ms", "rebuild_ms",
                                                                                "update_ms")},
             "e2e": e2e, "gpu_launches": int(launches), "clocks": clk}
+    batch.close()
+    if dist.rank == 0 and any(s.precision != 0 for s in specs) and not args.no_compare:
+        plain = plain_fp64_one_at_a_time(specs, device)
+        line["plain_fp64_one_at_a_time"] = plain
+        line["speedup_vs_plain_fp64"] = value / plain["value"]
+        line["split_precision_error"] = split_precision_error(specs, device)
     if dist.rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline_port(specs, seconds=args.cpu_seconds)
-    batch.close()
     return line
 
 
@@ -370,11 +473,15 @@ def main():
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="c2", choices=["c1", "c2", "c3", "c4"])
+    ap.add_argument("--workload", default="c4", choices=["c1", "c2", "c3", "c4"])
     ap.add_argument("--precision", default=None, choices=[None, "fp64", "fp32"])
     ap.add_argument("--tpp", type=int, default=1)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-compare", action="store_true", help="skip the plain-FP64 and error comparisons")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-profile-pass", action="store_true")
+    ap.add_argument("--relax-steps", type=int, default=300)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

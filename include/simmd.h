@@ -138,12 +138,12 @@ int simmd_forces(simmd_ctx* ctx, const double* noise, double* F_out);
 int simmd_step(simmd_ctx* ctx, int64_t nsteps, const double* noise);
 
 /* Set-up relaxation (not a reference routine): nsteps of steepest descent
- * r += F with each particle's move capped at max_disp, FP64, no noise, for
+ * r += step_size * F with each particle's move capped at max_disp, FP64, no noise, for
  * every replica; removes the overlaps of random initial positions before
  * dynamics (the role of find_random_initial_configuration!'s MC sweeps,
  * src/InitialConfiguration.jl:43-114).  Velocities are kept; F holds the
  * last relaxation forces. */
-int simmd_relax(simmd_ctx* ctx, int64_t nsteps, double max_disp);
+int simmd_relax(simmd_ctx* ctx, int64_t nsteps, double step_size, double max_disp);
 
 /* calculate_full_energy (epot), virial W = sum_pairs r_ij . F_ij, and
  * find_kinetic_energy (ekin) of replica 0; any pointer may be NULL. */

@@ -95,7 +95,7 @@ SIGNATURES = {
     "simmd_device_bytes": (C.c_int64, [_vp]),
     "simmd_time_force": (C.c_int, [_vp, C.c_int32, _P(C.c_float)]),
     "simmd_set_profile": (C.c_int, [_vp, C.c_int32]),
-    "simmd_relax": (C.c_int, [_vp, C.c_int64, C.c_double]),
+    "simmd_relax": (C.c_int, [_vp, C.c_int64, C.c_double, C.c_double]),
     "simmd_host_register": (C.c_int, [_vp, C.c_int64]),
     "simmd_host_unregister": (C.c_int, [_vp]),
     "simmd_energy_virial_noalloc": (C.c_int, [_P(Params), _vp, _vp, _vp, _vp, C.c_int64, _vp, _vp]),

@@ -94,8 +94,9 @@ class ReplicaBatch:
     def rebuild(self):
         _lib.check(self.lib.simmd_rebuild(self.ctx))
 
-    def relax(self, nsteps: int, max_disp: float):
-        _lib.check(self.lib.simmd_relax(self.ctx, nsteps, max_disp))
+    def relax(self, nsteps: int, step_size: float = 1e-3, max_disp: float = 0.05):
+        """capped steepest descent r += step_size*F, |dr| <= max_disp (set-up)"""
+        _lib.check(self.lib.simmd_relax(self.ctx, nsteps, step_size, max_disp))
 
     def step(self, nsteps: int):
         _lib.check(self.lib.simmd_step(self.ctx, int(nsteps), None))

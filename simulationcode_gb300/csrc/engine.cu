@@ -30,8 +30,8 @@ void launch_rebuild_impl(const Batch& b, const LaunchCfg& lc, unsigned* nbr_full
 void launch_export_impl(const Batch& b, const LaunchCfg& lc, int rep, const RepDesc& hd, const unsigned* lst,
                         const int* cnt, int T, long long* counts, long long* list, long long maxK, int half_only,
                         int* overflow);
-void launch_force_impl(const Batch& b, const LaunchCfg& lc, int mode, int grid, double* epp);
-int force_blocks_per_sm(int T, int mode);
+void launch_force_impl(const Batch& b, const LaunchCfg& lc, int mode, int prec_mask, double* epp);
+int force_blocks_per_sm(int T, int mode, int prec);
 void launch_kick_drift_impl(const Batch& b, const LaunchCfg& lc);
 void launch_brownian_update_impl(const Batch& b, const LaunchCfg& lc);
 void launch_rescale_impl(const Batch& b, const LaunchCfg& lc);
@@ -222,7 +222,7 @@ static int ensure_capacity(simmd_ctx* c, long long S_need, long long C_need, int
         TRY(grow_keep(c, &s.ux, S_old, S_new));
         TRY(grow_keep(c, &s.uy, S_old, S_new));
         TRY(grow_keep(c, &s.uz, S_old, S_new));
-        TRY(grow_keep(c, &s.off, S_old, S_new));
+        TRY(grow_keep(c, &s.rec, S_old, S_new));
         TRY(grow_keep(c, &s.cellc, S_old, S_new));
         TRY(grow_keep(c, &s.orig, S_old, S_new));
         TRY(grow_fresh(c, &s.ncnt, S_old, S_new));
@@ -341,7 +341,8 @@ static LaunchCfg make_lc(simmd_ctx* c, int mode)
     lc.stream = c->stream;
     long long nt = c->S_cap / TILE;
     lc.grid_stream = (int)std::max(1LL, std::min(nt, (long long)c->sm_count * 16));
-    lc.grid_force = c->sm_count * force_blocks_per_sm(c->T, mode);
+    lc.grid_force64 = c->sm_count * force_blocks_per_sm(c->T, mode, PREC_FP64);
+    lc.grid_force32 = c->sm_count * force_blocks_per_sm(c->T, mode, PREC_FP32);
     lc.launches = &c->launches;
     return lc;
 }
@@ -435,6 +436,29 @@ static int fill_desc(const simmd_params* p, const double* D, RepDesc& d)
     d.c4f = (float)d.c4;
     d.zetaf = (float)d.zeta;
     d.seed = p->seed;
+    // floor(rnew/L) of the wrap (src/MD.jl:520) without a divide: RN(x/L) >= 1
+    // exactly when x >= wrap_hi (found with IEEE host division)
+    double wx = L;
+    for (int k = 0; k < 64; k++) {
+        double q = std::nextafter(wx, 0.0);
+        if (q / L >= 1.0) wx = q;
+        else break;
+    }
+    d.wrap_hi = wx;
+    int ex = 0;
+    double mant = std::frexp(d.two_m, &ex);
+    d.two_m_pow2 = (mant == 0.5) ? 1 : 0;
+    d.inv_two_m = 1.0 / d.two_m;
+    // split-precision offset grid: the smallest power of two >= max(1/2, L/1022)
+    double hg = 0.5;
+    while (L / hg > 1022.0) hg *= 2.0;
+    d.h = hg;
+    d.inv_h = 1.0 / hg;
+    double Lhi = std::floor(L / hg) * hg;
+    d.hf = (float)hg;
+    d.Lhi_f = (float)Lhi;
+    d.Llo_f = (float)(L - Lhi);
+    d.rv2f = (float)d.rv2;
     return SIMMD_OK;
 }
 
@@ -573,6 +597,7 @@ static int remove_replica(simmd_ctx* c, int rid)
 // ---------------------------------------------------------------------------
 struct Mix {
     bool nl = false, br = false, rescale = false, noise = false;
+    int prec_mask = 0;  // bit 0: FP64 replicas, bit 1: split precision
 };
 
 static Mix batch_mix(simmd_ctx* c)
@@ -584,6 +609,7 @@ static Mix batch_mix(simmd_ctx* c)
         else m.nl = true;
         if (h.d.rescale) m.rescale = true;
         if (h.p.dynamics != SIMMD_NEWTONIAN) m.noise = true;
+        m.prec_mask |= (h.d.prec == PREC_FP64) ? 1 : 2;
     }
     return m;
 }
@@ -605,7 +631,7 @@ static void enqueue_step(simmd_ctx* c, const Batch& b, const LaunchCfg& lc, cons
         if (prof) cudaEventRecord(c->pev[2], c->stream);
     }
     if (prof) cudaEventRecord(c->pev[3], c->stream);
-    launch_force_impl(b, lc, fmode, lc.grid_force, nullptr);
+    launch_force_impl(b, lc, fmode, m.prec_mask, nullptr);
     if (prof) cudaEventRecord(c->pev[4], c->stream);
     if (m.rescale) launch_rescale_impl(b, lc);
     if (m.br) {
@@ -676,7 +702,10 @@ static int read_states(simmd_ctx* c)
     return st;
 }
 
-static int graph_key(const Mix& m, int fmode) { return (m.nl ? 1 : 0) | (m.br ? 2 : 0) | (m.rescale ? 4 : 0) | (fmode << 3); }
+static int graph_key(const Mix& m, int fmode)
+{
+    return (m.nl ? 1 : 0) | (m.br ? 2 : 0) | (m.rescale ? 4 : 0) | (m.prec_mask << 3) | (fmode << 5);
+}
 
 static int run_steps(simmd_ctx* c, long long nsteps, const double* noise)
 {
@@ -823,7 +852,7 @@ static void destroy_ctx(simmd_ctx* c)
     cudaStreamSynchronize(c->stream);
     invalidate_graph(c);
     Slots& s = c->s;
-    void* ptrs[] = {s.posD, s.vx, s.vy, s.vz, s.fx, s.fy, s.fz, s.ux, s.uy, s.uz, s.off, s.cellc, s.orig, s.nbr,
+    void* ptrs[] = {s.posD, s.vx, s.vy, s.vz, s.fx, s.fy, s.fz, s.ux, s.uy, s.uz, s.rec, s.cellc, s.orig, s.nbr,
                     s.ncnt, s.bin_cell, s.bin_rank, s.src, s.t_posD, s.t_vx, s.t_vy, s.t_vz, s.t_fx, s.t_fy,
                     s.t_fz, s.t_orig, s.cell_count, s.cell_start, c->nbr_full, c->ncnt_full, c->epp, c->d_desc,
                     c->d_state, c->d_tile_rep, c->d_tile_part, c->d_queue, c->d_stage, c->d_noise};
@@ -1027,12 +1056,12 @@ int simmd_forces(simmd_ctx* c, const double* noise, double* F_out)
         h.d.noise_step0 = c->h_state[single].step;
         h.d.noise_nsteps = 1;
         TRY(push_desc(c, single));
-        launch_force_impl(b, lc, FMODE_FORCES, lc.grid_force, nullptr);
+        launch_force_impl(b, lc, FMODE_FORCES, m.prec_mask, nullptr);
         h.d.noise_mode = NOISE_PHILOX;
         h.d.host_noise = nullptr;
         TRY(push_desc(c, single));
     } else {
-        launch_force_impl(b, lc, FMODE_FORCES, lc.grid_force, nullptr);
+        launch_force_impl(b, lc, FMODE_FORCES, m.prec_mask, nullptr);
     }
     CK(cudaGetLastError());
     TRY(read_states(c));
@@ -1054,7 +1083,7 @@ int simmd_energy_all(simmd_ctx* c)
     TRY(pending_rebuilds(c));
     Batch b = make_batch(c);
     LaunchCfg lc = make_lc(c, FMODE_ENERGY);
-    launch_force_impl(b, lc, FMODE_ENERGY, lc.grid_force, c->epp);
+    launch_force_impl(b, lc, FMODE_ENERGY, batch_mix(c).prec_mask, c->epp);
     launch_kinetic_impl(b, lc);
     CK(cudaGetLastError());
     return read_states(c);
@@ -1252,7 +1281,8 @@ int simmd_time_force(simmd_ctx* c, int32_t nrep, float* ms_per_launch)
     Batch b = make_batch(c);
     LaunchCfg lc = make_lc(c, FMODE_ENERGY);
     CK(cudaEventRecord(c->ev0, c->stream));
-    for (int k = 0; k < nrep; k++) launch_force_impl(b, lc, FMODE_ENERGY, lc.grid_force, nullptr);
+    const int pm = batch_mix(c).prec_mask;
+    for (int k = 0; k < nrep; k++) launch_force_impl(b, lc, FMODE_ENERGY, pm, nullptr);
     CK(cudaEventRecord(c->ev1, c->stream));
     CK(cudaEventSynchronize(c->ev1));
     float ms = 0;
@@ -1261,9 +1291,9 @@ int simmd_time_force(simmd_ctx* c, int32_t nrep, float* ms_per_launch)
     return SIMMD_OK;
 }
 
-int simmd_relax(simmd_ctx* c, int64_t nsteps, double max_disp)
+int simmd_relax(simmd_ctx* c, int64_t nsteps, double step_size, double max_disp)
 {
-    if (!c || nsteps < 0 || !(max_disp > 0)) return set_err(SIMMD_ERR_BAD_ARG, "bad argument");
+    if (!c || nsteps < 0 || !(max_disp > 0) || !(step_size > 0)) return set_err(SIMMD_ERR_BAD_ARG, "bad argument");
     CK(cudaSetDevice(c->device));
     TRY(pending_rebuilds(c));
     std::vector<RepDesc> saved;
@@ -1272,7 +1302,7 @@ int simmd_relax(simmd_ctx* c, int64_t nsteps, double max_disp)
         if (!c->reps[r].active) continue;
         RepDesc& d = c->reps[r].d;
         d.dyn = DYN_BROWNIAN;
-        d.dt_over_gamma = 1.0;
+        d.dt_over_gamma = step_size;
         d.relax_cap = max_disp;
         d.prec = PREC_FP64;
         TRY(push_desc(c, r));
@@ -1281,6 +1311,7 @@ int simmd_relax(simmd_ctx* c, int64_t nsteps, double max_disp)
     LaunchCfg lc = make_lc(c, FMODE_STEP);
     Mix m;
     m.br = true;
+    m.prec_mask = 1;  // the relaxation runs every replica in FP64
     for (long long s = 0; s < nsteps; s++) enqueue_step(c, b, lc, m, FMODE_STEP);
     CK(cudaGetLastError());
     for (int r = 0; r < c->R_cap; r++) {

@@ -11,149 +11,202 @@
 //   kick2 + centre-of-mass removal     src/MD.jl:528-542
 //   find_energy inner loops            src/AuxiliaryFunctions.jl:381-444, 477-507, 571-581
 //
-// One persistent kernel per launch: blocks pull 128-slot tiles from an atomic
-// work queue; a tile belongs to one replica, so (precision, dims, potential,
-// dynamics) are uniform per block.  T threads per particle split the
-// particle's list (interleaved ELL) and combine with __shfl_xor.  Every pair
-// is visited from both sides (no atomics, deterministic sums).
+// One persistent kernel per launch and precision: blocks pull 128-slot tiles
+// from an atomic work queue; a tile belongs to one replica, so (dims,
+// potential, dynamics) are uniform per block.  T threads per particle
+// (compile-time) split the particle's list (interleaved ELL) and combine
+// with __shfl_xor; the pair loop is unrolled by two so two gathers are in
+// flight per thread.  Every pair is visited from both sides (no atomics,
+// deterministic sums).
 //
 // FP64 path: the reference's per-pair operation order with explicit
 // round-to-nearest intrinsics, so each pair force is bit-identical to the
 // reference expression; only the order of the per-particle sum differs.
-// FP32 split path: pair arithmetic in FP32 on cell-relative FP32 offsets plus
-// an exact integer cell shift carried in the list entry; per-particle sums in
-// FP32, converted to FP64 for integration.
+// FP32 split path: pair arithmetic in FP32 on FP32 offsets of the FP64
+// positions from a power-of-two grid, with the grid shift and the box's
+// grid-multiple part applied exactly (split_dx); IEEE reciprocals; one
+// 32-byte record per neighbour gather; per-particle sums, random force and
+// the mean-force partial sums in FP32, integration in FP64.
 #include "simmd_internal.cuh"
 #include "simmd_reduce.cuh"
 
 namespace simmd {
 
+// ---------------------------------------------------------------------------
+// FP64 pair (reference arithmetic)
+// ---------------------------------------------------------------------------
 template <int DIM, int POT, bool EN>
-__device__ __forceinline__ void pairs_f64(const Batch& b, const RepDesc& d, long long i, int sub, int T,
+__device__ __forceinline__ void pair_f64(const RepDesc& d, long long halfLb, const double4_32a& pi,
+                                         const double4_32a& pj, double& fx, double& fy, double& fz, double& e,
+                                         double& w)
+{
+    const double L = d.L, rc2 = d.rc2;
+    const double dx = min_image_f64(dsub(pi.x, pj.x), halfLb, L);
+    const double dy = min_image_f64(dsub(pi.y, pj.y), halfLb, L);
+    double dz = 0.0, r2;
+    if (DIM == 3) {
+        dz = min_image_f64(dsub(pi.z, pj.z), halfLb, L);
+        r2 = dadd(dadd(dmul(dx, dx), dmul(dy, dy)), dmul(dz, dz));
+    } else {
+        r2 = dadd(dmul(dx, dx), dmul(dy, dy));
+    }
+    double Fr = 0.0, V = 0.0;
+    if (POT == POT_BERTHIER) {
+        const double md = dmul(dmul(dadd(pi.w, pj.w), 0.5), dsub(1.0, dmul(d.zeta, fabs(dsub(pi.w, pj.w)))));
+        const double mds = dmul(md, md);
+        const bool out = dmul(rc2, mds) < r2;
+        const double inv = drcp(mds);
+        const double ix2 = dmul(r2, inv);
+        const double ix4 = dmul(ix2, ix2);
+        const double xi14 = drcp(dmul(dmul(dmul(ix4, ix4), ix4), ix2));
+        Fr = out ? 0.0 : dmul(dmul(-2.0, inv), dsub(dadd(d.c2, dmul(dmul(2.0, d.c4), ix2)), dmul(6.0, xi14)));
+        if (EN && !out) {  // berthier_inner_loop3/2: invxi2 = rij2 / mean_d2
+            const double jx2 = ddiv(r2, mds);
+            const double jx4 = dmul(jx2, jx2);
+            const double xi12 = drcp(dmul(dmul(jx4, jx4), jx4));
+            V = dadd(dadd(dadd(xi12, dmul(d.c4, jx4)), dmul(d.c2, jx2)), d.c0);
+        }
+    } else if (DIM == 3) {  // compute_forces_lj_3d / LJ_inner_loop
+        const double xi2 = ddiv(d.sigma2, r2);
+        const double xi6 = dmul(dmul(xi2, xi2), xi2);
+        const double xi12 = dmul(xi6, xi6);
+        Fr = (rc2 < r2) ? 0.0 : ddiv(dmul(d.eps, dsub(dmul(48.0, xi12), dmul(24.0, xi6))), r2);
+        if (EN && !(d.lj_cut2 < r2)) V = dsub(dmul(dmul(4.0, d.eps), dsub(xi12, xi6)), d.Uc);
+    } else {  // generic path: mean_d = find_mean_D = sigma^2, squared; strict '>'
+        const double mds = d.sigma4;
+        if (d.lj_cut2 > r2) {
+            const double inv = drcp(r2);
+            const double xi2 = dmul(mds, inv);
+            const double xi6 = dmul(dmul(xi2, xi2), xi2);
+            const double xi12 = dmul(xi6, xi6);
+            Fr = dmul(dmul(d.eps, dsub(dmul(48.0, xi12), dmul(24.0, xi6))), inv);
+            if (EN) {
+                const double y2 = ddiv(mds, r2);
+                const double y4 = dmul(y2, y2);
+                const double y6 = dmul(y2, y4);
+                const double y12 = dmul(y6, y6);
+                V = dsub(dmul(dmul(4.0, d.eps), dsub(y12, y6)), d.Uc);
+            }
+        }
+    }
+    fx = dadd(fx, dmul(Fr, dx));
+    fy = dadd(fy, dmul(Fr, dy));
+    if (DIM == 3) fz = dadd(fz, dmul(Fr, dz));
+    if (EN) {
+        e = dadd(e, V);
+        w = dadd(w, dmul(Fr, r2));
+    }
+}
+
+template <int DIM, int POT, bool EN, int T>
+__device__ __forceinline__ void pairs_f64(const Batch& b, const RepDesc& d, long long i, int sub,
                                           const double4_32a pi, int cnt, double& fx, double& fy, double& fz,
                                           double& e, double& w)
 {
     const long long halfLb = __double_as_longlong(d.halfL);
-    const double L = d.L, rc2 = d.rc2;
     const unsigned* __restrict__ nbr = b.s.nbr;
     const double4_32a* __restrict__ posD = b.s.posD;
-    for (int n = sub; n < cnt; n += T) {
-        const unsigned ent = __ldg(nbr + nbr_addr(n, i, T, b.S));
-        const double4_32a pj = posD[ent & IDX_MASK];
-        const double dx = min_image_f64(dsub(pi.x, pj.x), halfLb, L);
-        const double dy = min_image_f64(dsub(pi.y, pj.y), halfLb, L);
-        double dz = 0.0, r2;
-        if (DIM == 3) {
-            dz = min_image_f64(dsub(pi.z, pj.z), halfLb, L);
-            r2 = dadd(dadd(dmul(dx, dx), dmul(dy, dy)), dmul(dz, dz));
-        } else {
-            r2 = dadd(dmul(dx, dx), dmul(dy, dy));
-        }
-        double Fr = 0.0, V = 0.0;
-        if (POT == POT_BERTHIER) {
-            const double md = dmul(dmul(dadd(pi.w, pj.w), 0.5), dsub(1.0, dmul(d.zeta, fabs(dsub(pi.w, pj.w)))));
-            const double mds = dmul(md, md);
-            const bool out = dmul(rc2, mds) < r2;
-            const double inv = drcp(mds);
-            const double ix2 = dmul(r2, inv);
-            const double ix4 = dmul(ix2, ix2);
-            const double xi14 = drcp(dmul(dmul(dmul(ix4, ix4), ix4), ix2));
-            Fr = out ? 0.0 : dmul(dmul(-2.0, inv), dsub(dadd(d.c2, dmul(dmul(2.0, d.c4), ix2)), dmul(6.0, xi14)));
-            if (EN && !out) {  // berthier_inner_loop3/2: invxi2 = rij2 / mean_d2
-                const double jx2 = ddiv(r2, mds);
-                const double jx4 = dmul(jx2, jx2);
-                const double xi12 = drcp(dmul(dmul(jx4, jx4), jx4));
-                V = dadd(dadd(dadd(xi12, dmul(d.c4, jx4)), dmul(d.c2, jx2)), d.c0);
-            }
-        } else if (DIM == 3) {  // compute_forces_lj_3d / LJ_inner_loop
-            const double xi2 = ddiv(d.sigma2, r2);
-            const double xi6 = dmul(dmul(xi2, xi2), xi2);
-            const double xi12 = dmul(xi6, xi6);
-            Fr = (rc2 < r2) ? 0.0 : ddiv(dmul(d.eps, dsub(dmul(48.0, xi12), dmul(24.0, xi6))), r2);
-            if (EN && !(d.lj_cut2 < r2)) V = dsub(dmul(dmul(4.0, d.eps), dsub(xi12, xi6)), d.Uc);
-        } else {  // generic path: mean_d = find_mean_D = sigma^2, squared; strict '>'
-            const double mds = d.sigma4;
-            if (d.lj_cut2 > r2) {
-                const double inv = drcp(r2);
-                const double xi2 = dmul(mds, inv);
-                const double xi6 = dmul(dmul(xi2, xi2), xi2);
-                const double xi12 = dmul(xi6, xi6);
-                Fr = dmul(dmul(d.eps, dsub(dmul(48.0, xi12), dmul(24.0, xi6))), inv);
-                if (EN) {
-                    const double y2 = ddiv(mds, r2);
-                    const double y4 = dmul(y2, y2);
-                    const double y6 = dmul(y2, y4);
-                    const double y12 = dmul(y6, y6);
-                    V = dsub(dmul(dmul(4.0, d.eps), dsub(y12, y6)), d.Uc);
-                }
-            }
-        }
-        fx = dadd(fx, dmul(Fr, dx));
-        fy = dadd(fy, dmul(Fr, dy));
-        if (DIM == 3) fz = dadd(fz, dmul(Fr, dz));
-        if (EN) {
-            e = dadd(e, V);
-            w = dadd(w, dmul(Fr, r2));
-        }
+    int n = sub;
+    for (; n + T < cnt; n += 2 * T) {
+        const unsigned j0 = __ldg(nbr + nbr_addr(n, i, T, b.S)) & IDX_MASK;
+        const unsigned j1 = __ldg(nbr + nbr_addr(n + T, i, T, b.S)) & IDX_MASK;
+        const double4_32a p0 = posD[j0];
+        const double4_32a p1 = posD[j1];
+        pair_f64<DIM, POT, EN>(d, halfLb, pi, p0, fx, fy, fz, e, w);
+        pair_f64<DIM, POT, EN>(d, halfLb, pi, p1, fx, fy, fz, e, w);
+    }
+    if (n < cnt) {
+        const unsigned j0 = __ldg(nbr + nbr_addr(n, i, T, b.S)) & IDX_MASK;
+        pair_f64<DIM, POT, EN>(d, halfLb, pi, posD[j0], fx, fy, fz, e, w);
     }
 }
 
+// ---------------------------------------------------------------------------
+// FP32 split-precision pair
+// ---------------------------------------------------------------------------
 template <int DIM, int POT, bool EN>
-__device__ __forceinline__ void pairs_f32(const Batch& b, const RepDesc& d, long long i, int sub, int T,
-                                          const float4 oi, int cnt, float& fx, float& fy, float& fz,
+__device__ __forceinline__ void pair_f32(const RepDesc& d, const float4& oi, int mix, int miy, int miz,
+                                         const float4& oj, int gj, float& fx, float& fy, float& fz, float& e,
+                                         float& w)
+{
+    const float dx = split_dx(oi.x, oj.x, mix, grid_axis(gj, 0), d);
+    const float dy = split_dx(oi.y, oj.y, miy, grid_axis(gj, 1), d);
+    float dz = 0.0f, r2;
+    if (DIM == 3) {
+        dz = split_dx(oi.z, oj.z, miz, grid_axis(gj, 2), d);
+        r2 = dx * dx + dy * dy + dz * dz;
+    } else {
+        r2 = dx * dx + dy * dy;
+    }
+    float Fr = 0.0f, V = 0.0f;
+    if (POT == POT_BERTHIER) {
+        const float md = (oi.w + oj.w) * 0.5f * (1.0f - d.zetaf * fabsf(oi.w - oj.w));
+        const float mds = md * md;
+        const float inv = __frcp_rn(mds);
+        const float ix2 = r2 * inv;
+        const float ix4 = ix2 * ix2;
+        const float xi14 = __frcp_rn(ix4 * ix4 * ix4 * ix2);
+        const bool in = r2 <= d.rc2f * mds;
+        Fr = in ? -2.0f * inv * (d.c2f + 2.0f * d.c4f * ix2 - 6.0f * xi14) : 0.0f;
+        if (EN && in) V = xi14 * ix2 + d.c4f * ix4 + d.c2f * ix2 + d.c0f;
+    } else {
+        const float inv = __frcp_rn(r2);
+        const float xi2 = (DIM == 3 ? d.sigma2f : d.sigma4f) * inv;
+        const float xi6 = xi2 * xi2 * xi2;
+        const float xi12 = xi6 * xi6;
+        const bool in = (DIM == 3) ? (r2 <= d.cut2f) : (r2 < d.cut2f);
+        Fr = in ? d.epsf * (48.0f * xi12 - 24.0f * xi6) * inv : 0.0f;
+        if (EN && in) V = 4.0f * d.epsf * (xi12 - xi6) - d.Ucf;
+    }
+    fx += Fr * dx;
+    fy += Fr * dy;
+    if (DIM == 3) fz += Fr * dz;
+    if (EN) {
+        e += V;
+        w += Fr * r2;
+    }
+}
+
+template <int DIM, int POT, bool EN, int T>
+__device__ __forceinline__ void pairs_f32(const Batch& b, const RepDesc& d, long long i, int sub,
+                                          const float4 oi, int gi, int cnt, float& fx, float& fy, float& fz,
                                           float& e, float& w)
 {
-    const float csf = d.csf, Lf = d.Lf, hL = d.halfLf;
     const unsigned* __restrict__ nbr = b.s.nbr;
-    const float4* __restrict__ off = b.s.off;
-    for (int n = sub; n < cnt; n += T) {
-        const unsigned ent = __ldg(nbr + nbr_addr(n, i, T, b.S));
-        const float4 oj = __ldg(off + (ent & IDX_MASK));
-        const unsigned code = ent >> IDX_BITS;
-        const float dx = min_image_f32(oi.x - oj.x + (float)((int)(code & 3u) - 1) * csf, hL, Lf);
-        const float dy = min_image_f32(oi.y - oj.y + (float)((int)((code >> 2) & 3u) - 1) * csf, hL, Lf);
-        float dz = 0.0f, r2;
-        if (DIM == 3) {
-            dz = min_image_f32(oi.z - oj.z + (float)((int)((code >> 4) & 3u) - 1) * csf, hL, Lf);
-            r2 = dx * dx + dy * dy + dz * dz;
-        } else {
-            r2 = dx * dx + dy * dy;
-        }
-        float Fr = 0.0f, V = 0.0f;
-        if (POT == POT_BERTHIER) {
-            const float md = (oi.w + oj.w) * 0.5f * (1.0f - d.zetaf * fabsf(oi.w - oj.w));
-            const float mds = md * md;
-            const float inv = __fdividef(1.0f, mds);
-            const float ix2 = r2 * inv;
-            const float ix4 = ix2 * ix2;
-            const float xi12 = __fdividef(1.0f, ix4 * ix4 * ix4);
-            const float xi14 = xi12 * __fdividef(1.0f, ix2);
-            const bool in = r2 <= d.rc2f * mds;
-            Fr = in ? -2.0f * inv * (d.c2f + 2.0f * d.c4f * ix2 - 6.0f * xi14) : 0.0f;
-            if (EN && in) V = xi12 + d.c4f * ix4 + d.c2f * ix2 + d.c0f;
-        } else {
-            const float inv = __fdividef(1.0f, r2);
-            const float xi2 = (DIM == 3 ? d.sigma2f : d.sigma4f) * inv;
-            const float xi6 = xi2 * xi2 * xi2;
-            const float xi12 = xi6 * xi6;
-            const bool in = (DIM == 3) ? (r2 <= d.cut2f) : (r2 < d.cut2f);
-            Fr = in ? d.epsf * (48.0f * xi12 - 24.0f * xi6) * inv : 0.0f;
-            if (EN && in) V = 4.0f * d.epsf * (xi12 - xi6) - d.Ucf;
-        }
-        fx += Fr * dx;
-        fy += Fr * dy;
-        if (DIM == 3) fz += Fr * dz;
-        if (EN) {
-            e += V;
-            w += Fr * r2;
-        }
+    const SplitRec* __restrict__ rec = b.s.rec;
+    const int mix = grid_axis(gi, 0), miy = grid_axis(gi, 1), miz = grid_axis(gi, 2);
+    int n = sub;
+    for (; n + T < cnt; n += 2 * T) {
+        const unsigned j0 = __ldg(nbr + nbr_addr(n, i, T, b.S)) & IDX_MASK;
+        const unsigned j1 = __ldg(nbr + nbr_addr(n + T, i, T, b.S)) & IDX_MASK;
+        const float4 o0 = __ldg(&rec[j0].o);
+        const int g0 = __ldg(&rec[j0].g);
+        const float4 o1 = __ldg(&rec[j1].o);
+        const int g1 = __ldg(&rec[j1].g);
+        pair_f32<DIM, POT, EN>(d, oi, mix, miy, miz, o0, g0, fx, fy, fz, e, w);
+        pair_f32<DIM, POT, EN>(d, oi, mix, miy, miz, o1, g1, fx, fy, fz, e, w);
+    }
+    if (n < cnt) {
+        const unsigned j0 = __ldg(nbr + nbr_addr(n, i, T, b.S)) & IDX_MASK;
+        pair_f32<DIM, POT, EN>(d, oi, mix, miy, miz, __ldg(&rec[j0].o), __ldg(&rec[j0].g), fx, fy, fz, e, w);
     }
 }
 
-__device__ __forceinline__ void particle_noise(const RepDesc& d, RepState& st, int oid, double xi[3])
+// v + dt*F/(2m); the divide is an exact scaling when 2m is a power of two
+__device__ __forceinline__ double kick(double v, double F, const RepDesc& d)
+{
+    const double t = dmul(d.dt, F);
+    return dadd(v, d.two_m_pow2 ? dmul(t, d.inv_two_m) : ddiv(t, d.two_m));
+}
+
+// N(0,1) deviates of this particle for the current noise step: the host
+// array (parity runs) or the Philox stream keyed by (seed, step, id, pair)
+template <int PREC>
+__device__ __forceinline__ void particle_noise(const RepDesc& d, RepState& st, int oid, double& x0, double& x1,
+                                               double& x2)
 {
     const long long step = st.step;
-    xi[0] = xi[1] = xi[2] = 0.0;
+    x0 = x1 = x2 = 0.0;
     if (d.noise_mode == NOISE_HOST) {
         long long k = step - d.noise_step0;
         if (k < 0 || k >= d.noise_nsteps) {
@@ -161,60 +214,57 @@ __device__ __forceinline__ void particle_noise(const RepDesc& d, RepState& st, i
             return;
         }
         const double* q = d.host_noise + (k * d.n + oid) * d.dims;
-        for (int c = 0; c < d.dims; c++) xi[c] = q[c];
-    } else if (d.prec == PREC_FP64) {
+        x0 = q[0];
+        x1 = q[1];
+        if (d.dims == 3) x2 = q[2];
+    } else if (PREC == PREC_FP64) {
         double z1;
-        normal_pair_f64(d.seed, step, oid, 0, xi[0], xi[1]);
-        if (d.dims == 3) normal_pair_f64(d.seed, step, oid, 1, xi[2], z1);
+        normal_pair_f64(d.seed, step, oid, 0, x0, x1);
+        if (d.dims == 3) normal_pair_f64(d.seed, step, oid, 1, x2, z1);
     } else {
         float a, c, z1;
         normal_pair_f32(d.seed, step, oid, 0, a, c);
-        xi[0] = a;
-        xi[1] = c;
+        x0 = a;
+        x1 = c;
         if (d.dims == 3) {
             normal_pair_f32(d.seed, step, oid, 1, a, z1);
-            xi[2] = a;
+            x2 = a;
         }
     }
 }
 
-template <bool EN>
-__device__ __forceinline__ void particle_pairs(const Batch& b, const RepDesc& d, long long i, int sub, int T,
-                                               double& fx, double& fy, double& fz, double& e, double& w)
+template <int DIM, bool EN, int PREC, int T>
+__device__ __forceinline__ void particle_pairs(const Batch& b, const RepDesc& d, long long i, int sub, double& fx,
+                                               double& fy, double& fz, double& e, double& w)
 {
     const int cnt = b.s.ncnt[i];
-    if (d.prec == PREC_FP64) {
+    if (PREC == PREC_FP64) {
         const double4_32a pi = b.s.posD[i];
-        if (d.dims == 3) {
-            if (d.pot == POT_BERTHIER) pairs_f64<3, POT_BERTHIER, EN>(b, d, i, sub, T, pi, cnt, fx, fy, fz, e, w);
-            else pairs_f64<3, POT_LJ, EN>(b, d, i, sub, T, pi, cnt, fx, fy, fz, e, w);
-        } else {
-            if (d.pot == POT_BERTHIER) pairs_f64<2, POT_BERTHIER, EN>(b, d, i, sub, T, pi, cnt, fx, fy, fz, e, w);
-            else pairs_f64<2, POT_LJ, EN>(b, d, i, sub, T, pi, cnt, fx, fy, fz, e, w);
-        }
+        if (d.pot == POT_BERTHIER) pairs_f64<DIM, POT_BERTHIER, EN, T>(b, d, i, sub, pi, cnt, fx, fy, fz, e, w);
+        else pairs_f64<DIM, POT_LJ, EN, T>(b, d, i, sub, pi, cnt, fx, fy, fz, e, w);
     } else {
-        const float4 oi = b.s.off[i];
+        const float4 oi = b.s.rec[i].o;
+        const int gi = b.s.rec[i].g;
         float gx = 0.f, gy = 0.f, gz = 0.f, ge = 0.f, gw = 0.f;
-        if (d.dims == 3) {
-            if (d.pot == POT_BERTHIER) pairs_f32<3, POT_BERTHIER, EN>(b, d, i, sub, T, oi, cnt, gx, gy, gz, ge, gw);
-            else pairs_f32<3, POT_LJ, EN>(b, d, i, sub, T, oi, cnt, gx, gy, gz, ge, gw);
-        } else {
-            if (d.pot == POT_BERTHIER) pairs_f32<2, POT_BERTHIER, EN>(b, d, i, sub, T, oi, cnt, gx, gy, gz, ge, gw);
-            else pairs_f32<2, POT_LJ, EN>(b, d, i, sub, T, oi, cnt, gx, gy, gz, ge, gw);
-        }
-        fx = gx; fy = gy; fz = gz; e = ge; w = gw;
+        if (d.pot == POT_BERTHIER) pairs_f32<DIM, POT_BERTHIER, EN, T>(b, d, i, sub, oi, gi, cnt, gx, gy, gz, ge, gw);
+        else pairs_f32<DIM, POT_LJ, EN, T>(b, d, i, sub, oi, gi, cnt, gx, gy, gz, ge, gw);
+        fx = gx;
+        fy = gy;
+        fz = gz;
+        e = ge;
+        w = gw;
     }
 }
 
-template <int MODE>
-__global__ void __launch_bounds__(512) k_force(Batch b, double* epp)
+template <int MODE, int PREC, int T>
+__global__ void __launch_bounds__(TILE * T, (PREC == PREC_FP32 ? 8 : 4) / T) k_force(Batch b, double* epp)
 {
     constexpr bool EN = (MODE == FMODE_ENERGY || MODE == FMODE_STEP_ENERGY);
     constexpr bool STEP = (MODE == FMODE_STEP || MODE == FMODE_STEP_ENERGY);
+    constexpr int NV = EN ? 5 : 3;
     __shared__ int s_tile;
     __shared__ int s_flag;
-    __shared__ double s_part[32 * 5];
-    const int T = b.tpp;
+    __shared__ double s_part[32 * NV];
     const int tid = threadIdx.x;
     const int p = tid / T, sub = tid - p * T;
     for (;;) {
@@ -226,49 +276,82 @@ __global__ void __launch_bounds__(512) k_force(Batch b, double* epp)
         const int r = b.tile_rep[t];
         if (r < 0) continue;
         const RepDesc& d = b.desc[r];
+        if (d.prec != PREC) continue;  // the other precision's launch handles this tile
         RepState& st = b.state[r];
         const long long i = (long long)t * TILE + p;
         const bool real = i < d.slot0 + d.n;
         double fx = 0.0, fy = 0.0, fz = 0.0, e = 0.0, w = 0.0;
-        if (real) particle_pairs<EN>(b, d, i, sub, T, fx, fy, fz, e, w);
-        for (int o = T >> 1; o > 0; o >>= 1) {
-            fx += __shfl_xor_sync(0xffffffffu, fx, o);
-            fy += __shfl_xor_sync(0xffffffffu, fy, o);
-            fz += __shfl_xor_sync(0xffffffffu, fz, o);
-            if (EN) {
-                e += __shfl_xor_sync(0xffffffffu, e, o);
-                w += __shfl_xor_sync(0xffffffffu, w, o);
+        if (real) {
+            if (d.dims == 3) particle_pairs<3, EN, PREC, T>(b, d, i, sub, fx, fy, fz, e, w);
+            else particle_pairs<2, EN, PREC, T>(b, d, i, sub, fx, fy, fz, e, w);
+        }
+        if (T > 1) {
+            if (PREC == PREC_FP32) {  // combine the T lanes in FP32
+                float gx = (float)fx, gy = (float)fy, gz = (float)fz, ge = (float)e, gw = (float)w;
+                for (int o = T >> 1; o > 0; o >>= 1) {
+                    gx += __shfl_xor_sync(0xffffffffu, gx, o);
+                    gy += __shfl_xor_sync(0xffffffffu, gy, o);
+                    gz += __shfl_xor_sync(0xffffffffu, gz, o);
+                    if (EN) {
+                        ge += __shfl_xor_sync(0xffffffffu, ge, o);
+                        gw += __shfl_xor_sync(0xffffffffu, gw, o);
+                    }
+                }
+                fx = gx; fy = gy; fz = gz; e = ge; w = gw;
+            } else {
+                for (int o = T >> 1; o > 0; o >>= 1) {
+                    fx += __shfl_xor_sync(0xffffffffu, fx, o);
+                    fy += __shfl_xor_sync(0xffffffffu, fy, o);
+                    fz += __shfl_xor_sync(0xffffffffu, fz, o);
+                    if (EN) {
+                        e += __shfl_xor_sync(0xffffffffu, e, o);
+                        w += __shfl_xor_sync(0xffffffffu, w, o);
+                    }
+                }
             }
         }
-        double pv[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+        double pv[NV];
+#pragma unroll
+        for (int k = 0; k < NV; k++) pv[k] = 0.0;
         const bool noise = d.dyn != DYN_NEWTONIAN && MODE != FMODE_ENERGY && d.relax_cap == 0.0;
+        const bool nl = d.dyn != DYN_BROWNIAN;
         if (sub == 0 && real) {
             if (EN) {
-                pv[3] = e;
-                pv[4] = w;
+                pv[NV - 2] = e;
+                pv[NV - 1] = w;
                 if (epp) epp[i] = e / 2.0;
             }
             if (MODE != FMODE_ENERGY) {
-                double Fx = fx, Fy = fy, Fz = fz;
                 double vx = 0.0, vy = 0.0, vz = 0.0;
-                const bool nl = d.dyn != DYN_BROWNIAN;
                 if (nl) {
                     vx = b.s.vx[i];
                     vy = b.s.vy[i];
                     if (d.dims == 3) vz = b.s.vz[i];
                 }
+                double Fx = fx, Fy = fy, Fz = fz;
                 if (noise) {
-                    double xi[3];
-                    particle_noise(d, st, b.s.orig[i], xi);
-                    if (d.dyn == DYN_LANGEVIN) {
+                    double x0, x1, x2;
+                    particle_noise<PREC>(d, st, b.s.orig[i], x0, x1, x2);
+                    if (PREC == PREC_FP32) {  // random force in FP32, as the pair force
+                        const float nf = (float)d.noise_factor;
+                        float gx = (float)fx + nf * (float)x0, gy = (float)fy + nf * (float)x1,
+                              gz = (float)fz + nf * (float)x2;
+                        if (d.dyn == DYN_LANGEVIN) {
+                            const float mg = -(float)d.gamma;
+                            gx += mg * (float)vx;
+                            gy += mg * (float)vy;
+                            gz += mg * (float)vz;
+                        }
+                        Fx = gx; Fy = gy; Fz = gz;
+                    } else if (d.dyn == DYN_LANGEVIN) {
                         const double mg = -d.gamma;
-                        Fx = dadd(Fx, dadd(dmul(mg, vx), dmul(d.noise_factor, xi[0])));
-                        Fy = dadd(Fy, dadd(dmul(mg, vy), dmul(d.noise_factor, xi[1])));
-                        if (d.dims == 3) Fz = dadd(Fz, dadd(dmul(mg, vz), dmul(d.noise_factor, xi[2])));
+                        Fx = dadd(Fx, dadd(dmul(mg, vx), dmul(d.noise_factor, x0)));
+                        Fy = dadd(Fy, dadd(dmul(mg, vy), dmul(d.noise_factor, x1)));
+                        if (d.dims == 3) Fz = dadd(Fz, dadd(dmul(mg, vz), dmul(d.noise_factor, x2)));
                     } else {
-                        Fx = dadd(Fx, dmul(d.noise_factor, xi[0]));
-                        Fy = dadd(Fy, dmul(d.noise_factor, xi[1]));
-                        if (d.dims == 3) Fz = dadd(Fz, dmul(d.noise_factor, xi[2]));
+                        Fx = dadd(Fx, dmul(d.noise_factor, x0));
+                        Fy = dadd(Fy, dmul(d.noise_factor, x1));
+                        if (d.dims == 3) Fz = dadd(Fz, dmul(d.noise_factor, x2));
                     }
                 }
                 b.s.fx[i] = Fx;
@@ -276,12 +359,12 @@ __global__ void __launch_bounds__(512) k_force(Batch b, double* epp)
                 if (d.dims == 3) b.s.fz[i] = Fz;
                 if (STEP) {
                     if (nl) {  // kick2 (src/MD.jl:529-531)
-                        vx = dadd(vx, ddiv(dmul(d.dt, Fx), d.two_m));
-                        vy = dadd(vy, ddiv(dmul(d.dt, Fy), d.two_m));
+                        vx = kick(vx, Fx, d);
+                        vy = kick(vy, Fy, d);
                         b.s.vx[i] = vx;
                         b.s.vy[i] = vy;
                         if (d.dims == 3) {
-                            vz = dadd(vz, ddiv(dmul(d.dt, Fz), d.two_m));
+                            vz = kick(vz, Fz, d);
                             b.s.vz[i] = vz;
                         }
                         pv[0] = vx; pv[1] = vy; pv[2] = vz;
@@ -291,8 +374,31 @@ __global__ void __launch_bounds__(512) k_force(Batch b, double* epp)
                 }
             }
         }
-        double out[5];
-        if (tile_reduce<5>(b, t, d, st, pv, out, s_part, &s_flag) && tid == 0) {
+        double out[NV];
+        bool last;
+        if (PREC == PREC_FP32 && STEP && !EN) {
+            // split precision: the Brownian mean-force partial sums per warp in
+            // FP32 (the forces carry FP32-level accuracy); velocity sums (FP64
+            // state) per warp in FP64; per-tile and per-replica sums in FP64
+            if (nl) {
+                warp_sum<NV>(pv);
+            } else {
+                float s0 = (float)pv[0], s1 = (float)pv[1], s2 = (float)pv[2];
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) {
+                    s0 += __shfl_xor_sync(0xffffffffu, s0, o);
+                    s1 += __shfl_xor_sync(0xffffffffu, s1, o);
+                    s2 += __shfl_xor_sync(0xffffffffu, s2, o);
+                }
+                pv[0] = s0;
+                pv[1] = s1;
+                pv[2] = s2;
+            }
+            last = tile_reduce<NV, true>(b, t, d, st, pv, out, s_part, &s_flag);
+        } else {
+            last = tile_reduce<NV>(b, t, d, st, pv, out, s_part, &s_flag);
+        }
+        if (last && tid == 0) {
             const double nd = (double)d.n;
             if (STEP) {
                 if (d.dyn == DYN_BROWNIAN) {
@@ -306,8 +412,8 @@ __global__ void __launch_bounds__(512) k_force(Batch b, double* epp)
                 }
             }
             if (EN) {
-                st.epot = out[3] / 2.0;
-                st.virial = out[4] / 2.0;
+                st.epot = out[NV - 2] / 2.0;
+                st.virial = out[NV - 1] / 2.0;
             }
             if (noise) st.step += 1;
         }
@@ -321,29 +427,51 @@ __global__ void __launch_bounds__(512) k_force(Batch b, double* epp)
     }
 }
 
-int force_blocks_per_sm(int T, int mode)
+// ---------------------------------------------------------------------------
+// host side: occupancy and launch, one instantiation per (mode, precision, T)
+// ---------------------------------------------------------------------------
+template <int MODE, int PREC>
+static void* kernel_ptr(int T)
+{
+    switch (T) {
+        case 2: return (void*)k_force<MODE, PREC, 2>;
+        case 4: return (void*)k_force<MODE, PREC, 4>;
+        default: return (void*)k_force<MODE, PREC, 1>;
+    }
+}
+
+template <int PREC>
+static void* kernel_for(int mode, int T)
+{
+    switch (mode) {
+        case FMODE_STEP: return kernel_ptr<FMODE_STEP, PREC>(T);
+        case FMODE_FORCES: return kernel_ptr<FMODE_FORCES, PREC>(T);
+        case FMODE_ENERGY: return kernel_ptr<FMODE_ENERGY, PREC>(T);
+        default: return kernel_ptr<FMODE_STEP_ENERGY, PREC>(T);
+    }
+}
+
+int force_blocks_per_sm(int T, int mode, int prec)
 {
     int nb = 0;
-    const int threads = TILE * T;
-    switch (mode) {
-        case FMODE_STEP: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_force<FMODE_STEP>, threads, 0); break;
-        case FMODE_FORCES: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_force<FMODE_FORCES>, threads, 0); break;
-        case FMODE_ENERGY: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_force<FMODE_ENERGY>, threads, 0); break;
-        default: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_force<FMODE_STEP_ENERGY>, threads, 0); break;
-    }
+    void* k = prec == PREC_FP64 ? kernel_for<PREC_FP64>(mode, T) : kernel_for<PREC_FP32>(mode, T);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k, TILE * T, 0);
     return nb > 0 ? nb : 1;
 }
 
-void launch_force_impl(const Batch& b, const LaunchCfg& lc, int mode, int grid, double* epp)
+// one launch per precision present in the batch (prec_mask bit 0: FP64, bit 1: FP32 split)
+void launch_force_impl(const Batch& b, const LaunchCfg& lc, int mode, int prec_mask, double* epp)
 {
-    const int threads = TILE * b.tpp;
-    switch (mode) {
-        case FMODE_STEP: k_force<FMODE_STEP><<<grid, threads, 0, lc.stream>>>(b, epp); break;
-        case FMODE_FORCES: k_force<FMODE_FORCES><<<grid, threads, 0, lc.stream>>>(b, epp); break;
-        case FMODE_ENERGY: k_force<FMODE_ENERGY><<<grid, threads, 0, lc.stream>>>(b, epp); break;
-        default: k_force<FMODE_STEP_ENERGY><<<grid, threads, 0, lc.stream>>>(b, epp); break;
+    for (int prec = 0; prec < 2; prec++) {
+        if (!(prec_mask & (1 << prec))) continue;
+        void* k = prec == PREC_FP64 ? kernel_for<PREC_FP64>(mode, b.tpp) : kernel_for<PREC_FP32>(mode, b.tpp);
+        Batch bb = b;
+        double* ep = epp;
+        void* args[] = {(void*)&bb, (void*)&ep};
+        cudaLaunchKernel(k, dim3(prec == PREC_FP64 ? lc.grid_force64 : lc.grid_force32), dim3(TILE * b.tpp), args,
+                         0, lc.stream);
+        if (lc.launches) *lc.launches += 1;
     }
-    if (lc.launches) *lc.launches += 1;
 }
 
 }  // namespace simmd

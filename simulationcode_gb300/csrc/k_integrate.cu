@@ -17,13 +17,21 @@
 
 namespace simmd {
 
-__device__ __forceinline__ float cell_offset_dyn(double x, int c, const RepDesc& d)
+// rnew - floor(rnew/L)*L (src/MD.jl:520) with floor(RN(rnew/L)) decided by
+// comparisons against 0 and wrap_hi = min{x : RN(x/L) >= 1}: bit-identical to
+// the divide for |dr| < L, no FP64 divide on the path
+__device__ __forceinline__ double wrap_coord(double x, const RepDesc& d)
 {
-    if (d.nc == 1) return (float)x;
-    double o = x - (double)c * d.cs;
-    o = (o > d.halfL) ? o - d.L : o;
-    o = (o < -d.halfL) ? o + d.L : o;
-    return (float)o;
+    if (x >= 0.0 && x < d.wrap_hi) return x;
+    if (x < 0.0 && x >= -d.L) return dsub(x, -d.L);
+    if (x >= d.wrap_hi && x < 2.0 * d.wrap_hi) return dsub(x, d.L);  // RN(x/L) in [1, 2)
+    return dsub(x, dmul(floor(ddiv(x, d.L)), d.L));
+}
+
+__device__ __forceinline__ double half_kick(double v, double F, const RepDesc& d)
+{
+    const double t = dmul(d.dt, F);
+    return dadd(v, d.two_m_pow2 ? dmul(t, d.inv_two_m) : ddiv(t, d.two_m));
 }
 
 // r += dr with the reference wrap rnew - floor(rnew/L)*L, displacement update,
@@ -42,25 +50,21 @@ __device__ __forceinline__ double drift_slot(const Batch& b, const RepDesc& d, l
         S.uz[i] = uz;
     }
     double4_32a p = S.posD[i];
-    double x = dadd(p.x, drx);
-    x = dsub(x, dmul(floor(ddiv(x, d.L)), d.L));
-    double y = dadd(p.y, dry);
-    y = dsub(y, dmul(floor(ddiv(y, d.L)), d.L));
-    double z = p.z;
-    if (d.dims == 3) {
-        z = dadd(p.z, drz);
-        z = dsub(z, dmul(floor(ddiv(z, d.L)), d.L));
-    }
+    const double x = wrap_coord(dadd(p.x, drx), d);
+    const double y = wrap_coord(dadd(p.y, dry), d);
+    const double z = (d.dims == 3) ? wrap_coord(dadd(p.z, drz), d) : p.z;
     S.posD[i] = make_double4_32a(x, y, z, p.w);
     if (d.prec == PREC_FP32) {
-        int c = S.cellc[i];
-        S.off[i] = make_float4(cell_offset_dyn(x, c & 1023, d), cell_offset_dyn(y, (c >> 10) & 1023, d),
-                               d.dims == 3 ? cell_offset_dyn(z, (c >> 20) & 1023, d) : 0.0f, (float)p.w);
+        const int g = S.rec[i].g;
+        S.rec[i].o = make_float4(grid_offset(x, grid_axis(g, 0), d), grid_offset(y, grid_axis(g, 1), d),
+                                 d.dims == 3 ? grid_offset(z, grid_axis(g, 2), d) : 0.0f, (float)p.w);
     }
     return u2;
 }
 
-__device__ __forceinline__ void warp_max_to_state(double u2, RepState& st)
+// block-level max of |disp|^2 (bit pattern; non-negative doubles order as
+// integers), one atomic per tile and only when it raises the replica's max
+__device__ __forceinline__ void block_max_to_state(double u2, RepState& st, unsigned long long* s_max)
 {
     unsigned long long bits = (unsigned long long)__double_as_longlong(u2);
     if (!(u2 == u2) || isinf(u2)) {
@@ -72,12 +76,21 @@ __device__ __forceinline__ void warp_max_to_state(double u2, RepState& st)
         unsigned long long y = __shfl_xor_sync(0xffffffffu, bits, o);
         bits = y > bits ? y : bits;
     }
-    if ((threadIdx.x & 31) == 0) atomicMax(&st.maxdisp2, bits);
+    const int w = threadIdx.x >> 5;
+    if ((threadIdx.x & 31) == 0) s_max[w] = bits;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned long long m = s_max[0];
+        for (int k = 1; k < (int)(blockDim.x >> 5); k++) m = s_max[k] > m ? s_max[k] : m;
+        if (m > *(volatile unsigned long long*)&st.maxdisp2) atomicMax(&st.maxdisp2, m);
+    }
+    __syncthreads();
 }
 
 // kick1 + drift for Newtonian / Langevin replicas (src/MD.jl:510-522)
 __global__ void k_kick_drift(Batch b)
 {
+    __shared__ unsigned long long s_max[TILE / 32];
     for (int t = blockIdx.x; t < b.ntiles; t += gridDim.x) {
         int r = b.tile_rep[t];
         if (r < 0) continue;
@@ -91,19 +104,19 @@ __global__ void k_kick_drift(Batch b)
             const double vs = st.vscale;
             double vx = dmul(dsub(S.vx[i], st.vmean[0]), vs);
             double vy = dmul(dsub(S.vy[i], st.vmean[1]), vs);
-            vx = dadd(vx, ddiv(dmul(d.dt, S.fx[i]), d.two_m));
-            vy = dadd(vy, ddiv(dmul(d.dt, S.fy[i]), d.two_m));
+            vx = half_kick(vx, S.fx[i], d);
+            vy = half_kick(vy, S.fy[i], d);
             S.vx[i] = vx;
             S.vy[i] = vy;
             double vz = 0.0;
             if (d.dims == 3) {
                 vz = dmul(dsub(S.vz[i], st.vmean[2]), vs);
-                vz = dadd(vz, ddiv(dmul(d.dt, S.fz[i]), d.two_m));
+                vz = half_kick(vz, S.fz[i], d);
                 S.vz[i] = vz;
             }
             u2 = drift_slot(b, d, i, dmul(d.dt, vx), dmul(d.dt, vy), dmul(d.dt, vz));
         }
-        warp_max_to_state(u2, st);
+        block_max_to_state(u2, st, s_max);
     }
 }
 
@@ -111,6 +124,7 @@ __global__ void k_kick_drift(Batch b)
 // dr = (dt/gamma) F, displacement, wrap
 __global__ void k_brownian_update(Batch b)
 {
+    __shared__ unsigned long long s_max[TILE / 32];
     for (int t = blockIdx.x; t < b.ntiles; t += gridDim.x) {
         int r = b.tile_rep[t];
         if (r < 0) continue;
@@ -152,7 +166,7 @@ __global__ void k_brownian_update(Batch b)
             }
             u2 = drift_slot(b, d, i, drx, dry, drz);
         }
-        warp_max_to_state(u2, st);
+        block_max_to_state(u2, st, s_max);
     }
 }
 
@@ -282,7 +296,7 @@ __global__ void k_load_aos(Batch b, int rep, const double* r, const double* v, c
     }
     S.ncnt[s] = 0;
     S.cellc[s] = 0;
-    S.off[s] = make_float4(0.f, 0.f, 0.f, 0.f);
+    rec_put(&S.rec[s], make_float4(0.f, 0.f, 0.f, 0.f), 0);
 }
 
 __global__ void k_store_aos(Batch b, int rep, double* r, double* v, double* F, double* disp,
@@ -337,9 +351,9 @@ __global__ void k_set_state(Batch b, int rep, const double* r, const double* v, 
         if (dm == 3) p.z = r[o * dm + 2];
         S.posD[s] = p;
         if (d.prec == PREC_FP32) {
-            int c = S.cellc[s];
-            S.off[s] = make_float4(cell_offset_dyn(p.x, c & 1023, d), cell_offset_dyn(p.y, (c >> 10) & 1023, d),
-                                   dm == 3 ? cell_offset_dyn(p.z, (c >> 20) & 1023, d) : 0.0f, (float)p.w);
+            const int g = S.rec[s].g;
+            S.rec[s].o = make_float4(grid_offset(p.x, grid_axis(g, 0), d), grid_offset(p.y, grid_axis(g, 1), d),
+                                   dm == 3 ? grid_offset(p.z, grid_axis(g, 2), d) : 0.0f, (float)p.w);
         }
     }
     if (v) {

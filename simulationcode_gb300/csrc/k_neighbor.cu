@@ -155,18 +155,7 @@ __global__ void k_rb_cellsort(Batch b)
     }
 }
 
-// FP32 cell-relative offset of coordinate x in cell c (nc >= 3), continuous
-// across the periodic wrap; for a single-cell axis the wrapped x itself
-__device__ __forceinline__ float cell_offset(double x, int c, const RepDesc& d)
-{
-    if (d.nc == 1) return (float)x;
-    double o = x - (double)c * d.cs;
-    o = (o > d.halfL) ? o - d.L : o;
-    o = (o < -d.halfL) ? o + d.L : o;
-    return (float)o;
-}
-
-__global__ void k_rb_gather(Batch b)
+__global__ void k_rb_gather(Batch b, int* ncnt_full)
 {
     for (int t = blockIdx.x; t < b.ntiles; t += gridDim.x) {
         int r = b.tile_rep[t];
@@ -178,6 +167,8 @@ __global__ void k_rb_gather(Batch b)
         S.ux[nw] = 0.0;
         S.uy[nw] = 0.0;
         S.uz[nw] = 0.0;
+        S.ncnt[nw] = 0;
+        if (ncnt_full) ncnt_full[nw] = 0;
         if (nw < d.slot0 + d.n) {
             int s = S.src[nw];
             double4_32a p = S.posD[s];
@@ -193,15 +184,18 @@ __global__ void k_rb_gather(Batch b)
             int nc = d.nc;
             int cx = lin % nc, cy = (lin / nc) % nc, cz = lin / (nc * nc);
             S.cellc[nw] = pack_cell(cx, cy, cz);
-            S.off[nw] = make_float4(cell_offset(p.x, cx, d), cell_offset(p.y, cy, d),
-                                    d.dims == 3 ? cell_offset(p.z, cz, d) : 0.0f, (float)p.w);
+            const int mx = grid_index(p.x, d), my = grid_index(p.y, d), mz = d.dims == 3 ? grid_index(p.z, d) : 0;
+            rec_put(&S.rec[nw],
+                    make_float4(grid_offset(p.x, mx, d), grid_offset(p.y, my, d),
+                                d.dims == 3 ? grid_offset(p.z, mz, d) : 0.0f, (float)p.w),
+                    mx | (my << 10) | (mz << 20));
         } else {
             S.t_posD[nw] = make_double4_32a(0.0, 0.0, 0.0, 0.0);
             S.t_vx[nw] = S.t_vy[nw] = S.t_vz[nw] = 0.0;
             S.t_fx[nw] = S.t_fy[nw] = S.t_fz[nw] = 0.0;
             S.t_orig[nw] = -1;
             S.cellc[nw] = 0;
-            S.off[nw] = make_float4(0.f, 0.f, 0.f, 0.f);
+            rec_put(&S.rec[nw], make_float4(0.f, 0.f, 0.f, 0.f), 0);
         }
     }
 }
@@ -213,112 +207,211 @@ __device__ __forceinline__ double mean_d_f64(const RepDesc& d, double Di, double
     return dmul(dmul(dadd(Di, Dj), 0.5), dsub(1.0, dmul(d.zeta, fabs(dsub(Di, Dj)))));
 }
 
+// ---------------------------------------------------------------------------
+// Verlet build, one home cell at a time: the block stages the candidates of
+// the home cell's stencil (27 cells in 3D, 9 in 2D; one cell along an axis
+// with fewer than three cells) in shared memory, then Tb lanes per home
+// particle test them in candidate order.  A lane's candidate passes an FP32
+// prefilter on the split-precision offsets, then the exact FP64 test of the
+// reference: d2 <= verlet^2 (the pair enumeration radius) and
+// d2 < (sqrt(rc2)*mean_d + skin)^2 (add_pair!, src/NeighborLists.jl:82-104).
+// Accepted entries are appended in candidate order (warp ballot + popc), so
+// the list order is a pure function of the replica's own state.
+// ---------------------------------------------------------------------------
+constexpr int BLD_THREADS = 128;
+constexpr int BLD_CHUNK = 512;
+
+struct BuildSmem {
+    float4 o[BLD_CHUNK];
+    int g[BLD_CHUNK];
+    int slot[BLD_CHUNK];
+    int ca[27];
+    int cn[27];
+    int pre[28];
+    int nst;
+    unsigned long long entries;
+    int maxcnt;
+};
+
 template <int DIM, bool FULL>
-__device__ void build_particle(const Batch& b, const RepDesc& d, RepState& st, long long i,
-                               unsigned* nbr_full, int* ncnt_full, int Kfull)
+__device__ void build_cell(const Batch& b, const RepDesc& d, RepState& st, int c, BuildSmem& sm,
+                           unsigned* nbr_full, int* ncnt_full, int Kfull)
 {
     const Slots& S = b.s;
-    const double4_32a pi = S.t_posD[i];
-    const float4 oi = S.off[i];
-    const int ci = S.cellc[i];
-    const int cx = ci & 1023, cy = (ci >> 10) & 1023, cz = (ci >> 20) & 1023;
+    const int tid = threadIdx.x;
     const int nc = d.nc;
+    const int cx = c % nc, cy = (c / nc) % nc, cz = c / (nc * nc);
+    const int ha = S.cell_start[d.cell0 + c], he = S.cell_start[d.cell0 + c + 1];
+    const int P = he - ha;
+    if (P == 0) return;  // uniform across the block
     const int rng = (nc >= 3) ? 1 : 0;
-    const long long halfLb = __double_as_longlong(d.halfL);
-    const float csf = d.csf;
-    const float pre_r = (d.pot == POT_LJ) ? d.rcutf * d.sigma2f + d.skinf
-                                          : d.rcutf * 1.0f + d.skinf;  // scaled by mean_d below
-    const float rvf = (float)sqrt(d.rv2) + 1e-3f;
-    int cnt = 0, cntf = 0;
+    const int w = 2 * rng + 1;
+    const int nst = (DIM == 3) ? w * w * w : w * w;
+    if (tid < nst) {
+        int ox = tid % w - rng, oy = (tid / w) % w - rng, oz = (DIM == 3) ? tid / (w * w) - rng : 0;
+        int x = (cx + ox + nc) % nc, y = (cy + oy + nc) % nc, z = (DIM == 3) ? (cz + oz + nc) % nc : 0;
+        int lin = x + nc * (y + nc * z);
+        int a = S.cell_start[d.cell0 + lin];
+        sm.ca[tid] = a;
+        sm.cn[tid] = S.cell_start[d.cell0 + lin + 1] - a;
+    }
+    __syncthreads();
+    if (tid == 0) {
+        int acc = 0;
+        for (int k = 0; k < nst; k++) {
+            sm.pre[k] = acc;
+            acc += sm.cn[k];
+        }
+        sm.pre[nst] = acc;
+    }
+    __syncthreads();
+    const int M = sm.pre[nst];
+    const int Tb = P <= 16 ? 8 : (P <= 32 ? 4 : (P <= 64 ? 2 : 1));
+    const int sub = tid % Tb;
+    const int lane = tid & 31;
+    const int gbase = (lane / Tb) * Tb;
+    const unsigned gmask = (Tb == 32) ? 0xffffffffu : ((1u << Tb) - 1u);
     const int K = b.K, T = b.tpp;
     const long long SS = b.S;
-    const int zr = (DIM == 3) ? rng : 0;
-    for (int oz = -zr; oz <= zr; oz++) {
-        int z = (DIM == 3) ? (cz + oz + nc) % nc : 0;
-        for (int oy = -rng; oy <= rng; oy++) {
-            int y = (cy + oy + nc) % nc;
-            for (int ox = -rng; ox <= rng; ox++) {
-                int x = (cx + ox + nc) % nc;
-                int lin = x + nc * (y + nc * z);
-                int a = S.cell_start[d.cell0 + lin], e = S.cell_start[d.cell0 + lin + 1];
-                unsigned code = (unsigned)(1 - ox) | ((unsigned)(1 - oy) << 2) |
-                                ((unsigned)(DIM == 3 ? 1 - oz : 1) << 4);
-                float shx = (float)(-ox) * csf, shy = (float)(-oy) * csf, shz = (float)(-oz) * csf;
-                for (int j = a; j < e; j++) {
-                    if (j == i) continue;
-                    float4 oj = S.off[j];
-                    float dxf = min_image_f32(oi.x - oj.x + shx, d.halfLf, d.Lf);
-                    float dyf = min_image_f32(oi.y - oj.y + shy, d.halfLf, d.Lf);
-                    float d2f = dxf * dxf + dyf * dyf;
-                    if (DIM == 3) {
-                        float dzf = min_image_f32(oi.z - oj.z + shz, d.halfLf, d.Lf);
-                        d2f += dzf * dzf;
+    const long long halfLb = __double_as_longlong(d.halfL);
+    for (int base = 0; base < P; base += BLD_THREADS / Tb) {
+        const int p = base + tid / Tb;
+        const bool active = p < P;
+        const long long i = ha + (active ? p : 0);
+        float4 oi = make_float4(0.f, 0.f, 0.f, 0.f);
+        int gi = 0;
+        double4_32a pi = make_double4_32a(0.0, 0.0, 0.0, 0.0);
+        if (active) {
+            oi = S.rec[i].o;
+            gi = S.rec[i].g;
+            pi = S.t_posD[i];
+        }
+        int cnt = 0, cntf = 0;
+        for (int c0 = 0; c0 < M; c0 += BLD_CHUNK) {
+            const int len = min(BLD_CHUNK, M - c0);
+            __syncthreads();
+            for (int q = tid; q < len; q += BLD_THREADS) {
+                const int idx = c0 + q;
+                int k = 0;
+                while (k + 1 < nst && sm.pre[k + 1] <= idx) k++;
+                const int j = sm.ca[k] + (idx - sm.pre[k]);
+                sm.o[q] = S.rec[j].o;
+                sm.g[q] = S.rec[j].g;
+                sm.slot[q] = j;
+            }
+            __syncthreads();
+            for (int q0 = 0; q0 < len; q0 += Tb) {
+                const int q = q0 + sub;
+                bool pred = false, predf = false;
+                if (active && q < len) {
+                    const int j = sm.slot[q];
+                    if (j != (int)i) {
+                        const float4 oj = sm.o[q];
+                        const int gj = sm.g[q];
+                        const float dxf = split_dx(oi.x, oj.x, grid_axis(gi, 0), grid_axis(gj, 0), d);
+                        const float dyf = split_dx(oi.y, oj.y, grid_axis(gi, 1), grid_axis(gj, 1), d);
+                        float d2f = dxf * dxf + dyf * dyf;
+                        if (DIM == 3) {
+                            const float dzf = split_dx(oi.z, oj.z, grid_axis(gi, 2), grid_axis(gj, 2), d);
+                            d2f += dzf * dzf;
+                        }
+                        // FP32 classification against the reference thresholds with a
+                        // relative margin (1e-5) far above the FP32 error of d2 and of
+                        // the thresholds (~1e-6): clear accepts and rejects are the
+                        // reference's decisions; the exact FP64 test runs only in the
+                        // narrow band around a threshold, so the pair set stays
+                        // bit-identical while the FP64 pipe stays idle
+                        float tf = (d.pot == POT_LJ) ? d.rcutf * d.sigma2f
+                                                     : d.rcutf * ((oi.w + oj.w) * 0.5f *
+                                                                  (1.0f - d.zetaf * fabsf(oi.w - oj.w)));
+                        tf += d.skinf;
+                        const float thr = fminf(tf * tf, d.rv2f);
+                        const float lo = thr * (1.0f - 1e-5f), hi = thr * (1.0f + 1e-5f);
+                        const float flo = d.rv2f * (1.0f - 1e-5f), fhi = d.rv2f * (1.0f + 1e-5f);
+                        const bool band = (d2f >= lo && d2f <= hi) || (FULL && d2f >= flo && d2f <= fhi);
+                        if (!band) {
+                            pred = d2f < lo;
+                            predf = d2f < flo;
+                        } else {
+                            // exact FP64 test in the reference's operation order
+                            const double4_32a pj = S.t_posD[j];
+                            const double ddx = min_image_f64(dsub(pi.x, pj.x), halfLb, d.L);
+                            const double ddy = min_image_f64(dsub(pi.y, pj.y), halfLb, d.L);
+                            double d2 = dadd(dmul(ddx, ddx), dmul(ddy, ddy));
+                            if (DIM == 3) {
+                                const double ddz = min_image_f64(dsub(pi.z, pj.z), halfLb, d.L);
+                                d2 = dadd(d2, dmul(ddz, ddz));
+                            }
+                            if (d2 <= d.rv2) {
+                                predf = true;
+                                const double tt = dadd(dmul(d.rcut, mean_d_f64(d, pi.w, pj.w)), d.skin);
+                                pred = d2 < dmul(tt, tt);
+                            }
+                        }
                     }
-                    float lim;
-                    if (FULL) {
-                        lim = rvf;
-                    } else if (d.pot == POT_LJ) {
-                        lim = pre_r + 1e-3f;
-                    } else {
-                        float mdf = (oi.w + oj.w) * 0.5f * (1.0f - d.zetaf * fabsf(oi.w - oj.w));
-                        lim = d.rcutf * mdf + d.skinf + 1e-3f;
+                }
+                const unsigned bal = __ballot_sync(0xffffffffu, pred);
+                const unsigned gb = (bal >> gbase) & gmask;
+                if (pred) {
+                    const int pos = cnt + __popc(gb & ((1u << sub) - 1u));
+                    if (pos < K) S.nbr[nbr_addr(pos, i, T, SS)] = (unsigned)sm.slot[q];
+                }
+                cnt += __popc(gb);
+                if (FULL) {
+                    const unsigned balf = __ballot_sync(0xffffffffu, predf);
+                    const unsigned gf = (balf >> gbase) & gmask;
+                    if (predf) {
+                        const int pos = cntf + __popc(gf & ((1u << sub) - 1u));
+                        if (pos < Kfull) nbr_full[(size_t)pos * SS + i] = (unsigned)sm.slot[q];
                     }
-                    if (d2f > lim * lim) continue;
-                    // exact FP64 test in the reference's operation order
-                    double4_32a pj = S.t_posD[j];
-                    double ddx = min_image_f64(dsub(pi.x, pj.x), halfLb, d.L);
-                    double ddy = min_image_f64(dsub(pi.y, pj.y), halfLb, d.L);
-                    double d2 = dadd(dmul(ddx, ddx), dmul(ddy, ddy));
-                    if (DIM == 3) {
-                        double ddz = min_image_f64(dsub(pi.z, pj.z), halfLb, d.L);
-                        d2 = dadd(d2, dmul(ddz, ddz));
-                    }
-                    if (!(d2 <= d.rv2)) continue;
-                    if (FULL) {
-                        if (cntf < Kfull) nbr_full[(size_t)cntf * SS + i] = (unsigned)j;
-                        cntf++;
-                    }
-                    double tt = dadd(dmul(d.rcut, mean_d_f64(d, pi.w, pj.w)), d.skin);
-                    if (d2 < dmul(tt, tt)) {
-                        if (cnt < K) S.nbr[nbr_addr(cnt, i, T, SS)] = (unsigned)j | (code << IDX_BITS);
-                        cnt++;
-                    }
+                    cntf += __popc(gf);
                 }
             }
         }
+        if (active && sub == 0) {
+            if (cnt > K) st.overflow = 1;
+            S.ncnt[i] = min(cnt, K);
+            if (FULL) {
+                if (cntf > Kfull) st.overflow = 1;
+                ncnt_full[i] = min(cntf, Kfull);
+            }
+            atomicMax(&sm.maxcnt, cnt);
+            atomicAdd(&sm.entries, (unsigned long long)min(cnt, K));
+        }
     }
-    if (cnt > K) st.overflow = 1;
-    S.ncnt[i] = min(cnt, K);
-    if (FULL) {
-        if (cntf > Kfull) st.overflow = 1;
-        ncnt_full[i] = min(cntf, Kfull);
-    }
-    atomicMax(&st.maxcount, cnt);
-    atomicAdd((unsigned long long*)&st.list_entries, (unsigned long long)min(cnt, K));
+    __syncthreads();
 }
 
-__global__ void k_rb_build(Batch b, unsigned* nbr_full, int* ncnt_full, int Kfull)
+__global__ void __launch_bounds__(BLD_THREADS) k_rb_build(Batch b, unsigned* nbr_full, int* ncnt_full, int Kfull)
 {
+    __shared__ BuildSmem sm;
     for (int t = blockIdx.x; t < b.ntiles; t += gridDim.x) {
         int r = b.tile_rep[t];
         if (r < 0) continue;
         const RepDesc& d = b.desc[r];
         RepState& st = b.state[r];
         if (!need_rebuild(st, d)) continue;
-        long long i = (long long)t * TILE + threadIdx.x;
-        Slots& S = b.s;
-        if (i < d.slot0 + d.n) {
-            if (d.dims == 3) {
-                if (nbr_full) build_particle<3, true>(b, d, st, i, nbr_full, ncnt_full, Kfull);
-                else build_particle<3, false>(b, d, st, i, nbr_full, ncnt_full, Kfull);
-            } else {
-                if (nbr_full) build_particle<2, true>(b, d, st, i, nbr_full, ncnt_full, Kfull);
-                else build_particle<2, false>(b, d, st, i, nbr_full, ncnt_full, Kfull);
-            }
-        } else {
-            S.ncnt[i] = 0;
-            if (nbr_full) ncnt_full[i] = 0;
+        if (threadIdx.x == 0) {
+            sm.entries = 0ull;
+            sm.maxcnt = 0;
         }
+        __syncthreads();
+        const int tl = t - d.tile0;
+        for (int c = tl; c < d.ncell; c += d.ntiles) {
+            if (d.dims == 3) {
+                if (nbr_full) build_cell<3, true>(b, d, st, c, sm, nbr_full, ncnt_full, Kfull);
+                else build_cell<3, false>(b, d, st, c, sm, nbr_full, ncnt_full, Kfull);
+            } else {
+                if (nbr_full) build_cell<2, true>(b, d, st, c, sm, nbr_full, ncnt_full, Kfull);
+                else build_cell<2, false>(b, d, st, c, sm, nbr_full, ncnt_full, Kfull);
+            }
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            atomicMax(&st.maxcount, sm.maxcnt);
+            if (sm.entries) atomicAdd((unsigned long long*)&st.list_entries, sm.entries);
+        }
+        __syncthreads();
     }
 }
 
@@ -364,8 +457,8 @@ void launch_rebuild_impl(const Batch& b, const LaunchCfg& lc, unsigned* nbr_full
     k_rb_scan<<<b.nreps, 1024, 0, lc.stream>>>(b);
     k_rb_scatter<<<g, TILE, 0, lc.stream>>>(b);
     k_rb_cellsort<<<g, TILE, 0, lc.stream>>>(b);
-    k_rb_gather<<<g, TILE, 0, lc.stream>>>(b);
-    k_rb_build<<<g, TILE, 0, lc.stream>>>(b, nbr_full, ncnt_full, Kfull);
+    k_rb_gather<<<g, TILE, 0, lc.stream>>>(b, ncnt_full);
+    k_rb_build<<<g, BLD_THREADS, 0, lc.stream>>>(b, nbr_full, ncnt_full, Kfull);
     k_rb_copyback<<<g, TILE, 0, lc.stream>>>(b);
     k_rb_done<<<(b.nreps + 127) / 128, 128, 0, lc.stream>>>(b);
     if (lc.launches) *lc.launches += 9;

@@ -45,6 +45,13 @@ struct RepDesc {
     double sigma2, sigma4, lj_cut2, eps, Uc, c0, c2, c4, zeta;
     double kBT, gamma, dt, m, noise_factor, dt_over_gamma, two_m, m_half;
     double relax_cap;          // > 0: capped steepest descent (set-up relaxation), no noise
+    double wrap_hi;            // smallest x with RN(x/L) >= 1: floor(x/L) without a divide
+    double inv_two_m;          // 1/(2m), used when 2m is a power of two (exact)
+    int two_m_pow2;
+    int pad2_;
+    // split precision: FP32 offsets from a power-of-two grid h (exact integer shifts)
+    double h, inv_h;
+    float hf, Lhi_f, Llo_f, rv2f;
     float Lf, halfLf, csf, rc2f, rcutf, skinf, sigma2f, sigma4f, cut2f, epsf, Ucf, c0f, c2f, c4f, zetaf;
     unsigned long long seed;
     const double* host_noise;  // [noise_nsteps][n][dims], original order
@@ -71,12 +78,20 @@ struct RepState {
     double fmax;
 };
 
+// split-precision gather record (one 32-byte sector): FP32 offsets of the
+// FP64 position from its grid point, FP32 diameter, packed grid index
+struct __align__(32) SplitRec {
+    float4 o;   // x, y, z offsets, D
+    int g;      // grid index, 10 bits per axis
+    int pad[3];
+};
+
 struct Slots {
     double4_32a* posD;                // x, y, z, D
     double *vx, *vy, *vz;
     double *fx, *fy, *fz;
     double *ux, *uy, *uz;         // displacement since the last rebuild
-    float4* off;                  // split precision: cell-relative offsets, D
+    SplitRec* rec;                // split precision: offsets + D + grid index
     int* cellc;                   // packed rebuild-time cell coords (10 bits each)
     int* orig;                    // original id, -1 for padding
     unsigned* nbr;                // ELL neighbour list
@@ -131,6 +146,45 @@ __device__ __forceinline__ float min_image_f32(float dx, float halfL, float L)
     dx = (dx > halfL) ? dx - L : dx;
     dx = (dx < -halfL) ? dx + L : dx;
     return dx;
+}
+
+// split precision: grid index of the FP32 offset origin (power-of-two grid h)
+__device__ __forceinline__ int grid_index(double x, const RepDesc& d)
+{
+    const double q = floor(x * d.inv_h + 0.5);
+    int m = (q == q) ? (int)fmax(fmin(q, 1023.0), 0.0) : 0;
+    return m;
+}
+
+// FP32 offset of coordinate x from its grid point m*h (m*h exact), continuous
+// across the periodic wrap
+__device__ __forceinline__ float grid_offset(double x, int m, const RepDesc& d)
+{
+    double o = x - (double)m * d.h;
+    o = (o > d.halfL) ? o - d.L : o;
+    o = (o < -d.halfL) ? o + d.L : o;
+    return (float)o;
+}
+
+__device__ __forceinline__ int grid_axis(int g, int axis) { return (g >> (10 * axis)) & 1023; }
+
+// minimum-image difference x_i - x_j of two split-precision coordinates:
+// ((o_i - o_j) - s*L_lo) + ((m_i - m_j)*h - s*L_hi) with the integer grid
+// shift and L_hi = floor(L/h)*h exact in FP32, so only the small offset
+// terms and the final sum round
+__device__ __forceinline__ float split_dx(float oi, float oj, int mi, int mj, const RepDesc& d)
+{
+    const float a = oi - oj;
+    const float G0 = (float)(mi - mj) * d.hf;
+    const float dx0 = a + G0;
+    const float s = (dx0 > d.halfLf) ? 1.0f : ((dx0 < -d.halfLf) ? -1.0f : 0.0f);
+    return (a - s * d.Llo_f) + (G0 - s * d.Lhi_f);
+}
+
+__device__ __forceinline__ void rec_put(SplitRec* r, float4 o, int g)
+{
+    r->o = o;
+    r->g = g;
 }
 
 __device__ __forceinline__ bool need_rebuild(const RepState& st, const RepDesc& d)
@@ -200,7 +254,8 @@ __device__ __forceinline__ void normal_pair_f32(unsigned long long seed, long lo
 struct LaunchCfg {
     cudaStream_t stream;
     int grid_stream;      // blocks for streaming kernels
-    int grid_force;       // blocks for the persistent force kernel
+    int grid_force64;     // blocks for the persistent force kernel, FP64 replicas
+    int grid_force32;     // ... split-precision replicas
     long long* launches;  // launch counter
 };
 

@@ -21,15 +21,16 @@ __device__ __forceinline__ void warp_sum(double (&v)[NV])
 }
 
 // Returns true in the threads of the block that must finalise replica r; in
-// that case out[] (valid in thread 0) holds the replica totals.
+// that case out[] (valid in thread 0) holds the replica totals.  WARP_DONE:
+// the caller has already reduced each warp (lane 0's v[] is used).
 // s_part must hold 32*NV doubles; s_flag one int.  Must be called by every
 // thread of the block (contains __syncthreads).
-template <int NV>
+template <int NV, bool WARP_DONE = false>
 __device__ bool tile_reduce(const Batch& b, int t, const RepDesc& d, RepState& st, double (&v)[NV],
                             double (&out)[NV], double* s_part, int* s_flag)
 {
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5, nw = blockDim.x >> 5;
-    warp_sum<NV>(v);
+    if (!WARP_DONE) warp_sum<NV>(v);  // else lane 0 already holds the warp's sums
     if (lane == 0)
 #pragma unroll
         for (int k = 0; k < NV; k++) s_part[wid * NV + k] = v[k];
