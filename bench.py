@@ -351,6 +351,13 @@ def run_gpu(args, dist):
             s.r = r
     batch, ids = build_batch(specs, device, args.tpp)
     batch.rebuild()
+    tune = None
+    if args.autotune:
+        from simulationcode_gb300.autotune import autotune
+        skins = [float(x) for x in args.tune_skins.split(",")] if args.tune_skins else None
+        tune = autotune(batch, tpps=(1, 2, 4), skins=skins,
+                        log=lambda m: print(m, file=sys.stderr, flush=True))
+        args.tpp = tune.tpp
     batch.step(args.warmup)
     st_before = [batch.stats(i) for i in ids]
     # kernel launches of this process before the timed region (for ncu -s)
@@ -448,7 +455,11 @@ def run_gpu(args, dist):
                        "l2": ("state larger than L2 (%.0f MB streamed per step)" % (step_bytes / 1e6))
                              if step_bytes > 129e6 else "state fits in L2 (%.0f MB; no flush)" % (step_bytes / 1e6),
                        "parallelism": "replicas only" if dist.ws > 1 else "single GPU",
-                       "rebuilds_in_timed_region": rebuilds},
+                       "rebuilds_in_timed_region": rebuilds,
+                       "skin": specs[0].skin,
+                       "autotune": None if tune is None else {"tpp": tune.tpp, "skin": tune.skin,
+                                                              "graph_steps": tune.graph_steps,
+                                                              "trials": tune.trials}},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
                          "kernel": "k_force", "force_ms_per_launch": force_ms,
@@ -482,6 +493,10 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-profile-pass", action="store_true")
     ap.add_argument("--relax-steps", type=int, default=300)
+    ap.add_argument("--no-autotune", dest="autotune", action="store_false",
+                    help="skip the autotuner (threads per particle, skin / rebuild cadence)")
+    ap.add_argument("--tune-skins", default="0.3,0.4,0.5",
+                    help="skins the autotuner may choose from (the rebuild cadence); empty: keep the configured skin")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -208,6 +208,10 @@ int simmd_energy_virial_noalloc(const simmd_params* p, const double* r, const do
 /* threads per particle in the force pass (1, 2, 4), CUDA-graph capture of
  * the step loop (0/1) and steps per captured graph. */
 int simmd_set_tuning(simmd_ctx* ctx, int32_t threads_per_particle, int32_t use_graphs, int32_t graph_steps);
+/* change the neighbour-list skin (the rebuild cadence) of one replica (or
+ * every replica: rep = -1); the lists are rebuilt before the next force
+ * evaluation.  Results are unchanged up to the order of the force sums. */
+int simmd_set_skin(simmd_ctx* ctx, int32_t rep, double skin);
 int simmd_sync(simmd_ctx* ctx);
 void* simmd_stream(simmd_ctx* ctx);          /* the context's cudaStream_t */
 int simmd_timer_start(simmd_ctx* ctx);       /* CUDA event on the context stream */

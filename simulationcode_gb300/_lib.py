@@ -87,6 +87,7 @@ SIGNATURES = {
     "simmd_stats_r": (C.c_int, [_vp, C.c_int32, _P(Stats)]),
     "simmd_replica_bytes": (C.c_int64, [_P(Params), C.c_int32]),
     "simmd_set_tuning": (C.c_int, [_vp, C.c_int32, C.c_int32, C.c_int32]),
+    "simmd_set_skin": (C.c_int, [_vp, C.c_int32, C.c_double]),
     "simmd_sync": (C.c_int, [_vp]),
     "simmd_stream": (_vp, [_vp]),
     "simmd_timer_start": (C.c_int, [_vp]),

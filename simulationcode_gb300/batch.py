@@ -145,6 +145,12 @@ class ReplicaBatch:
         return dict(force_ms=out[0], force_n=int(out[1]), kick_ms=out[2], rebuild_ms=out[3], update_ms=out[4],
                     steps=int(out[5]))
 
+    def set_skin(self, skin: float, rid: int = -1):
+        _lib.check(self.lib.simmd_set_skin(self.ctx, rid, skin))
+        for k, s in self.specs.items():
+            if rid in (-1, k):
+                s.skin = skin
+
     def set_tuning(self, tpp: int, graphs: bool = True, graph_steps: int = 16):
         _lib.check(self.lib.simmd_set_tuning(self.ctx, tpp, int(graphs), graph_steps))
 

@@ -71,6 +71,7 @@ struct HostRep {
     bool active = false;
     simmd_params p{};
     RepDesc d{};
+    double smax = 0.0;  // max(D): sets the Verlet radius
     long long steps_done = 0;
     long long noise_draws = 0;
     bool pending_rebuild = false;
@@ -368,10 +369,22 @@ static int validate(const simmd_params* p)
     return SIMMD_OK;
 }
 
-static int fill_desc(const simmd_params* p, const double* D, RepDesc& d)
+static double max_diameter(const double* D, long long N)
 {
     double smax = D[0];
-    for (long long i = 1; i < p->N; i++) smax = std::max(smax, D[i]);
+    for (long long i = 1; i < N; i++) smax = std::max(smax, D[i]);
+    return smax;
+}
+
+static int fill_desc_smax(const simmd_params* p, double smax, RepDesc& d);
+
+static int fill_desc(const simmd_params* p, const double* D, RepDesc& d)
+{
+    return fill_desc_smax(p, max_diameter(D, p->N), d);
+}
+
+static int fill_desc_smax(const simmd_params* p, double smax, RepDesc& d)
+{
     if (!(smax > 0)) return set_err(SIMMD_ERR_BAD_ARG, "diameters must be positive");
     double rc_v = p->verlet_force_cutoff > 0 ? p->verlet_force_cutoff : std::sqrt(p->force_cutoff2);
     double rv = p->skin + rc_v * smax;  // verlet_sphere_size, src/DataStructs.jl:351-352
@@ -569,6 +582,7 @@ static int add_replica(simmd_ctx* c, const simmd_params* p, const double* r, con
     h.active = true;
     h.p = *p;
     h.d = d;
+    h.smax = max_diameter(D, p->N);
     TRY(push_desc(c, rid));
     TRY(reset_state(c, rid, false));
     TRY(upload_rep(c, rid, r, v, F, D, nullptr));
@@ -913,6 +927,7 @@ int simmd_upload_r(simmd_ctx* c, int32_t rep, const double* r, const double* v, 
     // the Verlet radius depends on max(D): refresh the descriptor and cells
     RepDesc d;
     TRY(fill_desc(&h.p, D, d));
+    h.smax = max_diameter(D, h.p.N);
     if (d.ncell != h.d.ncell) {
         give_range(c->free_cells, h.d.cell0, h.d.ncell + 1);
         long long cstart;
@@ -1330,6 +1345,42 @@ int simmd_relax(simmd_ctx* c, int64_t nsteps, double step_size, double max_disp)
         st.vscale = 1.0;
         st.nonfinite = 0;
         CK(cudaMemcpyAsync(c->d_state + r, &st, sizeof(RepState), cudaMemcpyHostToDevice, c->stream));
+    }
+    CK(cudaStreamSynchronize(c->stream));
+    return SIMMD_OK;
+}
+
+int simmd_set_skin(simmd_ctx* c, int32_t rep, double skin)
+{
+    if (!c || !(skin >= 0)) return set_err(SIMMD_ERR_BAD_ARG, "bad argument");
+    CK(cudaSetDevice(c->device));
+    for (int r = 0; r < c->R_cap; r++) {
+        HostRep& h = c->reps[r];
+        if (!h.active || (rep >= 0 && r != rep)) continue;
+        simmd_params p = h.p;
+        p.skin = skin;
+        RepDesc d;
+        TRY(fill_desc_smax(&p, h.smax, d));
+        d.slot0 = h.d.slot0;
+        d.tile0 = h.d.tile0;
+        d.cell0 = h.d.cell0;
+        if (d.ncell != h.d.ncell) {
+            give_range(c->free_cells, h.d.cell0, h.d.ncell + 1);
+            long long cstart;
+            if (!take_range(c->free_cells, d.ncell + 1, &cstart)) {
+                TRY(ensure_capacity(c, c->S_cap, c->C_cap + d.ncell + 1, c->R_cap, c->K));
+                if (!take_range(c->free_cells, d.ncell + 1, &cstart)) return set_err(SIMMD_ERR_BUDGET, "cells");
+            }
+            d.cell0 = (int)cstart;
+        }
+        d.noise_mode = h.d.noise_mode;
+        d.host_noise = h.d.host_noise;
+        d.noise_step0 = h.d.noise_step0;
+        d.noise_nsteps = h.d.noise_nsteps;
+        h.p = p;
+        h.d = d;
+        TRY(push_desc(c, r));
+        h.pending_rebuild = true;
     }
     CK(cudaStreamSynchronize(c->stream));
     return SIMMD_OK;

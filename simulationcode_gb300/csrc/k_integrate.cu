@@ -22,10 +22,24 @@ namespace simmd {
 // the divide for |dr| < L, no FP64 divide on the path
 __device__ __forceinline__ double wrap_coord(double x, const RepDesc& d)
 {
-    if (x >= 0.0 && x < d.wrap_hi) return x;
+    // the common case 0 <= x < wrap_hi decided on the bit pattern (integer
+    // pipe; non-negative doubles order as integers, x < 0 has the sign bit)
+    const long long bits = __double_as_longlong(x);
+    if (bits >= 0 && bits < __double_as_longlong(d.wrap_hi)) return x;
     if (x < 0.0 && x >= -d.L) return dsub(x, -d.L);
     if (x >= d.wrap_hi && x < 2.0 * d.wrap_hi) return dsub(x, d.L);  // RN(x/L) in [1, 2)
     return dsub(x, dmul(floor(ddiv(x, d.L)), d.L));
+}
+
+// FP32 offset refresh: x - m*h in FP64 (one subtract; m*h exact), rounded to
+// FP32; the periodic unwrap (rare: a particle that crossed the box edge since
+// its rebuild) is decided in FP32 and redone in FP64 only then
+__device__ __forceinline__ float offset_refresh(double x, int m, const RepDesc& d)
+{
+    const double o = dsub(x, (double)m * d.h);
+    const float of = (float)o;
+    if (fabsf(of) < d.halfLf * 0.9f) return of;
+    return grid_offset(x, m, d);
 }
 
 __device__ __forceinline__ double half_kick(double v, double F, const RepDesc& d)
@@ -56,8 +70,9 @@ __device__ __forceinline__ double drift_slot(const Batch& b, const RepDesc& d, l
     S.posD[i] = make_double4_32a(x, y, z, p.w);
     if (d.prec == PREC_FP32) {
         const int g = S.rec[i].g;
-        S.rec[i].o = make_float4(grid_offset(x, grid_axis(g, 0), d), grid_offset(y, grid_axis(g, 1), d),
-                                 d.dims == 3 ? grid_offset(z, grid_axis(g, 2), d) : 0.0f, (float)p.w);
+        const float w = S.rec[i].o.w;
+        S.rec[i].o = make_float4(offset_refresh(x, grid_axis(g, 0), d), offset_refresh(y, grid_axis(g, 1), d),
+                                 d.dims == 3 ? offset_refresh(z, grid_axis(g, 2), d) : 0.0f, w);
     }
     return u2;
 }

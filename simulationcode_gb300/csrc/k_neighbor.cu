@@ -222,8 +222,7 @@ constexpr int BLD_THREADS = 128;
 constexpr int BLD_CHUNK = 512;
 
 struct BuildSmem {
-    float4 o[BLD_CHUNK];
-    int g[BLD_CHUNK];
+    float4 o[BLD_CHUNK];  // position relative to the home cell's grid reference (FP32), D
     int slot[BLD_CHUNK];
     int ca[27];
     int cn[27];
@@ -266,6 +265,10 @@ __device__ void build_cell(const Batch& b, const RepDesc& d, RepState& st, int c
     }
     __syncthreads();
     const int M = sm.pre[nst];
+    // grid reference point near the home cell centre: candidate coordinates
+    // relative to it are small, so a pair difference is one FP32 subtract
+    const int rfx = grid_index(((double)cx + 0.5) * d.cs, d), rfy = grid_index(((double)cy + 0.5) * d.cs, d),
+              rfz = (DIM == 3) ? grid_index(((double)cz + 0.5) * d.cs, d) : 0;
     const int Tb = P <= 16 ? 8 : (P <= 32 ? 4 : (P <= 64 ? 2 : 1));
     const int sub = tid % Tb;
     const int lane = tid & 31;
@@ -279,11 +282,12 @@ __device__ void build_cell(const Batch& b, const RepDesc& d, RepState& st, int c
         const bool active = p < P;
         const long long i = ha + (active ? p : 0);
         float4 oi = make_float4(0.f, 0.f, 0.f, 0.f);
-        int gi = 0;
         double4_32a pi = make_double4_32a(0.0, 0.0, 0.0, 0.0);
         if (active) {
-            oi = S.rec[i].o;
-            gi = S.rec[i].g;
+            const float4 o = S.rec[i].o;
+            const int g = S.rec[i].g;
+            oi = make_float4(split_dx(o.x, 0.0f, grid_axis(g, 0), rfx, d), split_dx(o.y, 0.0f, grid_axis(g, 1), rfy, d),
+                             DIM == 3 ? split_dx(o.z, 0.0f, grid_axis(g, 2), rfz, d) : 0.0f, o.w);
             pi = S.t_posD[i];
         }
         int cnt = 0, cntf = 0;
@@ -295,8 +299,11 @@ __device__ void build_cell(const Batch& b, const RepDesc& d, RepState& st, int c
                 int k = 0;
                 while (k + 1 < nst && sm.pre[k + 1] <= idx) k++;
                 const int j = sm.ca[k] + (idx - sm.pre[k]);
-                sm.o[q] = S.rec[j].o;
-                sm.g[q] = S.rec[j].g;
+                const float4 o = S.rec[j].o;
+                const int g = S.rec[j].g;
+                sm.o[q] = make_float4(split_dx(o.x, 0.0f, grid_axis(g, 0), rfx, d),
+                                      split_dx(o.y, 0.0f, grid_axis(g, 1), rfy, d),
+                                      DIM == 3 ? split_dx(o.z, 0.0f, grid_axis(g, 2), rfz, d) : 0.0f, o.w);
                 sm.slot[q] = j;
             }
             __syncthreads();
@@ -307,12 +314,11 @@ __device__ void build_cell(const Batch& b, const RepDesc& d, RepState& st, int c
                     const int j = sm.slot[q];
                     if (j != (int)i) {
                         const float4 oj = sm.o[q];
-                        const int gj = sm.g[q];
-                        const float dxf = split_dx(oi.x, oj.x, grid_axis(gi, 0), grid_axis(gj, 0), d);
-                        const float dyf = split_dx(oi.y, oj.y, grid_axis(gi, 1), grid_axis(gj, 1), d);
+                        const float dxf = min_image_f32(oi.x - oj.x, d.halfLf, d.Lf);
+                        const float dyf = min_image_f32(oi.y - oj.y, d.halfLf, d.Lf);
                         float d2f = dxf * dxf + dyf * dyf;
                         if (DIM == 3) {
-                            const float dzf = split_dx(oi.z, oj.z, grid_axis(gi, 2), grid_axis(gj, 2), d);
+                            const float dzf = min_image_f32(oi.z - oj.z, d.halfLf, d.Lf);
                             d2f += dzf * dzf;
                         }
                         // FP32 classification against the reference thresholds with a

@@ -47,7 +47,7 @@ def berthier_spec(N, dims, dynamics, rng, *, rho=1.02, skin=0.3, kBT=0.1, gamma=
     r = rng.uniform(0.0, L, (N, dims))
     v = gaussian_velocities(N, dims, kBT, 1.0, rng) if dynamics != _lib.BROWNIAN else None
     if max_neighbors is None:
-        max_neighbors = 80 if dims == 3 else 32
+        max_neighbors = 96 if dims == 3 else 40
     return ReplicaSpec(dims=dims, potential=_lib.POT_BERTHIER, dynamics=dynamics, N=N, box_size=L,
                        force_cutoff2=U.rc ** 2, skin=skin, verlet_force_cutoff=U.rc, r=r, D=D, v=v,
                        precision=precision, kBT=kBT, gamma=gamma, dt=dt, b_c0=U.c0, b_c2=U.c2, b_c4=U.c4,

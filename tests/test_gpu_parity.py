@@ -150,3 +150,22 @@ def test_split_precision_force_error(simlib, oracle, pot, dims, N):
     e64, w64, _ = g64.energy()
     e32, w32, _ = g32.energy()
     assert abs(e32 - e64) / N < 1e-5
+
+
+def test_set_skin_rebuilds_with_new_pair_set(simlib, oracle):
+    """simmd_set_skin (the autotuner's rebuild-cadence knob): the lists after
+    the change are the reference's lists for the new skin."""
+    import ctypes as C
+    p, r, v, D, rc = make_case(1, 3, 0, 1728, seed=12)
+    gpu = GpuSystem(p, r, D, v=v, force_cutoff=rc)
+    gpu.rebuild()
+    assert gpu.lib.simmd_set_skin(gpu.ctx, -1, C.c_double(0.5)) == 0
+    gpu.rebuild()
+    q = oracle.OrcParams.from_buffer_copy(p)
+    q.skin = 0.5
+    ref = oracle.OracleSystem(q, r, D, v=v, force_cutoff=rc)
+    ref.update_neighbor_lists()
+    assert np.array_equal(gpu.pairs(0), ref.half_pairs())
+    Fr = ref.calculate_new_forces().copy()
+    Fg = gpu.forces()
+    assert np.abs(Fg - Fr).max() <= 1e-12 * np.abs(Fr).max()
