@@ -188,11 +188,15 @@ def relax_specs(specs, device, steps=300, step_size=1e-3, cap=0.05):
     fmax = max(float(np.abs(b.state(i)[2]).max()) for i in ids[:64])
     print("relaxed: max |F| over the first replicas %.3g" % fmax, file=sys.stderr, flush=True)
     relax_launches[0] += b.launches()
+    kc = b.kernel_counts()
+    relax_counts[0] += kc[0]
+    relax_counts[1] += kc[1]
     b.close()
     return out
 
 
 relax_launches = [0]
+relax_counts = [0, 0]
 
 
 def plain_fp64_one_at_a_time(specs, device, steps=32):
@@ -361,8 +365,9 @@ def run_gpu(args, dist):
     batch.step(args.warmup)
     st_before = [batch.stats(i) for i in ids]
     # kernel launches of this process before the timed region (for ncu -s)
+    kc = batch.kernel_counts()
     print("LAUNCHES_BEFORE_TIMED=%d FORCE_LAUNCHES_BEFORE_TIMED=%d BUILD_LAUNCHES_BEFORE_TIMED=%d" % (
-        relax_launches[0] + batch.launches(), args.relax_steps + args.warmup, args.relax_steps + 2 + args.warmup),
+        relax_launches[0] + batch.launches(), relax_counts[0] + kc[0], relax_counts[1] + kc[1]),
         file=sys.stderr, flush=True)
     clocks = ClockSampler(device)
     clocks.start()

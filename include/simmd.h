@@ -217,6 +217,8 @@ void* simmd_stream(simmd_ctx* ctx);          /* the context's cudaStream_t */
 int simmd_timer_start(simmd_ctx* ctx);       /* CUDA event on the context stream */
 int simmd_timer_stop(simmd_ctx* ctx, float* ms);
 int64_t simmd_launch_count(simmd_ctx* ctx);  /* kernels launched by this context */
+/* force-kernel launches and neighbour-rebuild sequences issued so far */
+int simmd_kernel_counts(simmd_ctx* ctx, int64_t* force_launches, int64_t* rebuild_sequences);
 int64_t simmd_device_bytes(simmd_ctx* ctx);  /* device memory held */
 /* time the force pass alone: nrep launches, average ms per launch (CUDA
  * events around the launches on the context stream) */

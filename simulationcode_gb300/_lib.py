@@ -93,6 +93,7 @@ SIGNATURES = {
     "simmd_timer_start": (C.c_int, [_vp]),
     "simmd_timer_stop": (C.c_int, [_vp, _P(C.c_float)]),
     "simmd_launch_count": (C.c_int64, [_vp]),
+    "simmd_kernel_counts": (C.c_int, [_vp, _P(C.c_int64), _P(C.c_int64)]),
     "simmd_device_bytes": (C.c_int64, [_vp]),
     "simmd_time_force": (C.c_int, [_vp, C.c_int32, _P(C.c_float)]),
     "simmd_set_profile": (C.c_int, [_vp, C.c_int32]),

@@ -27,7 +27,7 @@ class TuneResult:
 
 
 def autotune(batch: ReplicaBatch, *, tpps: Iterable[int] = (1, 2, 4), skins: Optional[Iterable[float]] = None,
-             graph_steps: Iterable[int] = (16,), warmup: int = 16, steps: int = 48, log=None) -> TuneResult:
+             graph_steps: Iterable[int] = (16,), warmup: int = 32, steps: int = 96, log=None) -> TuneResult:
     """Grid search; ``skins`` None keeps the replicas' configured skin."""
     base_skin = next(iter(batch.specs.values())).skin if batch.specs else 0.3
     skins = [base_skin] if skins is None else list(skins)

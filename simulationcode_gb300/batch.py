@@ -58,6 +58,11 @@ class ReplicaSpec:
         p.rescale_temperature = int(bool(self.rescale_temperature))
         return p
 
+    def kernel_counts(self):
+        f, r = C.c_int64(), C.c_int64()
+        _lib.check(self.lib.simmd_kernel_counts(self.ctx, C.byref(f), C.byref(r)))
+        return f.value, r.value
+
     def device_bytes(self) -> int:
         p = self.params()
         return int(_lib.load().simmd_replica_bytes(C.byref(p), self.max_neighbors))
@@ -124,6 +129,11 @@ class ReplicaBatch:
 
     def launches(self) -> int:
         return int(self.lib.simmd_launch_count(self.ctx))
+
+    def kernel_counts(self):
+        f, r = C.c_int64(), C.c_int64()
+        _lib.check(self.lib.simmd_kernel_counts(self.ctx, C.byref(f), C.byref(r)))
+        return f.value, r.value
 
     def device_bytes(self) -> int:
         return int(self.lib.simmd_device_bytes(self.ctx))

@@ -110,6 +110,9 @@ struct simmd_ctx {
     int* d_tile_rep = nullptr;
     double* d_tile_part = nullptr;
     int* d_queue = nullptr;
+    int* d_plan_tiles = nullptr;
+    int2* d_plan_cells = nullptr;
+    int* d_plan_cnt = nullptr;
     std::vector<int> h_tile_rep;
     std::vector<RepState> h_state;
     double* d_stage = nullptr;  // AoS staging, 5 arrays of stage_cap doubles
@@ -118,11 +121,13 @@ struct simmd_ctx {
     long long noise_cap = 0;
     long long bytes = 0;
     long long launches = 0;
+    long long n_force = 0, n_rebuild = 0;  // force kernel launches, rebuild sequences
     long long max_count_seen = 0;
     // graph cache
     cudaGraphExec_t gexec = nullptr;
     int gkey = -1;
     long long g_launches_per_replay = 0;
+    long long g_force_per_replay = 0, g_rebuild_per_replay = 0;
 };
 
 // ---------------------------------------------------------------------------
@@ -241,6 +246,7 @@ static int ensure_capacity(simmd_ctx* c, long long S_need, long long C_need, int
         TRY(grow_fresh(c, &c->epp, S_old, S_new));
         long long nt_old = S_old / TILE, nt_new = S_new / TILE;
         TRY(grow_fresh(c, &c->d_tile_part, nt_old * NPART, nt_new * NPART));
+        TRY(grow_fresh(c, &c->d_plan_tiles, nt_old, nt_new));
         TRY(grow_keep(c, &c->d_tile_rep, nt_old, nt_new));
         c->h_tile_rep.resize((size_t)nt_new, -1);
         CK(cudaMemcpyAsync(c->d_tile_rep, c->h_tile_rep.data(), sizeof(int) * nt_new, cudaMemcpyHostToDevice,
@@ -267,6 +273,7 @@ static int ensure_capacity(simmd_ctx* c, long long S_need, long long C_need, int
         long long C_old = c->C_cap, C_new = std::max(C_need, C_old + C_old / 2);
         TRY(grow_fresh(c, &c->s.cell_count, C_old, C_new));
         TRY(grow_fresh(c, &c->s.cell_start, C_old, C_new));
+        TRY(grow_fresh(c, &c->d_plan_cells, C_old, C_new));
         c->free_cells.push_back({C_old, C_new - C_old});
         c->C_cap = C_new;
         force_rebuild_all(c);
@@ -333,6 +340,9 @@ static Batch make_batch(simmd_ctx* c)
     b.s = c->s;
     b.tile_part = c->d_tile_part;
     b.queue = c->d_queue;
+    b.plan_tiles = c->d_plan_tiles;
+    b.plan_cells = c->d_plan_cells;
+    b.plan_cnt = c->d_plan_cnt;
     return b;
 }
 
@@ -630,6 +640,7 @@ static Mix batch_mix(simmd_ctx* c)
 
 static void rebuild_launch(simmd_ctx* c, const Batch& b, const LaunchCfg& lc)
 {
+    c->n_rebuild += 1;
     launch_rebuild_impl(b, lc, c->keep_full ? c->nbr_full : nullptr, c->keep_full ? c->ncnt_full : nullptr,
                         c->Kfull);
 }
@@ -646,6 +657,7 @@ static void enqueue_step(simmd_ctx* c, const Batch& b, const LaunchCfg& lc, cons
     }
     if (prof) cudaEventRecord(c->pev[3], c->stream);
     launch_force_impl(b, lc, fmode, m.prec_mask, nullptr);
+    c->n_force += __builtin_popcount(m.prec_mask);
     if (prof) cudaEventRecord(c->pev[4], c->stream);
     if (m.rescale) launch_rescale_impl(b, lc);
     if (m.br) {
@@ -762,12 +774,16 @@ static int run_steps(simmd_ctx* c, long long nsteps, const double* noise)
         if (!c->gexec || c->gkey != key) {
             invalidate_graph(c);
             cudaGraph_t g;
-            long long l0 = c->launches;
+            long long l0 = c->launches, f0 = c->n_force, r0 = c->n_rebuild;
             CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
             for (int s = 0; s < c->graph_steps; s++) enqueue_step(c, b, lc, m, fmode);
             cudaError_t e = cudaStreamEndCapture(c->stream, &g);
             c->g_launches_per_replay = c->launches - l0;
+            c->g_force_per_replay = c->n_force - f0;
+            c->g_rebuild_per_replay = c->n_rebuild - r0;
             c->launches = l0;
+            c->n_force = f0;
+            c->n_rebuild = r0;
             CK(e);
             e = cudaGraphInstantiate(&c->gexec, g, 0);
             cudaGraphDestroy(g);
@@ -778,6 +794,8 @@ static int run_steps(simmd_ctx* c, long long nsteps, const double* noise)
         for (long long k = 0; k < reps; k++) {
             CK(cudaGraphLaunch(c->gexec, c->stream));
             c->launches += c->g_launches_per_replay;
+            c->n_force += c->g_force_per_replay;
+            c->n_rebuild += c->g_rebuild_per_replay;
         }
         for (long long s = reps * c->graph_steps; s < nsteps; s++) enqueue_step(c, b, lc, m, fmode);
         CK(cudaGetLastError());
@@ -852,6 +870,9 @@ int simmd_engine_create(int32_t device, simmd_ctx** out)
     for (auto& e : c->pev) cudaEventCreate(&e);
     int st = dalloc(c, &c->d_queue, 4);
     if (st == SIMMD_OK) st = cudaMemsetAsync(c->d_queue, 0, 4 * sizeof(int), c->stream) == cudaSuccess ? 0 : SIMMD_ERR_CUDA;
+    if (st == SIMMD_OK) st = dalloc(c, &c->d_plan_cnt, 4);
+    if (st == SIMMD_OK)
+        st = cudaMemsetAsync(c->d_plan_cnt, 0, 4 * sizeof(int), c->stream) == cudaSuccess ? 0 : SIMMD_ERR_CUDA;
     if (st != SIMMD_OK) {
         delete c;
         return st;
@@ -869,7 +890,8 @@ static void destroy_ctx(simmd_ctx* c)
     void* ptrs[] = {s.posD, s.vx, s.vy, s.vz, s.fx, s.fy, s.fz, s.ux, s.uy, s.uz, s.rec, s.cellc, s.orig, s.nbr,
                     s.ncnt, s.bin_cell, s.bin_rank, s.src, s.t_posD, s.t_vx, s.t_vy, s.t_vz, s.t_fx, s.t_fy,
                     s.t_fz, s.t_orig, s.cell_count, s.cell_start, c->nbr_full, c->ncnt_full, c->epp, c->d_desc,
-                    c->d_state, c->d_tile_rep, c->d_tile_part, c->d_queue, c->d_stage, c->d_noise};
+                    c->d_state, c->d_tile_rep, c->d_tile_part, c->d_queue, c->d_stage, c->d_noise,
+                    c->d_plan_tiles, c->d_plan_cells, c->d_plan_cnt};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     cudaEventDestroy(c->ev0);
@@ -1286,6 +1308,14 @@ int simmd_timer_stop(simmd_ctx* c, float* ms)
 }
 
 int64_t simmd_launch_count(simmd_ctx* c) { return c ? c->launches : 0; }
+
+int simmd_kernel_counts(simmd_ctx* c, int64_t* force_launches, int64_t* rebuild_sequences)
+{
+    if (!c) return set_err(SIMMD_ERR_BAD_ARG, "NULL context");
+    if (force_launches) *force_launches = c->n_force;
+    if (rebuild_sequences) *rebuild_sequences = c->n_rebuild;
+    return SIMMD_OK;
+}
 int64_t simmd_device_bytes(simmd_ctx* c) { return c ? c->bytes : 0; }
 
 int simmd_time_force(simmd_ctx* c, int32_t nrep, float* ms_per_launch)

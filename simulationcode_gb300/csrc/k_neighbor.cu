@@ -2,51 +2,71 @@
 // src/NeighborLists.jl:24-104 of SimulationCode.jl) for every replica whose
 // skin trigger fired or whose rebuild was requested by the host.
 //
-// Sequence (each kernel covers all replicas and skips those not rebuilding):
-//   zero      cell counters of the replica
+// Sequence:
+//   plan      one block per replica: a rebuilding replica appends its tiles
+//             and cells to the plan lists and zeroes its cell counters; the
+//             kernels below work on those lists only, so the cost follows the
+//             replicas that rebuild, not the batch size
 //   bin       cell of each particle (FP64 position / cell size), rank in the
 //             cell by atomicAdd
 //   scan      one block per replica: exclusive scan of the counts -> starts
 //   scatter   new slot = start[cell] + rank  (src[new] = old slot)
-//   cellsort  each cell's slots ordered by original particle id, so the
-//             layout (and every later sum) is deterministic and independent
-//             of the other replicas in the batch
+//   cellsort  one warp per cell: slots ordered by original particle id, so
+//             the layout (and every later sum) is deterministic and
+//             independent of the other replicas in the batch
 //   gather    particle state to the new order (staging), displacement := 0,
-//             packed cell coordinates and FP32 cell-relative offsets
-//   build     per particle, the 27 (3D) / 9 (2D) stencil cells; an FP32
-//             prefilter on the offsets, then the exact FP64 test of the
-//             reference: d2 <= verlet^2 (the pair enumeration radius) and
+//             packed cell coordinates and split-precision records
+//   build     one block per cell: the stencil's candidates staged in shared
+//             memory; FP32 classification with a margin, the exact FP64 test
+//             of the reference only in the band around a threshold:
+//             d2 <= verlet^2 (the pair enumeration radius) and
 //             d2 < (sqrt(rc2)*mean_d + skin)^2 (add_pair!'s half-list test),
 //             d2 from dx - round(dx/L)*L in the reference's operation order.
 //             The list stores each pair in both directions (no atomics in
-//             the force pass); staging copied back to the main arrays.
-//   done      reset displacement max / request flag, count the rebuild.
+//             the force pass)
+//   copyback  staging to the main arrays
+//   done      reset displacement max / request flag, count the rebuild,
+//             clear the plan
 #include "simmd_internal.cuh"
 
 namespace simmd {
 
 __device__ __forceinline__ int pack_cell(int cx, int cy, int cz) { return cx | (cy << 10) | (cz << 20); }
 
-__global__ void k_rb_zero(Batch b)
+__device__ __forceinline__ int plan_count(const Batch& b, int which)
 {
-    for (int t = blockIdx.x; t < b.ntiles; t += gridDim.x) {
-        int r = b.tile_rep[t];
-        if (r < 0) continue;
-        const RepDesc& d = b.desc[r];
-        if (!need_rebuild(b.state[r], d)) continue;
-        int tl = t - d.tile0;
-        for (int c = tl * TILE + threadIdx.x; c < d.ncell + 1; c += d.ntiles * TILE)
-            b.s.cell_count[d.cell0 + c] = 0;
+    return *(volatile const int*)&b.plan_cnt[which];
+}
+
+// one block per replica: the tiles and cells of a rebuilding replica go to
+// the plan lists (order of replicas arbitrary, each task independent), and
+// its cell counters are zeroed
+__global__ void k_rb_plan(Batch b)
+{
+    const int r = blockIdx.x;
+    if (r >= b.nreps) return;
+    const RepDesc& d = b.desc[r];
+    if (!d.active || !need_rebuild(b.state[r], d)) return;
+    __shared__ int s_tb, s_cb;
+    if (threadIdx.x == 0) {
+        s_tb = atomicAdd(&b.plan_cnt[0], d.ntiles);
+        s_cb = atomicAdd(&b.plan_cnt[1], d.ncell);
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < d.ntiles; k += blockDim.x) b.plan_tiles[s_tb + k] = d.tile0 + k;
+    for (int c = threadIdx.x; c < d.ncell; c += blockDim.x) {
+        b.plan_cells[s_cb + c] = make_int2(r, c);
+        b.s.cell_count[d.cell0 + c] = 0;
     }
 }
 
 __global__ void k_rb_bin(Batch b)
 {
-    for (int t = blockIdx.x; t < b.ntiles; t += gridDim.x) {
-        int r = b.tile_rep[t];
-        if (r < 0) continue;
+    const int ntask = plan_count(b, 0);
+    for (int k = blockIdx.x; k < ntask; k += gridDim.x) {
+        const int t = b.plan_tiles[k];
+        const int r = b.tile_rep[t];
         const RepDesc& d = b.desc[r];
-        if (!need_rebuild(b.state[r], d)) continue;
         long long s = (long long)t * TILE + threadIdx.x;
         if (s >= d.slot0 + d.n) continue;
         double4_32a p = b.s.posD[s];
@@ -56,10 +76,10 @@ __global__ void k_rb_bin(Batch b)
         bool finite = isfinite(p.x) && isfinite(p.y) && isfinite(p.z);
         if (!finite) b.state[r].nonfinite = 1;
         if (nc > 1 && finite) {
-            for (int k = 0; k < d.dims; k++) {
-                int ci = (int)floor(x[k] * d.inv_cs);
+            for (int k2 = 0; k2 < d.dims; k2++) {
+                int ci = (int)floor(x[k2] * d.inv_cs);
                 ci = ci < 0 ? 0 : (ci >= nc ? nc - 1 : ci);
-                c[k] = ci;
+                c[k2] = ci;
             }
         }
         int lin = c[0] + nc * (c[1] + nc * c[2]);
@@ -118,11 +138,11 @@ __global__ void k_rb_scan(Batch b)
 
 __global__ void k_rb_scatter(Batch b)
 {
-    for (int t = blockIdx.x; t < b.ntiles; t += gridDim.x) {
-        int r = b.tile_rep[t];
-        if (r < 0) continue;
+    const int ntask = plan_count(b, 0);
+    for (int k = blockIdx.x; k < ntask; k += gridDim.x) {
+        const int t = b.plan_tiles[k];
+        const int r = b.tile_rep[t];
         const RepDesc& d = b.desc[r];
-        if (!need_rebuild(b.state[r], d)) continue;
         long long s = (long long)t * TILE + threadIdx.x;
         if (s >= d.slot0 + d.n) continue;
         int nw = b.s.cell_start[d.cell0 + b.s.bin_cell[s]] + b.s.bin_rank[s];
@@ -130,21 +150,32 @@ __global__ void k_rb_scatter(Batch b)
     }
 }
 
+// one warp per cell: the cell's slots ordered by original particle id (rank
+// sort through shuffles; ids are unique), so the layout is deterministic
 __global__ void k_rb_cellsort(Batch b)
 {
-    for (int t = blockIdx.x; t < b.ntiles; t += gridDim.x) {
-        int r = b.tile_rep[t];
-        if (r < 0) continue;
-        const RepDesc& d = b.desc[r];
-        if (!need_rebuild(b.state[r], d)) continue;
-        int tl = t - d.tile0;
-        for (int c = tl * TILE + threadIdx.x; c < d.ncell; c += d.ntiles * TILE) {
-            int a = b.s.cell_start[d.cell0 + c], e = b.s.cell_start[d.cell0 + c + 1];
-            int* src = b.s.src;
-            for (int k = a + 1; k < e; k++) {  // insertion sort by original id
-                int sv = src[k];
+    const int ntask = plan_count(b, 1);
+    const int lane = threadIdx.x & 31;
+    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
+    int* src = b.s.src;
+    for (int k = gw; k < ntask; k += nw) {
+        const int2 task = b.plan_cells[k];
+        const RepDesc& d = b.desc[task.x];
+        const int a = b.s.cell_start[d.cell0 + task.y], e = b.s.cell_start[d.cell0 + task.y + 1];
+        const int n = e - a;
+        if (n <= 32) {
+            const int v = lane < n ? src[a + lane] : 0;
+            const int key = lane < n ? b.s.orig[v] : 0x7fffffff;
+            int rank = 0;
+            for (int q = 0; q < n; q++) rank += (__shfl_sync(0xffffffffu, key, q) < key) ? 1 : 0;
+            __syncwarp();
+            if (lane < n) src[a + rank] = v;
+            __syncwarp();
+        } else if (lane == 0) {  // large cell (tiny boxes): insertion sort
+            for (int q = a + 1; q < e; q++) {
+                int sv = src[q];
                 int key = b.s.orig[sv];
-                int m = k - 1;
+                int m = q - 1;
                 while (m >= a && b.s.orig[src[m]] > key) {
                     src[m + 1] = src[m];
                     m--;
@@ -157,11 +188,11 @@ __global__ void k_rb_cellsort(Batch b)
 
 __global__ void k_rb_gather(Batch b, int* ncnt_full)
 {
-    for (int t = blockIdx.x; t < b.ntiles; t += gridDim.x) {
-        int r = b.tile_rep[t];
-        if (r < 0) continue;
+    const int ntask = plan_count(b, 0);
+    for (int k = blockIdx.x; k < ntask; k += gridDim.x) {
+        const int t = b.plan_tiles[k];
+        const int r = b.tile_rep[t];
         const RepDesc& d = b.desc[r];
-        if (!need_rebuild(b.state[r], d)) continue;
         long long nw = (long long)t * TILE + threadIdx.x;
         Slots& S = b.s;
         S.ux[nw] = 0.0;
@@ -391,31 +422,27 @@ __device__ void build_cell(const Batch& b, const RepDesc& d, RepState& st, int c
 __global__ void __launch_bounds__(BLD_THREADS) k_rb_build(Batch b, unsigned* nbr_full, int* ncnt_full, int Kfull)
 {
     __shared__ BuildSmem sm;
-    for (int t = blockIdx.x; t < b.ntiles; t += gridDim.x) {
-        int r = b.tile_rep[t];
-        if (r < 0) continue;
-        const RepDesc& d = b.desc[r];
-        RepState& st = b.state[r];
-        if (!need_rebuild(st, d)) continue;
+    const int ntask = plan_count(b, 1);
+    for (int k = blockIdx.x; k < ntask; k += gridDim.x) {
+        const int2 task = b.plan_cells[k];
+        const RepDesc& d = b.desc[task.x];
+        RepState& st = b.state[task.x];
         if (threadIdx.x == 0) {
             sm.entries = 0ull;
             sm.maxcnt = 0;
         }
         __syncthreads();
-        const int tl = t - d.tile0;
-        for (int c = tl; c < d.ncell; c += d.ntiles) {
-            if (d.dims == 3) {
-                if (nbr_full) build_cell<3, true>(b, d, st, c, sm, nbr_full, ncnt_full, Kfull);
-                else build_cell<3, false>(b, d, st, c, sm, nbr_full, ncnt_full, Kfull);
-            } else {
-                if (nbr_full) build_cell<2, true>(b, d, st, c, sm, nbr_full, ncnt_full, Kfull);
-                else build_cell<2, false>(b, d, st, c, sm, nbr_full, ncnt_full, Kfull);
-            }
+        if (d.dims == 3) {
+            if (nbr_full) build_cell<3, true>(b, d, st, task.y, sm, nbr_full, ncnt_full, Kfull);
+            else build_cell<3, false>(b, d, st, task.y, sm, nbr_full, ncnt_full, Kfull);
+        } else {
+            if (nbr_full) build_cell<2, true>(b, d, st, task.y, sm, nbr_full, ncnt_full, Kfull);
+            else build_cell<2, false>(b, d, st, task.y, sm, nbr_full, ncnt_full, Kfull);
         }
         __syncthreads();
-        if (threadIdx.x == 0) {
+        if (threadIdx.x == 0 && sm.entries) {
             atomicMax(&st.maxcount, sm.maxcnt);
-            if (sm.entries) atomicAdd((unsigned long long*)&st.list_entries, sm.entries);
+            atomicAdd((unsigned long long*)&st.list_entries, sm.entries);
         }
         __syncthreads();
     }
@@ -425,11 +452,9 @@ __global__ void __launch_bounds__(BLD_THREADS) k_rb_build(Batch b, unsigned* nbr
 // reads neighbours' staged positions
 __global__ void k_rb_copyback(Batch b)
 {
-    for (int t = blockIdx.x; t < b.ntiles; t += gridDim.x) {
-        int r = b.tile_rep[t];
-        if (r < 0) continue;
-        const RepDesc& d = b.desc[r];
-        if (!need_rebuild(b.state[r], d)) continue;
+    const int ntask = plan_count(b, 0);
+    for (int k = blockIdx.x; k < ntask; k += gridDim.x) {
+        const int t = b.plan_tiles[k];
         long long i = (long long)t * TILE + threadIdx.x;
         Slots& S = b.s;
         S.posD[i] = S.t_posD[i];
@@ -446,6 +471,10 @@ __global__ void k_rb_copyback(Batch b)
 __global__ void k_rb_done(Batch b)
 {
     int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r == 0) {  // every rebuild kernel of this sequence has run: the plan is spent
+        b.plan_cnt[0] = 0;
+        b.plan_cnt[1] = 0;
+    }
     if (r >= b.nreps) return;
     const RepDesc& d = b.desc[r];
     RepState& st = b.state[r];
@@ -458,7 +487,7 @@ __global__ void k_rb_done(Batch b)
 void launch_rebuild_impl(const Batch& b, const LaunchCfg& lc, unsigned* nbr_full, int* ncnt_full, int Kfull)
 {
     int g = lc.grid_stream;
-    k_rb_zero<<<g, TILE, 0, lc.stream>>>(b);
+    k_rb_plan<<<b.nreps, 128, 0, lc.stream>>>(b);
     k_rb_bin<<<g, TILE, 0, lc.stream>>>(b);
     k_rb_scan<<<b.nreps, 1024, 0, lc.stream>>>(b);
     k_rb_scatter<<<g, TILE, 0, lc.stream>>>(b);

@@ -119,6 +119,10 @@ struct Batch {
     Slots s;
     double* tile_part;            // [ntiles][NPART]
     int* queue;                   // work-queue heads [4]
+    // rebuild plan: tiles and cells of the replicas rebuilding this step
+    int* plan_tiles;              // [ntiles]
+    int2* plan_cells;             // [cell capacity] (replica, cell)
+    int* plan_cnt;                // [0] tiles, [1] cells
 };
 
 // ---------------------------------------------------------------------------
