@@ -222,13 +222,20 @@ def plain_fp64_one_at_a_time(specs, device, steps=32):
             "replicas": len(specs)}
 
 
-def split_precision_error(specs, device, nsample=16):
+def split_precision_error(specs, device, positions=None, nsample=16):
     """FP32-split vs FP64 on the same configurations (pair forces, Newtonian
-    copies so no noise enters): force relative RMS and |dE|/N."""
+    copies so no noise enters): force relative RMS and |dE|/N.  positions:
+    the workload's states after its timed steps (equilibrated), else the
+    set-up configurations."""
     import copy
     from simulationcode_gb300 import _lib
     from simulationcode_gb300.batch import ReplicaBatch
-    sample = specs[:nsample]
+    sample = []
+    for k, s0 in enumerate(specs[:nsample]):
+        s1 = copy.copy(s0)
+        if positions is not None:
+            s1.r = positions[k]
+        sample.append(s1)
     num = den = 0.0
     de = 0.0
     n = 0
@@ -354,6 +361,8 @@ def run_gpu(args, dist):
         for s, r in zip(specs, rel):
             s.r = r
     batch, ids = build_batch(specs, device, args.tpp)
+    if args.skin is not None:
+        batch.set_skin(args.skin)
     batch.rebuild()
     tune = None
     if args.autotune:
@@ -472,12 +481,15 @@ def run_gpu(args, dist):
             "step_breakdown_ms": {k: prof[k] / max(prof["steps"], 1) for k in ("force_ms", "kick_ms", "rebuild_ms",
                                                                                "update_ms")},
             "e2e": e2e, "gpu_launches": int(launches), "clocks": clk}
+    evolved = [batch.state(i)[0] for i in ids[:16]]
     batch.close()
     if dist.rank == 0 and any(s.precision != 0 for s in specs) and not args.no_compare:
         plain = plain_fp64_one_at_a_time(specs, device)
         line["plain_fp64_one_at_a_time"] = plain
         line["speedup_vs_plain_fp64"] = value / plain["value"]
-        line["split_precision_error"] = split_precision_error(specs, device)
+        err = split_precision_error(specs, device, positions=evolved)
+        err["states"] = "the workload's states after its timed steps"
+        line["split_precision_error"] = err
     if dist.rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline_port(specs, seconds=args.cpu_seconds)
     return line
@@ -498,6 +510,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-profile-pass", action="store_true")
     ap.add_argument("--relax-steps", type=int, default=300)
+    ap.add_argument("--skin", type=float, default=None, help="override the workload's skin (without autotuning)")
     ap.add_argument("--no-autotune", dest="autotune", action="store_false",
                     help="skip the autotuner (threads per particle, skin / rebuild cadence)")
     ap.add_argument("--tune-skins", default="0.3,0.4,0.5",

@@ -1374,6 +1374,7 @@ int simmd_relax(simmd_ctx* c, int64_t nsteps, double step_size, double max_disp)
         st.vmean[0] = st.vmean[1] = st.vmean[2] = 0.0;
         st.vscale = 1.0;
         st.nonfinite = 0;
+        st.fmean_pending = 0;
         CK(cudaMemcpyAsync(c->d_state + r, &st, sizeof(RepState), cudaMemcpyHostToDevice, c->stream));
     }
     CK(cudaStreamSynchronize(c->stream));

@@ -23,10 +23,10 @@
 // round-to-nearest intrinsics, so each pair force is bit-identical to the
 // reference expression; only the order of the per-particle sum differs.
 // FP32 split path: pair arithmetic in FP32 on FP32 offsets of the FP64
-// positions from a power-of-two grid, with the grid shift and the box's
-// grid-multiple part applied exactly (split_dx); IEEE reciprocals; one
-// 32-byte record per neighbour gather; per-particle sums, random force and
-// the mean-force partial sums in FP32, integration in FP64.
+// positions from a power-of-two grid, with the grid-point difference exact
+// (split_dx_g); one 32-byte record per neighbour gather; per-particle sums,
+// random force (four deviates per Philox call) and the mean-force partial
+// sums in FP32, integration in FP64.
 #include "simmd_internal.cuh"
 #include "simmd_reduce.cuh"
 
@@ -125,15 +125,14 @@ __device__ __forceinline__ void pairs_f64(const Batch& b, const RepDesc& d, long
 // FP32 split-precision pair
 // ---------------------------------------------------------------------------
 template <int DIM, int POT, bool EN>
-__device__ __forceinline__ void pair_f32(const RepDesc& d, const float4& oi, int mix, int miy, int miz,
-                                         const float4& oj, int gj, float& fx, float& fy, float& fz, float& e,
-                                         float& w)
+__device__ __forceinline__ void pair_f32(const RepDesc& d, const float4& oi, const float4& gi, const float4& oj,
+                                         const float4& gj, float& fx, float& fy, float& fz, float& e, float& w)
 {
-    const float dx = split_dx(oi.x, oj.x, mix, grid_axis(gj, 0), d);
-    const float dy = split_dx(oi.y, oj.y, miy, grid_axis(gj, 1), d);
+    const float dx = split_dx_g(oi.x, oj.x, gi.x, gj.x, d);
+    const float dy = split_dx_g(oi.y, oj.y, gi.y, gj.y, d);
     float dz = 0.0f, r2;
     if (DIM == 3) {
-        dz = split_dx(oi.z, oj.z, miz, grid_axis(gj, 2), d);
+        dz = split_dx_g(oi.z, oj.z, gi.z, gj.z, d);
         r2 = dx * dx + dy * dy + dz * dz;
     } else {
         r2 = dx * dx + dy * dy;
@@ -142,15 +141,15 @@ __device__ __forceinline__ void pair_f32(const RepDesc& d, const float4& oi, int
     if (POT == POT_BERTHIER) {
         const float md = (oi.w + oj.w) * 0.5f * (1.0f - d.zetaf * fabsf(oi.w - oj.w));
         const float mds = md * md;
-        const float inv = __frcp_rn(mds);
+        const float inv = __fdividef(1.0f, mds);
         const float ix2 = r2 * inv;
         const float ix4 = ix2 * ix2;
-        const float xi14 = __frcp_rn(ix4 * ix4 * ix4 * ix2);
+        const float xi14 = __fdividef(1.0f, ix4 * ix4 * ix4 * ix2);
         const bool in = r2 <= d.rc2f * mds;
         Fr = in ? -2.0f * inv * (d.c2f + 2.0f * d.c4f * ix2 - 6.0f * xi14) : 0.0f;
         if (EN && in) V = xi14 * ix2 + d.c4f * ix4 + d.c2f * ix2 + d.c0f;
     } else {
-        const float inv = __frcp_rn(r2);
+        const float inv = __fdividef(1.0f, r2);
         const float xi2 = (DIM == 3 ? d.sigma2f : d.sigma4f) * inv;
         const float xi6 = xi2 * xi2 * xi2;
         const float xi12 = xi6 * xi6;
@@ -167,28 +166,37 @@ __device__ __forceinline__ void pair_f32(const RepDesc& d, const float4& oi, int
     }
 }
 
+// list entry n of the particle: from the tile's rows staged in shared memory
+// (rows < nrows), else from global memory
+template <int T>
+__device__ __forceinline__ unsigned list_entry(const Batch& b, const unsigned* s_rows, int nrows, long long i, int p,
+                                               int n)
+{
+    const int row = n / T;
+    if (row < nrows) return s_rows[row * (TILE * T) + p * T + (n % T)] & IDX_MASK;
+    return __ldg(b.s.nbr + nbr_addr(n, i, T, b.S)) & IDX_MASK;
+}
+
 template <int DIM, int POT, bool EN, int T>
 __device__ __forceinline__ void pairs_f32(const Batch& b, const RepDesc& d, long long i, int sub,
-                                          const float4 oi, int gi, int cnt, float& fx, float& fy, float& fz,
-                                          float& e, float& w)
+                                          const float4 oi, const float4 gi, int cnt, float& fx, float& fy,
+                                          float& fz, float& e, float& w, const unsigned* s_rows, int nrows, int p)
 {
-    const unsigned* __restrict__ nbr = b.s.nbr;
     const SplitRec* __restrict__ rec = b.s.rec;
-    const int mix = grid_axis(gi, 0), miy = grid_axis(gi, 1), miz = grid_axis(gi, 2);
     int n = sub;
     for (; n + T < cnt; n += 2 * T) {
-        const unsigned j0 = __ldg(nbr + nbr_addr(n, i, T, b.S)) & IDX_MASK;
-        const unsigned j1 = __ldg(nbr + nbr_addr(n + T, i, T, b.S)) & IDX_MASK;
+        const unsigned j0 = list_entry<T>(b, s_rows, nrows, i, p, n);
+        const unsigned j1 = list_entry<T>(b, s_rows, nrows, i, p, n + T);
         const float4 o0 = __ldg(&rec[j0].o);
-        const int g0 = __ldg(&rec[j0].g);
+        const float4 g0 = __ldg(&rec[j0].g);
         const float4 o1 = __ldg(&rec[j1].o);
-        const int g1 = __ldg(&rec[j1].g);
-        pair_f32<DIM, POT, EN>(d, oi, mix, miy, miz, o0, g0, fx, fy, fz, e, w);
-        pair_f32<DIM, POT, EN>(d, oi, mix, miy, miz, o1, g1, fx, fy, fz, e, w);
+        const float4 g1 = __ldg(&rec[j1].g);
+        pair_f32<DIM, POT, EN>(d, oi, gi, o0, g0, fx, fy, fz, e, w);
+        pair_f32<DIM, POT, EN>(d, oi, gi, o1, g1, fx, fy, fz, e, w);
     }
     if (n < cnt) {
-        const unsigned j0 = __ldg(nbr + nbr_addr(n, i, T, b.S)) & IDX_MASK;
-        pair_f32<DIM, POT, EN>(d, oi, mix, miy, miz, __ldg(&rec[j0].o), __ldg(&rec[j0].g), fx, fy, fz, e, w);
+        const unsigned j0 = list_entry<T>(b, s_rows, nrows, i, p, n);
+        pair_f32<DIM, POT, EN>(d, oi, gi, __ldg(&rec[j0].o), __ldg(&rec[j0].g), fx, fy, fz, e, w);
     }
 }
 
@@ -233,27 +241,84 @@ __device__ __forceinline__ void particle_noise(const RepDesc& d, RepState& st, i
     }
 }
 
-template <int DIM, bool EN, int PREC, int T>
-__device__ __forceinline__ void particle_pairs(const Batch& b, const RepDesc& d, long long i, int sub, double& fx,
-                                               double& fy, double& fz, double& e, double& w)
+template <int DIM, bool EN, int T>
+__device__ __forceinline__ void particle_pairs_f64(const Batch& b, const RepDesc& d, long long i, int sub, double& fx,
+                                                   double& fy, double& fz, double& e, double& w)
 {
     const int cnt = b.s.ncnt[i];
-    if (PREC == PREC_FP64) {
-        const double4_32a pi = b.s.posD[i];
-        if (d.pot == POT_BERTHIER) pairs_f64<DIM, POT_BERTHIER, EN, T>(b, d, i, sub, pi, cnt, fx, fy, fz, e, w);
-        else pairs_f64<DIM, POT_LJ, EN, T>(b, d, i, sub, pi, cnt, fx, fy, fz, e, w);
-    } else {
-        const float4 oi = b.s.rec[i].o;
-        const int gi = b.s.rec[i].g;
-        float gx = 0.f, gy = 0.f, gz = 0.f, ge = 0.f, gw = 0.f;
-        if (d.pot == POT_BERTHIER) pairs_f32<DIM, POT_BERTHIER, EN, T>(b, d, i, sub, oi, gi, cnt, gx, gy, gz, ge, gw);
-        else pairs_f32<DIM, POT_LJ, EN, T>(b, d, i, sub, oi, gi, cnt, gx, gy, gz, ge, gw);
-        fx = gx;
-        fy = gy;
-        fz = gz;
-        e = ge;
-        w = gw;
+    const double4_32a pi = b.s.posD[i];
+    if (d.pot == POT_BERTHIER) pairs_f64<DIM, POT_BERTHIER, EN, T>(b, d, i, sub, pi, cnt, fx, fy, fz, e, w);
+    else pairs_f64<DIM, POT_LJ, EN, T>(b, d, i, sub, pi, cnt, fx, fy, fz, e, w);
+}
+
+template <int DIM, bool EN, int T>
+__device__ __forceinline__ void particle_pairs_f32(const Batch& b, const RepDesc& d, long long i, int sub, int cnt,
+                                                   float& fx, float& fy, float& fz, float& e, float& w,
+                                                   const unsigned* s_rows, int nrows, int p)
+{
+    const float4 oi = b.s.rec[i].o;
+    const float4 gi = b.s.rec[i].g;
+    if (d.pot == POT_BERTHIER)
+        pairs_f32<DIM, POT_BERTHIER, EN, T>(b, d, i, sub, oi, gi, cnt, fx, fy, fz, e, w, s_rows, nrows, p);
+    else pairs_f32<DIM, POT_LJ, EN, T>(b, d, i, sub, oi, gi, cnt, fx, fy, fz, e, w, s_rows, nrows, p);
+}
+
+// rows of the tile's list staged in shared memory (16-byte loads, all rows
+// issued at once): the pair loop then waits only on the record gathers
+constexpr int STAGE_WORDS = 6144;  // 24 KB of list entries per block
+
+template <int T>
+__device__ __forceinline__ int stage_rows(const Batch& b, int t, int maxcnt, unsigned* s_rows)
+{
+    constexpr int row_words = TILE * T;
+    const int nrows = min((maxcnt + T - 1) / T, STAGE_WORDS / row_words);
+    const int vec_per_row = row_words / 4;
+    const uint4* src = reinterpret_cast<const uint4*>(b.s.nbr);
+    uint4* dst = reinterpret_cast<uint4*>(s_rows);
+    for (int v = threadIdx.x; v < nrows * vec_per_row; v += blockDim.x) {
+        const int row = v / vec_per_row, c4 = v - row * vec_per_row;
+        dst[v] = __ldg(src + (((size_t)row * (size_t)(b.S * T) + (size_t)t * row_words) >> 2) + c4);
     }
+    return nrows;
+}
+
+template <typename R, int T, bool EN>
+__device__ __forceinline__ void combine_lanes(R& fx, R& fy, R& fz, R& e, R& w)
+{
+#pragma unroll
+    for (int o = T >> 1; o > 0; o >>= 1) {
+        fx += __shfl_xor_sync(0xffffffffu, fx, o);
+        fy += __shfl_xor_sync(0xffffffffu, fy, o);
+        fz += __shfl_xor_sync(0xffffffffu, fz, o);
+        if (EN) {
+            e += __shfl_xor_sync(0xffffffffu, e, o);
+            w += __shfl_xor_sync(0xffffffffu, w, o);
+        }
+    }
+}
+
+// last tile of a replica: the replica totals -> COM velocity / mean force,
+// energy and virial, noise counter
+template <int MODE, int NV>
+__device__ __forceinline__ void finish_replica(const RepDesc& d, RepState& st, const double (&out)[NV], bool noise)
+{
+    constexpr bool EN = (MODE == FMODE_ENERGY || MODE == FMODE_STEP_ENERGY);
+    constexpr bool STEP = (MODE == FMODE_STEP || MODE == FMODE_STEP_ENERGY);
+    const double nd = (double)d.n;
+    if (STEP) {
+        double* m = (d.dyn == DYN_BROWNIAN) ? st.fmean : st.vmean;
+        m[0] = ddiv(out[0], nd);
+        m[1] = ddiv(out[1], nd);
+        m[2] = ddiv(out[2], nd);
+    }
+    if (EN) {
+        st.epot = out[NV - 2] / 2.0;
+        st.virial = out[NV - 1] / 2.0;
+    }
+    // Brownian steps leave F - <F> implicit (applied by the position update
+    // and by the download); a plain force evaluation leaves F final
+    if (MODE != FMODE_ENERGY && d.dyn == DYN_BROWNIAN) st.fmean_pending = STEP ? 1 : 0;
+    if (noise) st.step += 1;
 }
 
 template <int MODE, int PREC, int T>
@@ -264,7 +329,9 @@ __global__ void __launch_bounds__(TILE * T, (PREC == PREC_FP32 ? 8 : 4) / T) k_f
     constexpr int NV = EN ? 5 : 3;
     __shared__ int s_tile;
     __shared__ int s_flag;
+    __shared__ int s_maxcnt;
     __shared__ double s_part[32 * NV];
+    __shared__ __align__(16) unsigned s_rows[PREC == PREC_FP32 ? STAGE_WORDS : 4];
     const int tid = threadIdx.x;
     const int p = tid / T, sub = tid - p * T;
     for (;;) {
@@ -280,143 +347,171 @@ __global__ void __launch_bounds__(TILE * T, (PREC == PREC_FP32 ? 8 : 4) / T) k_f
         RepState& st = b.state[r];
         const long long i = (long long)t * TILE + p;
         const bool real = i < d.slot0 + d.n;
-        double fx = 0.0, fy = 0.0, fz = 0.0, e = 0.0, w = 0.0;
-        if (real) {
-            if (d.dims == 3) particle_pairs<3, EN, PREC, T>(b, d, i, sub, fx, fy, fz, e, w);
-            else particle_pairs<2, EN, PREC, T>(b, d, i, sub, fx, fy, fz, e, w);
-        }
-        if (T > 1) {
-            if (PREC == PREC_FP32) {  // combine the T lanes in FP32
-                float gx = (float)fx, gy = (float)fy, gz = (float)fz, ge = (float)e, gw = (float)w;
-                for (int o = T >> 1; o > 0; o >>= 1) {
-                    gx += __shfl_xor_sync(0xffffffffu, gx, o);
-                    gy += __shfl_xor_sync(0xffffffffu, gy, o);
-                    gz += __shfl_xor_sync(0xffffffffu, gz, o);
-                    if (EN) {
-                        ge += __shfl_xor_sync(0xffffffffu, ge, o);
-                        gw += __shfl_xor_sync(0xffffffffu, gw, o);
-                    }
-                }
-                fx = gx; fy = gy; fz = gz; e = ge; w = gw;
-            } else {
-                for (int o = T >> 1; o > 0; o >>= 1) {
-                    fx += __shfl_xor_sync(0xffffffffu, fx, o);
-                    fy += __shfl_xor_sync(0xffffffffu, fy, o);
-                    fz += __shfl_xor_sync(0xffffffffu, fz, o);
-                    if (EN) {
-                        e += __shfl_xor_sync(0xffffffffu, e, o);
-                        w += __shfl_xor_sync(0xffffffffu, w, o);
-                    }
-                }
-            }
-        }
+        const bool noise = d.dyn != DYN_NEWTONIAN && MODE != FMODE_ENERGY && d.relax_cap == 0.0;
+        const bool nl = d.dyn != DYN_BROWNIAN;
         double pv[NV];
 #pragma unroll
         for (int k = 0; k < NV; k++) pv[k] = 0.0;
-        const bool noise = d.dyn != DYN_NEWTONIAN && MODE != FMODE_ENERGY && d.relax_cap == 0.0;
-        const bool nl = d.dyn != DYN_BROWNIAN;
-        if (sub == 0 && real) {
-            if (EN) {
-                pv[NV - 2] = e;
-                pv[NV - 1] = w;
-                if (epp) epp[i] = e / 2.0;
-            }
-            if (MODE != FMODE_ENERGY) {
-                double vx = 0.0, vy = 0.0, vz = 0.0;
-                if (nl) {
-                    vx = b.s.vx[i];
-                    vy = b.s.vy[i];
-                    if (d.dims == 3) vz = b.s.vz[i];
-                }
-                double Fx = fx, Fy = fy, Fz = fz;
-                if (noise) {
-                    double x0, x1, x2;
-                    particle_noise<PREC>(d, st, b.s.orig[i], x0, x1, x2);
-                    if (PREC == PREC_FP32) {  // random force in FP32, as the pair force
-                        const float nf = (float)d.noise_factor;
-                        float gx = (float)fx + nf * (float)x0, gy = (float)fy + nf * (float)x1,
-                              gz = (float)fz + nf * (float)x2;
-                        if (d.dyn == DYN_LANGEVIN) {
-                            const float mg = -(float)d.gamma;
-                            gx += mg * (float)vx;
-                            gy += mg * (float)vy;
-                            gz += mg * (float)vz;
-                        }
-                        Fx = gx; Fy = gy; Fz = gz;
-                    } else if (d.dyn == DYN_LANGEVIN) {
-                        const double mg = -d.gamma;
-                        Fx = dadd(Fx, dadd(dmul(mg, vx), dmul(d.noise_factor, x0)));
-                        Fy = dadd(Fy, dadd(dmul(mg, vy), dmul(d.noise_factor, x1)));
-                        if (d.dims == 3) Fz = dadd(Fz, dadd(dmul(mg, vz), dmul(d.noise_factor, x2)));
-                    } else {
-                        Fx = dadd(Fx, dmul(d.noise_factor, x0));
-                        Fy = dadd(Fy, dmul(d.noise_factor, x1));
-                        if (d.dims == 3) Fz = dadd(Fz, dmul(d.noise_factor, x2));
-                    }
-                }
-                b.s.fx[i] = Fx;
-                b.s.fy[i] = Fy;
-                if (d.dims == 3) b.s.fz[i] = Fz;
-                if (STEP) {
-                    if (nl) {  // kick2 (src/MD.jl:529-531)
-                        vx = kick(vx, Fx, d);
-                        vy = kick(vy, Fy, d);
-                        b.s.vx[i] = vx;
-                        b.s.vy[i] = vy;
-                        if (d.dims == 3) {
-                            vz = kick(vz, Fz, d);
-                            b.s.vz[i] = vz;
-                        }
-                        pv[0] = vx; pv[1] = vy; pv[2] = vz;
-                    } else {
-                        pv[0] = Fx; pv[1] = Fy; pv[2] = Fz;
-                    }
-                }
-            }
-        }
         double out[NV];
         bool last;
-        if (PREC == PREC_FP32 && STEP && !EN) {
-            // split precision: the Brownian mean-force partial sums per warp in
-            // FP32 (the forces carry FP32-level accuracy); velocity sums (FP64
-            // state) per warp in FP64; per-tile and per-replica sums in FP64
-            if (nl) {
-                warp_sum<NV>(pv);
-            } else {
-                float s0 = (float)pv[0], s1 = (float)pv[1], s2 = (float)pv[2];
+        if constexpr (PREC == PREC_FP32) {
+            // ---- split precision: everything per particle in FP32 except the
+            // FP64 state updates (force store, velocity kick)
+            float fx = 0.f, fy = 0.f, fz = 0.f, e = 0.f, w = 0.f;
+            const int cnt = real ? b.s.ncnt[i] : 0;
+            if (tid == 0) s_maxcnt = 0;
+            __syncthreads();
+            if (sub == 0 && cnt > 0) atomicMax(&s_maxcnt, cnt);
+            __syncthreads();
+            const int nrows = stage_rows<T>(b, t, s_maxcnt, s_rows);
+            __syncthreads();
+            if (real) {
+                if (d.dims == 3) particle_pairs_f32<3, EN, T>(b, d, i, sub, cnt, fx, fy, fz, e, w, s_rows, nrows, p);
+                else particle_pairs_f32<2, EN, T>(b, d, i, sub, cnt, fx, fy, fz, e, w, s_rows, nrows, p);
+            }
+            if (T > 1) combine_lanes<float, T, EN>(fx, fy, fz, e, w);
+            float q0 = 0.f, q1 = 0.f, q2 = 0.f;  // per-particle contribution to the replica sums
+            if (sub == 0 && real) {
+                if (EN && epp) epp[i] = (double)e / 2.0;
+                if (MODE != FMODE_ENERGY) {
+                    double vx = 0.0, vy = 0.0, vz = 0.0;
+                    if (nl) {
+                        vx = b.s.vx[i];
+                        vy = b.s.vy[i];
+                        if (d.dims == 3) vz = b.s.vz[i];
+                    }
+                    if (noise) {
+                        const float nf = (float)d.noise_factor;
+                        float z0, z1, z2 = 0.f, zz;
+                        if (d.noise_mode == NOISE_HOST) {
+                            double x0, x1, x2;
+                            particle_noise<PREC_FP32>(d, st, b.s.orig[i], x0, x1, x2);
+                            z0 = (float)x0;
+                            z1 = (float)x1;
+                            z2 = (float)x2;
+                        } else {
+                            normal_quad_f32(d.seed, st.step, b.s.orig[i], z0, z1, z2, zz);
+                        }
+                        fx += nf * z0;
+                        fy += nf * z1;
+                        fz += nf * z2;
+                        if (d.dyn == DYN_LANGEVIN) {
+                            const float mg = -(float)d.gamma;
+                            fx += mg * (float)vx;
+                            fy += mg * (float)vy;
+                            fz += mg * (float)vz;
+                        }
+                    }
+                    const double Fx = fx, Fy = fy, Fz = fz;
+                    b.s.fx[i] = Fx;
+                    b.s.fy[i] = Fy;
+                    if (d.dims == 3) b.s.fz[i] = Fz;
+                    if (STEP) {
+                        if (nl) {  // kick2 in FP64 (src/MD.jl:529-531)
+                            vx = kick(vx, Fx, d);
+                            vy = kick(vy, Fy, d);
+                            b.s.vx[i] = vx;
+                            b.s.vy[i] = vy;
+                            if (d.dims == 3) {
+                                vz = kick(vz, Fz, d);
+                                b.s.vz[i] = vz;
+                            }
+                            q0 = (float)vx;
+                            q1 = (float)vy;
+                            q2 = (float)vz;
+                        } else {
+                            q0 = fx;
+                            q1 = fy;
+                            q2 = fz;
+                        }
+                    }
+                }
+            }
+            // per-warp sums in FP32 (the summed quantities carry FP32-level
+            // accuracy), energy and virial in FP64; tile and replica sums FP64
+            if (STEP) {
 #pragma unroll
                 for (int o = 16; o > 0; o >>= 1) {
-                    s0 += __shfl_xor_sync(0xffffffffu, s0, o);
-                    s1 += __shfl_xor_sync(0xffffffffu, s1, o);
-                    s2 += __shfl_xor_sync(0xffffffffu, s2, o);
+                    q0 += __shfl_xor_sync(0xffffffffu, q0, o);
+                    q1 += __shfl_xor_sync(0xffffffffu, q1, o);
+                    q2 += __shfl_xor_sync(0xffffffffu, q2, o);
                 }
-                pv[0] = s0;
-                pv[1] = s1;
-                pv[2] = s2;
+                if ((tid & 31) == 0) {  // only lane 0's value is read (WARP_DONE)
+                    pv[0] = q0;
+                    pv[1] = q1;
+                    pv[2] = q2;
+                }
+            }
+            if (EN) {
+                double de = (sub == 0 && real) ? (double)e : 0.0, dw = (sub == 0 && real) ? (double)w : 0.0;
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) {
+                    de += __shfl_xor_sync(0xffffffffu, de, o);
+                    dw += __shfl_xor_sync(0xffffffffu, dw, o);
+                }
+                pv[NV - 2] = de;
+                pv[NV - 1] = dw;
             }
             last = tile_reduce<NV, true>(b, t, d, st, pv, out, s_part, &s_flag);
         } else {
-            last = tile_reduce<NV>(b, t, d, st, pv, out, s_part, &s_flag);
-        }
-        if (last && tid == 0) {
-            const double nd = (double)d.n;
-            if (STEP) {
-                if (d.dyn == DYN_BROWNIAN) {
-                    st.fmean[0] = ddiv(out[0], nd);
-                    st.fmean[1] = ddiv(out[1], nd);
-                    st.fmean[2] = ddiv(out[2], nd);
-                } else {
-                    st.vmean[0] = ddiv(out[0], nd);
-                    st.vmean[1] = ddiv(out[1], nd);
-                    st.vmean[2] = ddiv(out[2], nd);
+            // ---- FP64: the reference's arithmetic
+            double fx = 0.0, fy = 0.0, fz = 0.0, e = 0.0, w = 0.0;
+            if (real) {
+                if (d.dims == 3) particle_pairs_f64<3, EN, T>(b, d, i, sub, fx, fy, fz, e, w);
+                else particle_pairs_f64<2, EN, T>(b, d, i, sub, fx, fy, fz, e, w);
+            }
+            if (T > 1) combine_lanes<double, T, EN>(fx, fy, fz, e, w);
+            if (sub == 0 && real) {
+                if (EN) {
+                    pv[NV - 2] = e;
+                    pv[NV - 1] = w;
+                    if (epp) epp[i] = e / 2.0;
+                }
+                if (MODE != FMODE_ENERGY) {
+                    double vx = 0.0, vy = 0.0, vz = 0.0;
+                    if (nl) {
+                        vx = b.s.vx[i];
+                        vy = b.s.vy[i];
+                        if (d.dims == 3) vz = b.s.vz[i];
+                    }
+                    double Fx = fx, Fy = fy, Fz = fz;
+                    if (noise) {
+                        double x0, x1, x2;
+                        particle_noise<PREC_FP64>(d, st, b.s.orig[i], x0, x1, x2);
+                        if (d.dyn == DYN_LANGEVIN) {  // F += -gamma v + sqrt(2kBT gamma/dt) xi
+                            const double mg = -d.gamma;
+                            Fx = dadd(Fx, dadd(dmul(mg, vx), dmul(d.noise_factor, x0)));
+                            Fy = dadd(Fy, dadd(dmul(mg, vy), dmul(d.noise_factor, x1)));
+                            if (d.dims == 3) Fz = dadd(Fz, dadd(dmul(mg, vz), dmul(d.noise_factor, x2)));
+                        } else {
+                            Fx = dadd(Fx, dmul(d.noise_factor, x0));
+                            Fy = dadd(Fy, dmul(d.noise_factor, x1));
+                            if (d.dims == 3) Fz = dadd(Fz, dmul(d.noise_factor, x2));
+                        }
+                    }
+                    b.s.fx[i] = Fx;
+                    b.s.fy[i] = Fy;
+                    if (d.dims == 3) b.s.fz[i] = Fz;
+                    if (STEP) {
+                        if (nl) {  // kick2 (src/MD.jl:529-531)
+                            vx = kick(vx, Fx, d);
+                            vy = kick(vy, Fy, d);
+                            b.s.vx[i] = vx;
+                            b.s.vy[i] = vy;
+                            if (d.dims == 3) {
+                                vz = kick(vz, Fz, d);
+                                b.s.vz[i] = vz;
+                            }
+                            pv[0] = vx; pv[1] = vy; pv[2] = vz;
+                        } else {
+                            pv[0] = Fx; pv[1] = Fy; pv[2] = Fz;
+                        }
+                    }
                 }
             }
-            if (EN) {
-                st.epot = out[NV - 2] / 2.0;
-                st.virial = out[NV - 1] / 2.0;
-            }
-            if (noise) st.step += 1;
+            last = tile_reduce<NV>(b, t, d, st, pv, out, s_part, &s_flag);
         }
+        if (last && tid == 0) finish_replica<MODE, NV>(d, st, out, noise);
     }
     if (tid == 0) {
         __threadfence();

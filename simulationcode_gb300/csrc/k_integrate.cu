@@ -34,12 +34,15 @@ __device__ __forceinline__ double wrap_coord(double x, const RepDesc& d)
 // FP32 offset refresh: x - m*h in FP64 (one subtract; m*h exact), rounded to
 // FP32; the periodic unwrap (rare: a particle that crossed the box edge since
 // its rebuild) is decided in FP32 and redone in FP64 only then
-__device__ __forceinline__ float offset_refresh(double x, int m, const RepDesc& d)
+__device__ __forceinline__ float offset_refresh(double x, float g, const RepDesc& d)
 {
-    const double o = dsub(x, (double)m * d.h);
+    const double o = dsub(x, (double)g);  // exact: g = m*h and |x - g| small
     const float of = (float)o;
     if (fabsf(of) < d.halfLf * 0.9f) return of;
-    return grid_offset(x, m, d);
+    double q = o;  // crossed the periodic boundary since the rebuild
+    q = (q > d.halfL) ? q - d.L : q;
+    q = (q < -d.halfL) ? q + d.L : q;
+    return (float)q;
 }
 
 __device__ __forceinline__ double half_kick(double v, double F, const RepDesc& d)
@@ -69,10 +72,10 @@ __device__ __forceinline__ double drift_slot(const Batch& b, const RepDesc& d, l
     const double z = (d.dims == 3) ? wrap_coord(dadd(p.z, drz), d) : p.z;
     S.posD[i] = make_double4_32a(x, y, z, p.w);
     if (d.prec == PREC_FP32) {
-        const int g = S.rec[i].g;
+        const float4 g = S.rec[i].g;
         const float w = S.rec[i].o.w;
-        S.rec[i].o = make_float4(offset_refresh(x, grid_axis(g, 0), d), offset_refresh(y, grid_axis(g, 1), d),
-                                 d.dims == 3 ? offset_refresh(z, grid_axis(g, 2), d) : 0.0f, w);
+        S.rec[i].o = make_float4(offset_refresh(x, g.x, d), offset_refresh(y, g.y, d),
+                                 d.dims == 3 ? offset_refresh(z, g.z, d) : 0.0f, w);
     }
     return u2;
 }
@@ -135,8 +138,11 @@ __global__ void k_kick_drift(Batch b)
     }
 }
 
-// Brownian position update (src/MD.jl:444-467 as intended): F -= <F>,
-// dr = (dt/gamma) F, displacement, wrap
+// Brownian position update (src/MD.jl:444-467 as intended): dr = (dt/gamma)
+// (F - <F>), displacement, wrap.  F itself is left as computed (the mean
+// subtraction is applied again when F is downloaded), saving a store.
+// FP64 replicas: the reference's rounding, (dt/gamma)*(F - <F>); split
+// precision: one fused multiply-add (the force is FP32-accurate anyway).
 __global__ void k_brownian_update(Batch b)
 {
     __shared__ unsigned long long s_max[TILE / 32];
@@ -150,17 +156,17 @@ __global__ void k_brownian_update(Batch b)
         double u2 = 0.0;
         if (i < d.slot0 + d.n) {
             const Slots& S = b.s;
-            double Fx = dsub(S.fx[i], st.fmean[0]);
-            double Fy = dsub(S.fy[i], st.fmean[1]);
-            S.fx[i] = Fx;
-            S.fy[i] = Fy;
-            double Fz = 0.0;
-            if (d.dims == 3) {
-                Fz = dsub(S.fz[i], st.fmean[2]);
-                S.fz[i] = Fz;
+            const double c = d.dt_over_gamma;
+            double drx, dry, drz = 0.0;
+            if (d.prec == PREC_FP64) {
+                drx = dmul(c, dsub(S.fx[i], st.fmean[0]));
+                dry = dmul(c, dsub(S.fy[i], st.fmean[1]));
+                if (d.dims == 3) drz = dmul(c, dsub(S.fz[i], st.fmean[2]));
+            } else {
+                drx = fma(c, S.fx[i], -c * st.fmean[0]);
+                dry = fma(c, S.fy[i], -c * st.fmean[1]);
+                if (d.dims == 3) drz = fma(c, S.fz[i], -c * st.fmean[2]);
             }
-            double drx = dmul(d.dt_over_gamma, Fx), dry = dmul(d.dt_over_gamma, Fy),
-                   drz = dmul(d.dt_over_gamma, Fz);
             if (d.relax_cap > 0.0) {  // set-up relaxation: |dr| <= relax_cap per particle
                 double m = fmax(fabs(drx), fmax(fabs(dry), fabs(drz)));
                 if (m > 0.0) {
@@ -311,7 +317,7 @@ __global__ void k_load_aos(Batch b, int rep, const double* r, const double* v, c
     }
     S.ncnt[s] = 0;
     S.cellc[s] = 0;
-    rec_put(&S.rec[s], make_float4(0.f, 0.f, 0.f, 0.f), 0);
+    rec_put(&S.rec[s], make_float4(0.f, 0.f, 0.f, 0.f), make_float4(0.f, 0.f, 0.f, 0.f));
 }
 
 __global__ void k_store_aos(Batch b, int rep, double* r, double* v, double* F, double* disp,
@@ -336,9 +342,16 @@ __global__ void k_store_aos(Batch b, int rep, double* r, double* v, double* F, d
         if (dm == 3) v[o * dm + 2] = S.vz[s];
     }
     if (F) {
-        F[o * dm] = S.fx[s];
-        F[o * dm + 1] = S.fy[s];
-        if (dm == 3) F[o * dm + 2] = S.fz[s];
+        const RepState& st = b.state[rep];
+        if (d.dyn == DYN_BROWNIAN && st.fmean_pending) {  // F - <F> of the last Brownian step
+            F[o * dm] = dsub(S.fx[s], st.fmean[0]);
+            F[o * dm + 1] = dsub(S.fy[s], st.fmean[1]);
+            if (dm == 3) F[o * dm + 2] = dsub(S.fz[s], st.fmean[2]);
+        } else {
+            F[o * dm] = S.fx[s];
+            F[o * dm + 1] = S.fy[s];
+            if (dm == 3) F[o * dm + 2] = S.fz[s];
+        }
     }
     if (disp) {
         disp[o * dm] = S.ux[s];
@@ -366,9 +379,9 @@ __global__ void k_set_state(Batch b, int rep, const double* r, const double* v, 
         if (dm == 3) p.z = r[o * dm + 2];
         S.posD[s] = p;
         if (d.prec == PREC_FP32) {
-            const int g = S.rec[s].g;
-            S.rec[s].o = make_float4(grid_offset(p.x, grid_axis(g, 0), d), grid_offset(p.y, grid_axis(g, 1), d),
-                                   dm == 3 ? grid_offset(p.z, grid_axis(g, 2), d) : 0.0f, (float)p.w);
+            const float4 g = S.rec[s].g;
+            S.rec[s].o = make_float4(offset_refresh(p.x, g.x, d), offset_refresh(p.y, g.y, d),
+                                     dm == 3 ? offset_refresh(p.z, g.z, d) : 0.0f, (float)p.w);
         }
     }
     if (v) {
@@ -380,6 +393,7 @@ __global__ void k_set_state(Batch b, int rep, const double* r, const double* v, 
         S.fx[s] = F[o * dm];
         S.fy[s] = F[o * dm + 1];
         if (dm == 3) S.fz[s] = F[o * dm + 2];
+        if (k == 0) b.state[rep].fmean_pending = 0;  // the host's F is final
     }
     if (disp) {
         S.ux[s] = disp[o * dm];

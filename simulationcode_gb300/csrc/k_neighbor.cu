@@ -219,14 +219,14 @@ __global__ void k_rb_gather(Batch b, int* ncnt_full)
             rec_put(&S.rec[nw],
                     make_float4(grid_offset(p.x, mx, d), grid_offset(p.y, my, d),
                                 d.dims == 3 ? grid_offset(p.z, mz, d) : 0.0f, (float)p.w),
-                    mx | (my << 10) | (mz << 20));
+                    make_float4((float)mx * d.hf, (float)my * d.hf, (float)mz * d.hf, 0.0f));
         } else {
             S.t_posD[nw] = make_double4_32a(0.0, 0.0, 0.0, 0.0);
             S.t_vx[nw] = S.t_vy[nw] = S.t_vz[nw] = 0.0;
             S.t_fx[nw] = S.t_fy[nw] = S.t_fz[nw] = 0.0;
             S.t_orig[nw] = -1;
             S.cellc[nw] = 0;
-            rec_put(&S.rec[nw], make_float4(0.f, 0.f, 0.f, 0.f), 0);
+            rec_put(&S.rec[nw], make_float4(0.f, 0.f, 0.f, 0.f), make_float4(0.f, 0.f, 0.f, 0.f));
         }
     }
 }
@@ -298,8 +298,9 @@ __device__ void build_cell(const Batch& b, const RepDesc& d, RepState& st, int c
     const int M = sm.pre[nst];
     // grid reference point near the home cell centre: candidate coordinates
     // relative to it are small, so a pair difference is one FP32 subtract
-    const int rfx = grid_index(((double)cx + 0.5) * d.cs, d), rfy = grid_index(((double)cy + 0.5) * d.cs, d),
-              rfz = (DIM == 3) ? grid_index(((double)cz + 0.5) * d.cs, d) : 0;
+    const float rfx = (float)grid_index(((double)cx + 0.5) * d.cs, d) * d.hf,
+                rfy = (float)grid_index(((double)cy + 0.5) * d.cs, d) * d.hf,
+                rfz = (DIM == 3) ? (float)grid_index(((double)cz + 0.5) * d.cs, d) * d.hf : 0.0f;
     const int Tb = P <= 16 ? 8 : (P <= 32 ? 4 : (P <= 64 ? 2 : 1));
     const int sub = tid % Tb;
     const int lane = tid & 31;
@@ -316,9 +317,9 @@ __device__ void build_cell(const Batch& b, const RepDesc& d, RepState& st, int c
         double4_32a pi = make_double4_32a(0.0, 0.0, 0.0, 0.0);
         if (active) {
             const float4 o = S.rec[i].o;
-            const int g = S.rec[i].g;
-            oi = make_float4(split_dx(o.x, 0.0f, grid_axis(g, 0), rfx, d), split_dx(o.y, 0.0f, grid_axis(g, 1), rfy, d),
-                             DIM == 3 ? split_dx(o.z, 0.0f, grid_axis(g, 2), rfz, d) : 0.0f, o.w);
+            const float4 g = S.rec[i].g;
+            oi = make_float4(split_dx_g(o.x, 0.0f, g.x, rfx, d), split_dx_g(o.y, 0.0f, g.y, rfy, d),
+                             DIM == 3 ? split_dx_g(o.z, 0.0f, g.z, rfz, d) : 0.0f, o.w);
             pi = S.t_posD[i];
         }
         int cnt = 0, cntf = 0;
@@ -331,10 +332,9 @@ __device__ void build_cell(const Batch& b, const RepDesc& d, RepState& st, int c
                 while (k + 1 < nst && sm.pre[k + 1] <= idx) k++;
                 const int j = sm.ca[k] + (idx - sm.pre[k]);
                 const float4 o = S.rec[j].o;
-                const int g = S.rec[j].g;
-                sm.o[q] = make_float4(split_dx(o.x, 0.0f, grid_axis(g, 0), rfx, d),
-                                      split_dx(o.y, 0.0f, grid_axis(g, 1), rfy, d),
-                                      DIM == 3 ? split_dx(o.z, 0.0f, grid_axis(g, 2), rfz, d) : 0.0f, o.w);
+                const float4 g = S.rec[j].g;
+                sm.o[q] = make_float4(split_dx_g(o.x, 0.0f, g.x, rfx, d), split_dx_g(o.y, 0.0f, g.y, rfy, d),
+                                      DIM == 3 ? split_dx_g(o.z, 0.0f, g.z, rfz, d) : 0.0f, o.w);
                 sm.slot[q] = j;
             }
             __syncthreads();

@@ -68,6 +68,8 @@ struct RepState {
     int done_count;
     int maxcount;
     int noise_range_error;
+    int fmean_pending;            // Brownian: F holds F before the mean-force subtraction
+    int pad_state_;
     long long step;               // noise draws so far (Philox counter)
     long long rebuilds;
     long long list_entries;       // total list length at the last rebuild
@@ -81,9 +83,8 @@ struct RepState {
 // split-precision gather record (one 32-byte sector): FP32 offsets of the
 // FP64 position from its grid point, FP32 diameter, packed grid index
 struct __align__(32) SplitRec {
-    float4 o;   // x, y, z offsets, D
-    int g;      // grid index, 10 bits per axis
-    int pad[3];
+    float4 o;   // x, y, z offsets from the grid point, D
+    float4 g;   // grid point m*h per axis (exact in FP32), unused
 };
 
 struct Slots {
@@ -185,10 +186,23 @@ __device__ __forceinline__ float split_dx(float oi, float oj, int mi, int mj, co
     return (a - s * d.Llo_f) + (G0 - s * d.Lhi_f);
 }
 
-__device__ __forceinline__ void rec_put(SplitRec* r, float4 o, int g)
+__device__ __forceinline__ void rec_put(SplitRec* r, float4 o, float4 g)
 {
     r->o = o;
     r->g = g;
+}
+
+// minimum-image x_i - x_j from split records: (o_i - o_j) + (g_i - g_j) with
+// the grid difference exact; across the periodic boundary (rare) the box is
+// removed as L_hi (a grid multiple, exact) plus L_lo
+__device__ __forceinline__ float split_dx_g(float oi, float oj, float gi, float gj, const RepDesc& d)
+{
+    const float a = oi - oj;
+    const float G0 = gi - gj;
+    const float dx0 = a + G0;
+    if (fabsf(dx0) <= d.halfLf) return dx0;
+    const float s = dx0 > 0.0f ? 1.0f : -1.0f;
+    return (a - s * d.Llo_f) + (G0 - s * d.Lhi_f);
 }
 
 __device__ __forceinline__ bool need_rebuild(const RepState& st, const RepDesc& d)
@@ -234,6 +248,26 @@ __device__ __forceinline__ void normal_pair_f64(unsigned long long seed, long lo
     sincospi(2.0 * w, &s, &c);
     z0 = rad * c;
     z1 = rad * s;
+}
+
+// four FP32 deviates from one Philox call (split-precision path): 24-bit
+// uniforms from each 32-bit word, two Box-Muller pairs
+__device__ __forceinline__ void normal_quad_f32(unsigned long long seed, long long step, int particle, float& z0,
+                                                float& z1, float& z2, float& z3)
+{
+    uint4 o = philox4x32_10(make_uint4((unsigned)particle, 0u, (unsigned)step,
+                                       (unsigned)((unsigned long long)step >> 32)),
+                            make_uint2((unsigned)seed, (unsigned)(seed >> 32)));
+    const float u0 = ((float)(o.x >> 8) + 1.0f) * 0x1.0p-24f, w0 = (float)(o.y >> 8) * 0x1.0p-24f;
+    const float u1 = ((float)(o.z >> 8) + 1.0f) * 0x1.0p-24f, w1 = (float)(o.w >> 8) * 0x1.0p-24f;
+    const float r0 = sqrtf(-2.0f * __logf(u0)), r1 = sqrtf(-2.0f * __logf(u1));
+    float s0, c0, s1, c1;
+    sincospif(2.0f * w0, &s0, &c0);
+    sincospif(2.0f * w1, &s1, &c1);
+    z0 = r0 * c0;
+    z1 = r0 * s0;
+    z2 = r1 * c1;
+    z3 = r1 * s1;
 }
 
 // FP32 deviates (split-precision path): 24-bit uniforms, |z| <= 5.8

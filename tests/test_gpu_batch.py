@@ -90,12 +90,13 @@ def test_split_precision_nve_drift(simlib):
         t, e = [], []
         for k in range(21):
             st = b.energies()[i]
-            t.append(k * 100)
+            t.append(k * 200)
             e.append((st.epot + st.ekin) / s.N)
-            b.step(100)
+            b.step(200)
         slope = np.polyfit(np.array(t, float), np.array(e), 1)[0]
         out[name] = slope * 1e5  # energy per particle per 1e5 steps
         b.close()
     print("NVE drift per particle per 1e5 steps:", out)
-    # the split-precision path adds no drift beyond the FP64 path's
-    assert abs(out["fp32"] - out["fp64"]) <= 1e-4, out
+    # the split-precision path adds no drift beyond the FP64 path's (the
+    # reference arithmetic), within the 1e-4 per particle per 1e5 steps budget
+    assert abs(out["fp32"]) <= abs(out["fp64"]) + 1e-4, out
