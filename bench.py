@@ -148,15 +148,15 @@ def peaks():
 
 def force_bytes_per_launch(specs, stats):
     """Algorithmic HBM bytes of one force-kernel launch: per particle its own
-    position record (FP64 x,y,z,D = 32 B, or the FP32 offset record 16 B), the
+    position record (FP64 x,y,z,D = 32 B, or the split record = FP32 offsets,
+    D and FP32 grid point = 32 B), the
     list count, original id and 4 B per list entry, the force write (8 B per
     component) and, when the second half-kick is fused (Newtonian/Langevin),
     the velocity read and write (16 B per component).  Neighbour positions
     are gathered from L2 (cell-sorted layout) and not counted."""
     total = 0
     for s, st in zip(specs, stats):
-        own = 32 if s.precision == 0 else 16
-        per = own + 4 + 4 + 8 * s.dims
+        per = 32 + 4 + 4 + 8 * s.dims
         if s.dynamics != 2:
             per += 16 * s.dims
         total += s.N * per + 4 * int(st.list_entries)

@@ -231,7 +231,7 @@ static int ensure_capacity(simmd_ctx* c, long long S_need, long long C_need, int
         TRY(grow_keep(c, &s.rec, S_old, S_new));
         TRY(grow_keep(c, &s.cellc, S_old, S_new));
         TRY(grow_keep(c, &s.orig, S_old, S_new));
-        TRY(grow_fresh(c, &s.ncnt, S_old, S_new));
+        TRY(grow_keep(c, &s.ncnt, S_old, S_new));
         TRY(grow_fresh(c, &s.bin_cell, S_old, S_new));
         TRY(grow_fresh(c, &s.bin_rank, S_old, S_new));
         TRY(grow_fresh(c, &s.src, S_old, S_new));
@@ -256,17 +256,24 @@ static int ensure_capacity(simmd_ctx* c, long long S_need, long long C_need, int
         c->S_cap = S_new;
     }
     int K_new = grow_k ? K_need : c->K;
-    if (grow_s || grow_k) {
+    if (grow_s && !grow_k) {
+        // tile-major lists: the old tiles keep their addresses, so resident
+        // replicas keep their lists and their rebuild schedule
+        TRY(grow_keep(c, &c->s.nbr, S_old * (long long)c->K, c->S_cap * (long long)c->K));
+    }
+    if (grow_k) {
         dfree(c, &c->s.nbr, (size_t)S_old * (size_t)c->K);
         TRY(dalloc(c, &c->s.nbr, (size_t)c->S_cap * (size_t)K_new));
         c->K = K_new;
-        if (c->keep_full) {
-            dfree(c, &c->nbr_full, (size_t)S_old * (size_t)c->Kfull);
-            dfree(c, &c->ncnt_full, (size_t)S_old);
-            c->Kfull = std::max(c->K, c->Kfull);
-            TRY(dalloc(c, &c->nbr_full, (size_t)c->S_cap * (size_t)c->Kfull));
-            TRY(dalloc(c, &c->ncnt_full, (size_t)c->S_cap));
-        }
+        force_rebuild_all(c);
+    }
+    if ((grow_s || grow_k) && c->keep_full) {
+        // the full list (parity export only) is slot-major: rebuild it
+        dfree(c, &c->nbr_full, (size_t)S_old * (size_t)c->Kfull);
+        dfree(c, &c->ncnt_full, (size_t)S_old);
+        c->Kfull = std::max(c->K, c->Kfull);
+        TRY(dalloc(c, &c->nbr_full, (size_t)c->S_cap * (size_t)c->Kfull));
+        TRY(dalloc(c, &c->ncnt_full, (size_t)c->S_cap));
         force_rebuild_all(c);
     }
     if (grow_c) {
@@ -276,7 +283,7 @@ static int ensure_capacity(simmd_ctx* c, long long S_need, long long C_need, int
         TRY(grow_fresh(c, &c->d_plan_cells, C_old, C_new));
         c->free_cells.push_back({C_old, C_new - C_old});
         c->C_cap = C_new;
-        force_rebuild_all(c);
+        // cell counts and starts are scratch of each rebuild: nothing to keep
     }
     if (grow_r) {
         int R_old = c->R_cap, R_new = std::max(R_need, R_old + R_old / 2 + 1);

@@ -108,15 +108,15 @@ __device__ __forceinline__ void pairs_f64(const Batch& b, const RepDesc& d, long
     const double4_32a* __restrict__ posD = b.s.posD;
     int n = sub;
     for (; n + T < cnt; n += 2 * T) {
-        const unsigned j0 = __ldg(nbr + nbr_addr(n, i, T, b.S)) & IDX_MASK;
-        const unsigned j1 = __ldg(nbr + nbr_addr(n + T, i, T, b.S)) & IDX_MASK;
+        const unsigned j0 = __ldg(nbr + nbr_addr(n, i, T, b.K)) & IDX_MASK;
+        const unsigned j1 = __ldg(nbr + nbr_addr(n + T, i, T, b.K)) & IDX_MASK;
         const double4_32a p0 = posD[j0];
         const double4_32a p1 = posD[j1];
         pair_f64<DIM, POT, EN>(d, halfLb, pi, p0, fx, fy, fz, e, w);
         pair_f64<DIM, POT, EN>(d, halfLb, pi, p1, fx, fy, fz, e, w);
     }
     if (n < cnt) {
-        const unsigned j0 = __ldg(nbr + nbr_addr(n, i, T, b.S)) & IDX_MASK;
+        const unsigned j0 = __ldg(nbr + nbr_addr(n, i, T, b.K)) & IDX_MASK;
         pair_f64<DIM, POT, EN>(d, halfLb, pi, posD[j0], fx, fy, fz, e, w);
     }
 }
@@ -174,7 +174,7 @@ __device__ __forceinline__ unsigned list_entry(const Batch& b, const unsigned* s
 {
     const int row = n / T;
     if (row < nrows) return s_rows[row * (TILE * T) + p * T + (n % T)] & IDX_MASK;
-    return __ldg(b.s.nbr + nbr_addr(n, i, T, b.S)) & IDX_MASK;
+    return __ldg(b.s.nbr + nbr_addr(n, i, T, b.K)) & IDX_MASK;
 }
 
 template <int DIM, int POT, bool EN, int T>
@@ -272,13 +272,10 @@ __device__ __forceinline__ int stage_rows(const Batch& b, int t, int maxcnt, uns
 {
     constexpr int row_words = TILE * T;
     const int nrows = min((maxcnt + T - 1) / T, STAGE_WORDS / row_words);
-    const int vec_per_row = row_words / 4;
-    const uint4* src = reinterpret_cast<const uint4*>(b.s.nbr);
+    // the tile's rows are one contiguous run (tile-major list layout)
+    const uint4* src = reinterpret_cast<const uint4*>(b.s.nbr + (size_t)t * ((size_t)TILE * (size_t)b.K));
     uint4* dst = reinterpret_cast<uint4*>(s_rows);
-    for (int v = threadIdx.x; v < nrows * vec_per_row; v += blockDim.x) {
-        const int row = v / vec_per_row, c4 = v - row * vec_per_row;
-        dst[v] = __ldg(src + (((size_t)row * (size_t)(b.S * T) + (size_t)t * row_words) >> 2) + c4);
-    }
+    for (int v = threadIdx.x; v < nrows * (row_words / 4); v += blockDim.x) dst[v] = __ldg(src + v);
     return nrows;
 }
 

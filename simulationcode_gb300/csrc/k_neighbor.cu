@@ -391,7 +391,7 @@ __device__ void build_cell(const Batch& b, const RepDesc& d, RepState& st, int c
                 const unsigned gb = (bal >> gbase) & gmask;
                 if (pred) {
                     const int pos = cnt + __popc(gb & ((1u << sub) - 1u));
-                    if (pos < K) S.nbr[nbr_addr(pos, i, T, SS)] = (unsigned)sm.slot[q];
+                    if (pos < K) S.nbr[nbr_addr(pos, i, T, K)] = (unsigned)sm.slot[q];
                 }
                 cnt += __popc(gb);
                 if (FULL) {
@@ -515,7 +515,7 @@ __global__ void k_export(Batch b, int rep, const unsigned* lst, const int* cnt, 
     int n = cnt[s];
     long long k = 0;
     for (int q = 0; q < n; q++) {
-        unsigned e = half_only ? lst[nbr_addr(q, s, rowstride_T, b.S)] : lst[(size_t)q * b.S + s];
+        unsigned e = half_only ? lst[nbr_addr(q, s, rowstride_T, b.K)] : lst[(size_t)q * b.S + s];
         int oj = b.s.orig[e & IDX_MASK];
         if (half_only && oj < oi) continue;
         if (k < maxK) list[k + maxK * (long long)oi] = (long long)oj + 1;

@@ -210,9 +210,16 @@ __device__ __forceinline__ bool need_rebuild(const RepState& st, const RepDesc& 
     return st.force_rebuild || (__longlong_as_double((long long)st.maxdisp2) > d.skin_half2);
 }
 
-__device__ __forceinline__ size_t nbr_addr(int n, long long slot, int T, long long S)
+// List layout, tile-major: the TILE slots of a tile own TILE*K consecutive
+// entries (K = entries per particle, a multiple of T).  Row q of the tile
+// holds entries q*T .. q*T+T-1 of every particle of the tile, so the T
+// threads of one particle and the particles of one warp read one contiguous
+// run per row.  The address does not depend on the slot capacity, so a
+// capacity grow keeps the lists (a copy of the old prefix).
+__device__ __forceinline__ size_t nbr_addr(int n, long long slot, int T, int K)
 {
-    return (size_t)(n / T) * (size_t)(S * T) + (size_t)slot * T + (size_t)(n % T);
+    return (size_t)(slot / TILE) * ((size_t)TILE * (size_t)K) + (size_t)(n / T) * (size_t)(TILE * T) +
+           (size_t)(slot % TILE) * (size_t)T + (size_t)(n % T);
 }
 
 // ---------------------------------------------------------------------------
