@@ -222,6 +222,89 @@ def plain_fp64_one_at_a_time(specs, device, steps=32):
             "replicas": len(specs)}
 
 
+def run_serving(device, serve_seconds, capacity_seconds, concurrency=64, seed=5, log=None):
+    """Serving (continuous batching): (1) capacity = particle-steps/s of the
+    split-precision request mix with ``concurrency`` requests kept in flight
+    (closed loop, ``capacity_seconds`` of wall clock); (2) a Poisson stream at
+    0.8 x that capacity (in requests/s, from the stream's mean N*steps) for
+    ``serve_seconds`` of arrivals, served to completion: p50/p99 completion
+    latency and served particle-steps/s; (3) the plain FP64 path, one replica
+    at a time, on a sample of the same requests."""
+    from simulationcode_gb300 import workloads as W
+    from simulationcode_gb300.serving import Request, Server, poisson_arrivals
+    t_setup = time.perf_counter()
+    say = log or (lambda m: None)
+    pool = W.c5_requests(3 * concurrency, seed=seed + 1)
+    say("serving: %d capacity requests generated (%.1f s)" % (len(pool), time.perf_counter() - t_setup))
+    W.relax_on_device([s for s, _ in pool], device)
+    say("serving: relaxed (%.1f s)" % (time.perf_counter() - t_setup))
+    srv = Server(device=device, tick_steps=256, download=False)
+    it = iter(pool)
+    for _ in range(concurrency):
+        srv.submit(Request(*next(it)))
+    t0 = time.perf_counter()
+    exhausted = False
+    while time.perf_counter() - t0 < capacity_seconds and (srv.active or srv.waiting):
+        srv.admit()
+        srv.tick()
+        while not exhausted and len(srv.active) + len(srv.waiting) < concurrency:
+            try:
+                srv.submit(Request(*next(it)))
+            except StopIteration:
+                exhausted = True
+    cap_s = time.perf_counter() - t0
+    capacity = srv.particle_steps / cap_s
+    cap_failed = sum(1 for c in srv.completions if not c.ok)
+    srv.batch.close()
+    say("serving: capacity %.3g particle-steps/s over %.1f s, %d ticks, %d completed, %d failed" % (
+        capacity, cap_s, srv.ticks, len(srv.completions) - cap_failed, cap_failed))
+    if not capacity > 0 or cap_failed:
+        msgs = sorted({c.message for c in srv.completions if not c.ok})[:3]
+        return {"error": "capacity run failed: %d failed requests %s" % (cap_failed, msgs),
+                "capacity_particle_steps_per_s": capacity}
+    mean_work = float(np.mean([d[0] * d[4] for d in W.c5_draws(4096, seed=seed + 2)]))
+    rate = 0.8 * capacity / mean_work
+    n_req = max(16, int(round(rate * serve_seconds)))
+    say("serving: rate %.2f requests/s, %d requests" % (rate, n_req))
+    reqs = W.c5_requests(n_req, seed=seed + 2)
+    W.relax_on_device([s for s, _ in reqs], device)
+    rng = np.random.default_rng(seed + 3)
+    arrivals = poisson_arrivals(n_req, rate, rng)
+    setup_s = time.perf_counter() - t_setup - cap_s
+    say("serving: open loop starts (set-up %.1f s)" % setup_s)
+    srv = Server(device=device, tick_steps=256, download=True)
+    last = [time.perf_counter()]
+
+    def progress(s):
+        if time.perf_counter() - last[0] > 5.0:
+            last[0] = time.perf_counter()
+            say("serving: t=%.1f s active %d waiting %d done %d" % (s.now(), len(s.active), len(s.waiting),
+                                                                  len(s.completions)))
+
+    done = srv.run([Request(sp, st, float(a), tag=k) for k, ((sp, st), a) in enumerate(zip(reqs, arrivals))],
+                   sleep=lambda dt: time.sleep(min(dt, 1.0)), on_tick=progress)
+    summ = srv.summary(done)
+    srv.batch.close()
+    sample = [sp for sp, _ in reqs[:16]]
+    plain = plain_fp64_one_at_a_time(sample, device, steps=256)
+    out = {"capacity_particle_steps_per_s": capacity, "capacity_concurrency": concurrency,
+           "capacity_seconds": cap_s, "rate_requests_per_s": rate, "load": 0.8,
+           "mean_particle_steps_per_request": mean_work,
+           "p50_latency_s": summ["p50_s"], "p99_latency_s": summ["p99_s"], "mean_latency_s": summ["mean_s"],
+           "served_particle_steps_per_s": summ["particle_steps_per_s"], "requests": summ["requests"],
+           "completed": summ["completed"], "failed": summ["failed"], "makespan_s": summ["makespan_s"],
+           "peak_active": summ["peak_active"], "peak_admitted_bytes": summ["peak_admitted_bytes"],
+           "budget_bytes": summ["budget_bytes"], "ticks": summ["ticks"], "tick_steps": 256,
+           "plain_fp64_one_at_a_time": plain,
+           "capacity_vs_plain_fp64": capacity / plain["value"],
+           "setup_s": setup_s,
+           "precision": "f32-split", "arrival_window_s": serve_seconds}
+    if log:
+        log("serving: capacity %.3g ps/s, rate %.2f req/s, %d requests, p50 %.3f s, p99 %.3f s" % (
+            capacity, rate, n_req, summ["p50_s"], summ["p99_s"]))
+    return out
+
+
 def split_precision_error(specs, device, positions=None, nsample=16):
     """FP32-split vs FP64 on the same configurations (pair forces, Newtonian
     copies so no noise enters): force relative RMS and |dE|/N.  positions:
@@ -490,6 +573,9 @@ def run_gpu(args, dist):
         err = split_precision_error(specs, device, positions=evolved)
         err["states"] = "the workload's states after its timed steps"
         line["split_precision_error"] = err
+    if dist.rank == 0 and args.serve_seconds > 0:
+        line["serving"] = run_serving(device, args.serve_seconds, args.serve_capacity_seconds,
+                                      log=lambda m: print(m, file=sys.stderr, flush=True))
     if dist.rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline_port(specs, seconds=args.cpu_seconds)
     return line
@@ -515,6 +601,10 @@ def main():
                     help="skip the autotuner (threads per particle, skin / rebuild cadence)")
     ap.add_argument("--tune-skins", default="0.3,0.4,0.5",
                     help="skins the autotuner may choose from (the rebuild cadence); empty: keep the configured skin")
+    ap.add_argument("--serve-seconds", type=float, default=30.0,
+                    help="arrival window of the serving run (0: no serving run)")
+    ap.add_argument("--serve-capacity-seconds", type=float, default=6.0,
+                    help="closed-loop window that measures the serving capacity")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -180,6 +180,11 @@ int simmd_energy_all(simmd_ctx* ctx);
 int simmd_stats_r(simmd_ctx* ctx, int32_t rep, simmd_stats* out);
 /* device bytes a replica of this shape needs (admission against a budget) */
 int64_t simmd_replica_bytes(const simmd_params* p, int32_t max_neighbors);
+/* cap on the context's capacity-sized device memory (0 = none): a grow
+   that would pass it is not made and the call that needed it returns
+   SIMMD_ERR_BUDGET with the context unchanged.  No counterpart in the
+   reference (a serving-layer control). */
+int simmd_set_budget(simmd_ctx* ctx, int64_t bytes);
 
 /* ---- energy without device allocation ----------------------------------- */
 

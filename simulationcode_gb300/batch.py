@@ -58,12 +58,8 @@ class ReplicaSpec:
         p.rescale_temperature = int(bool(self.rescale_temperature))
         return p
 
-    def kernel_counts(self):
-        f, r = C.c_int64(), C.c_int64()
-        _lib.check(self.lib.simmd_kernel_counts(self.ctx, C.byref(f), C.byref(r)))
-        return f.value, r.value
-
     def device_bytes(self) -> int:
+        """device bytes this replica occupies in a context (admission)"""
         p = self.params()
         return int(_lib.load().simmd_replica_bytes(C.byref(p), self.max_neighbors))
 
@@ -137,6 +133,14 @@ class ReplicaBatch:
 
     def device_bytes(self) -> int:
         return int(self.lib.simmd_device_bytes(self.ctx))
+
+    def set_budget(self, nbytes: int):
+        """cap on the context's capacity grows (0 = none)"""
+        _lib.check(self.lib.simmd_set_budget(self.ctx, int(nbytes)))
+
+    def replica_bytes(self, spec: "ReplicaSpec") -> int:
+        p = spec.params()
+        return int(self.lib.simmd_replica_bytes(C.byref(p), spec.max_neighbors))
 
     def timer_start(self):
         _lib.check(self.lib.simmd_timer_start(self.ctx))

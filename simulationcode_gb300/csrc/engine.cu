@@ -120,6 +120,7 @@ struct simmd_ctx {
     double* d_noise = nullptr;
     long long noise_cap = 0;
     long long bytes = 0;
+    long long budget = 0;  // 0: no limit on capacity grows
     long long launches = 0;
     long long n_force = 0, n_rebuild = 0;  // force kernel launches, rebuild sequences
     long long max_count_seen = 0;
@@ -202,6 +203,23 @@ static int force_rebuild_all(simmd_ctx* c)
     return SIMMD_OK;
 }
 
+// device bytes of the capacity-sized arrays: per slot the state (posD 32,
+// v/F/u 72), the split record 32, cellc/orig/ncnt 12, rebuild scratch
+// (bin/rank/src 12, staged posD/v/F/orig 84), per-particle energy 8 and the
+// list 4K; per tile the partial sums, plan and owner; per cell count, start
+// and plan entry; per replica its descriptor and state
+constexpr long long SLOT_BYTES = 32 + 72 + 32 + 12 + 12 + 84 + 8;
+constexpr long long TILE_BYTES = NPART * 8 + 4 + 4;
+constexpr long long CELL_BYTES = 4 + 4 + 8;
+
+static long long capacity_bytes(const simmd_ctx* c, long long S, long long C, int R, int K)
+{
+    long long b = S * (SLOT_BYTES + 4LL * K) + (S / TILE) * TILE_BYTES + C * CELL_BYTES +
+                  (long long)R * (long long)(sizeof(RepDesc) + sizeof(RepState));
+    if (c->keep_full) b += S * (4LL * std::max(K, c->Kfull) + 4);
+    return b;
+}
+
 // (re)size everything that depends on slot capacity S, list rows K, T
 static int ensure_capacity(simmd_ctx* c, long long S_need, long long C_need, int R_need, int K_need)
 {
@@ -213,9 +231,28 @@ static int ensure_capacity(simmd_ctx* c, long long S_need, long long C_need, int
     bool grow_r = R_need > c->R_cap;
     bool grow_k = K_need > c->K;
     if (!grow_s && !grow_c && !grow_r && !grow_k) return SIMMD_OK;
-    invalidate_graph(c);
-    long long S_old = c->S_cap, S_new = grow_s ? std::max(S_need, S_old + S_old / 2) : S_old;
+    const long long S_old = c->S_cap, C_old = c->C_cap;
+    const int R_old = c->R_cap;
+    // geometric growth, or exactly the need when that would break the budget
+    long long S_new = grow_s ? std::max(S_need, S_old + S_old / 2) : S_old;
     S_new = (S_new + TILE - 1) / TILE * TILE;
+    long long C_new = grow_c ? std::max(C_need, C_old + C_old / 2) : C_old;
+    int R_new = grow_r ? std::max(R_need, R_old + R_old / 2 + 1) : R_old;
+    const int K_proj = grow_k ? K_need : c->K;
+    if (c->budget > 0) {
+        const long long now = capacity_bytes(c, S_old, C_old, R_old, c->K);
+        auto projected = [&](long long S, long long C, int R) {
+            return c->bytes - now + capacity_bytes(c, S, C, R, K_proj);
+        };
+        if (projected(S_new, C_new, R_new) > c->budget) {
+            if (grow_s) S_new = S_need;
+            if (grow_c) C_new = C_need;
+            if (grow_r) R_new = R_need;
+        }
+        if (projected(S_new, C_new, R_new) > c->budget)
+            return set_err(SIMMD_ERR_BUDGET, "device memory budget exceeded");
+    }
+    invalidate_graph(c);
     if (grow_s) {
         Slots& s = c->s;
         TRY(grow_keep(c, &s.posD, S_old, S_new));
@@ -277,7 +314,6 @@ static int ensure_capacity(simmd_ctx* c, long long S_need, long long C_need, int
         force_rebuild_all(c);
     }
     if (grow_c) {
-        long long C_old = c->C_cap, C_new = std::max(C_need, C_old + C_old / 2);
         TRY(grow_fresh(c, &c->s.cell_count, C_old, C_new));
         TRY(grow_fresh(c, &c->s.cell_start, C_old, C_new));
         TRY(grow_fresh(c, &c->d_plan_cells, C_old, C_new));
@@ -286,7 +322,6 @@ static int ensure_capacity(simmd_ctx* c, long long S_need, long long C_need, int
         // cell counts and starts are scratch of each rebuild: nothing to keep
     }
     if (grow_r) {
-        int R_old = c->R_cap, R_new = std::max(R_need, R_old + R_old / 2 + 1);
         TRY(grow_keep(c, &c->d_desc, R_old, R_new));
         TRY(grow_keep(c, &c->d_state, R_old, R_new));
         c->reps.resize(R_new);
@@ -1257,11 +1292,11 @@ int64_t simmd_replica_bytes(const simmd_params* p, int32_t max_neighbors)
     if (!p || p->N < 1) return 0;
     long long npad = (p->N + TILE - 1) / TILE * TILE;
     long long K = max_neighbors > 0 ? max_neighbors : 200;
-    // per slot: posD 32 + v,F,u 72 + off 16 + cellc/orig/ncnt 12 + scratch (bin x3 12, t_posD 32,
-    // t_v/t_F 48, t_orig 4) + epp 8 + list 4K
-    long long per = 32 + 72 + 16 + 12 + 12 + 32 + 48 + 4 + 8 + 4 * K;
-    long long cells = npad;  // upper bound of cells actually used
-    return npad * per + cells * 8 + 4096;
+    RepDesc d;
+    long long cells = npad;  // upper bound without the geometry
+    if (validate(p) == SIMMD_OK && fill_desc_smax(p, 1.0, d) == SIMMD_OK) cells = d.ncell + 1;
+    return npad * (SLOT_BYTES + 4 * K) + (npad / TILE) * TILE_BYTES + cells * CELL_BYTES +
+           (long long)(sizeof(RepDesc) + sizeof(RepState));
 }
 
 int simmd_set_tuning(simmd_ctx* c, int32_t tpp, int32_t use_graphs, int32_t graph_steps)
@@ -1324,6 +1359,14 @@ int simmd_kernel_counts(simmd_ctx* c, int64_t* force_launches, int64_t* rebuild_
     return SIMMD_OK;
 }
 int64_t simmd_device_bytes(simmd_ctx* c) { return c ? c->bytes : 0; }
+
+int simmd_set_budget(simmd_ctx* c, int64_t bytes)
+{
+    if (!c) return set_err(SIMMD_ERR_BAD_ARG, "NULL context");
+    if (bytes < 0) return set_err(SIMMD_ERR_BAD_ARG, "budget < 0");
+    c->budget = bytes;
+    return SIMMD_OK;
+}
 
 int simmd_time_force(simmd_ctx* c, int32_t nrep, float* ms_per_launch)
 {

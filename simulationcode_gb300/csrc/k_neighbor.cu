@@ -46,9 +46,12 @@ __global__ void k_rb_plan(Batch b)
     const int r = blockIdx.x;
     if (r >= b.nreps) return;
     const RepDesc& d = b.desc[r];
-    if (!d.active || !need_rebuild(b.state[r], d)) return;
+    // a replica with a non-finite state is not rebuilt (its particles would
+    // all bin into one cell); the host retires it on the status
+    if (!d.active || b.state[r].nonfinite || !need_rebuild(b.state[r], d)) return;
     __shared__ int s_tb, s_cb;
     if (threadIdx.x == 0) {
+        b.state[r].in_plan = 1;
         s_tb = atomicAdd(&b.plan_cnt[0], d.ntiles);
         s_cb = atomicAdd(&b.plan_cnt[1], d.ncell);
     }
@@ -94,7 +97,7 @@ __global__ void k_rb_scan(Batch b)
     int r = blockIdx.x;
     if (r >= b.nreps) return;
     const RepDesc& d = b.desc[r];
-    if (!d.active || !need_rebuild(b.state[r], d)) return;
+    if (!d.active || !b.state[r].in_plan) return;  // membership fixed by the plan
     __shared__ int warp_sums[32];
     const int nthr = blockDim.x;
     const int nc = d.ncell;
@@ -171,17 +174,20 @@ __global__ void k_rb_cellsort(Batch b)
             __syncwarp();
             if (lane < n) src[a + rank] = v;
             __syncwarp();
-        } else if (lane == 0) {  // large cell (tiny boxes): insertion sort
-            for (int q = a + 1; q < e; q++) {
-                int sv = src[q];
-                int key = b.s.orig[sv];
-                int m = q - 1;
-                while (m >= a && b.s.orig[src[m]] > key) {
-                    src[m + 1] = src[m];
-                    m--;
-                }
-                src[m + 1] = sv;
+        } else {  // larger cell: rank sort by the warp (n^2/32 compares per
+                  // lane), through the per-slot scratch bin_rank, which the
+                  // scatter has consumed
+            int* tmp = b.s.bin_rank;
+            for (int q = lane; q < n; q += 32) {
+                const int v = src[a + q];
+                const int key = b.s.orig[v];
+                int rank = 0;
+                for (int u = 0; u < n; u++) rank += (b.s.orig[src[a + u]] < key) ? 1 : 0;
+                tmp[a + rank] = v;
             }
+            __syncwarp();
+            for (int q = lane; q < n; q += 32) src[a + q] = tmp[a + q];
+            __syncwarp();
         }
     }
 }
@@ -478,7 +484,8 @@ __global__ void k_rb_done(Batch b)
     if (r >= b.nreps) return;
     const RepDesc& d = b.desc[r];
     RepState& st = b.state[r];
-    if (!d.active || !need_rebuild(st, d)) return;
+    if (!d.active || !st.in_plan) return;
+    st.in_plan = 0;
     st.maxdisp2 = 0ull;
     st.force_rebuild = 0;
     st.rebuilds += 1;

@@ -5,12 +5,11 @@
 //     multiple of TILE; slots hold particles in cell-sorted order after each
 //     rebuild, padding slots (orig < 0) never appear in a cell or a list;
 //   * per-slot SoA FP64 arrays v, F, displacement; an AoS double4_32a (x,y,z,D)
-//     gathered by neighbours; an AoS float4 of cell-relative FP32 offsets
-//     (split-precision path); packed rebuild-time cell coordinates; the
-//     original particle id;
-//   * a padded ELL neighbour list nbr[(n/T)*(S*T) + slot*T + n%T] (T = threads
-//     per particle) holding the slot of j in the low 26 bits and, for the
-//     split-precision path, the cell offset of j relative to i in the top 6;
+//     gathered by neighbours; a 32-byte split-precision record (FP32 offsets
+//     from a power-of-two grid point, D, the grid point); packed rebuild-time
+//     cell coordinates; the original particle id;
+//   * a padded ELL neighbour list, tile-major (see nbr_addr; T = threads per
+//     particle), each entry the slot of j (low 26 bits);
 //   * per-replica descriptors (read-only) and states (flags, counters,
 //     reductions), a tile -> replica table and per-tile partial sums.
 #pragma once
@@ -69,7 +68,7 @@ struct RepState {
     int maxcount;
     int noise_range_error;
     int fmean_pending;            // Brownian: F holds F before the mean-force subtraction
-    int pad_state_;
+    int in_plan;                  // listed by the current rebuild sequence's plan
     long long step;               // noise draws so far (Philox counter)
     long long rebuilds;
     long long list_entries;       // total list length at the last rebuild
