@@ -35,6 +35,19 @@ sys.path.insert(0, ROOT)
 MEASURED_PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
 
 
+def rank_specs(workload, rank, precision=None):
+    """the workload of one rank: replicas only (no system spans GPUs), so
+    every rank runs its own full copy of the workload with its own seeds;
+    rank 0 has the workload's canonical seeds"""
+    from simulationcode_gb300 import workloads as W
+    import inspect
+    fn = W.WORKLOADS[workload]
+    kw = {} if precision is None else {"precision": precision}
+    if rank:
+        kw["seed"] = inspect.signature(fn).parameters["seed"].default + 7919 * rank
+    return fn(**kw)
+
+
 def dist_env():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -56,11 +69,17 @@ class Dist:
             self.dist.barrier()
 
     def max(self, x):
+        return self._reduce(x, "MAX")
+
+    def sum(self, x):
+        return self._reduce(x, "SUM")
+
+    def _reduce(self, x, op):
         if self.ws == 1:
             return x
         import torch
         t = torch.tensor([float(x)], dtype=torch.float64)
-        self.dist.all_reduce(t, op=self.dist.ReduceOp.MAX)
+        self.dist.all_reduce(t, op=getattr(self.dist.ReduceOp, op))
         return float(t.item())
 
     def close(self):
@@ -437,7 +456,7 @@ def run_gpu(args, dist):
     lib = _lib.load()
     device = dist.local
     prec = {"fp64": _lib.FP64, "fp32": _lib.FP32_SPLIT}[args.precision] if args.precision else None
-    specs = W.WORKLOADS[args.workload]() if prec is None else W.WORKLOADS[args.workload](precision=prec)
+    specs = rank_specs(args.workload, dist.rank, prec)
     # set-up: relax random starts on the GPU (not timed)
     if any(s.potential == _lib.POT_BERTHIER for s in specs) and args.relax_steps > 0:
         rel = relax_specs(specs, device, steps=args.relax_steps)
@@ -474,7 +493,8 @@ def run_gpu(args, dist):
     clk = clocks.stop()
     ms = dist.max(ms)
     n = sum(s.N for s in specs)
-    value = n * args.steps / (ms / 1000.0)
+    n_all = dist.sum(n)           # particles of every rank (replicas only)
+    value = n_all * args.steps / (ms / 1000.0)
     st_after = [batch.stats(i) for i in ids]
     rebuilds = sum(b.rebuilds - a.rebuilds for a, b in zip(st_before, st_after))
 
@@ -535,7 +555,7 @@ def run_gpu(args, dist):
         for a in [r, v, D, F] + outs:
             lib.simmd_host_unregister(C.c_void_p(a.ctypes.data))
     e2e_steps = max(e2e_steps, 1)
-    e2e = {"value": n * e2e_steps / e2e_s, "unit": "particle-steps/s",
+    e2e = {"value": n_all * e2e_steps / e2e_s, "unit": "particle-steps/s",
            "h2d_bytes_per_step": h2d / e2e_steps, "d2h_bytes_per_step": d2h / e2e_steps,
            "what": "simmd_upload_r (r, v, D from page-locked host) + simmd_step(K) + simmd_download_r (r, v, F) "
                    "for every replica, wall clock"}
@@ -547,7 +567,8 @@ def run_gpu(args, dist):
     line = {"metric": "particle-steps/s", "value": value, "unit": "particle-steps/s", "n_gpus": dist.ws,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": dtype, "data": "synthetic",
-            "config": {"workload": args.workload, "description": W.DESCRIPTIONS[args.workload], "particles": n,
+            "config": {"workload": args.workload, "description": W.DESCRIPTIONS[args.workload],
+                       "particles": int(n_all), "particles_per_rank": n,
                        "replicas": len(specs), "threads_per_particle": args.tpp,
                        "l2": ("state larger than L2 (%.0f MB streamed per step)" % (step_bytes / 1e6))
                              if step_bytes > 129e6 else "state fits in L2 (%.0f MB; no flush)" % (step_bytes / 1e6),

@@ -177,6 +177,13 @@ __device__ __forceinline__ unsigned list_entry(const Batch& b, const unsigned* s
     return __ldg(b.s.nbr + nbr_addr(n, i, T, b.K)) & IDX_MASK;
 }
 
+// neighbour records gathered PAIR_UNROLL at a time (all loads issued before
+// the arithmetic); the pairs are still summed in list order
+#ifndef SIMMD_PAIR_UNROLL
+#define SIMMD_PAIR_UNROLL 2
+#endif
+constexpr int PAIR_UNROLL = SIMMD_PAIR_UNROLL;
+
 template <int DIM, int POT, bool EN, int T>
 __device__ __forceinline__ void pairs_f32(const Batch& b, const RepDesc& d, long long i, int sub,
                                           const float4 oi, const float4 gi, int cnt, float& fx, float& fy,
@@ -184,17 +191,20 @@ __device__ __forceinline__ void pairs_f32(const Batch& b, const RepDesc& d, long
 {
     const SplitRec* __restrict__ rec = b.s.rec;
     int n = sub;
-    for (; n + T < cnt; n += 2 * T) {
-        const unsigned j0 = list_entry<T>(b, s_rows, nrows, i, p, n);
-        const unsigned j1 = list_entry<T>(b, s_rows, nrows, i, p, n + T);
-        const float4 o0 = __ldg(&rec[j0].o);
-        const float4 g0 = __ldg(&rec[j0].g);
-        const float4 o1 = __ldg(&rec[j1].o);
-        const float4 g1 = __ldg(&rec[j1].g);
-        pair_f32<DIM, POT, EN>(d, oi, gi, o0, g0, fx, fy, fz, e, w);
-        pair_f32<DIM, POT, EN>(d, oi, gi, o1, g1, fx, fy, fz, e, w);
+    for (; n + (PAIR_UNROLL - 1) * T < cnt; n += PAIR_UNROLL * T) {
+        unsigned j[PAIR_UNROLL];
+        float4 o[PAIR_UNROLL], g[PAIR_UNROLL];
+#pragma unroll
+        for (int u = 0; u < PAIR_UNROLL; u++) j[u] = list_entry<T>(b, s_rows, nrows, i, p, n + u * T);
+#pragma unroll
+        for (int u = 0; u < PAIR_UNROLL; u++) {
+            o[u] = __ldg(&rec[j[u]].o);
+            g[u] = __ldg(&rec[j[u]].g);
+        }
+#pragma unroll
+        for (int u = 0; u < PAIR_UNROLL; u++) pair_f32<DIM, POT, EN>(d, oi, gi, o[u], g[u], fx, fy, fz, e, w);
     }
-    if (n < cnt) {
+    for (; n < cnt; n += T) {
         const unsigned j0 = list_entry<T>(b, s_rows, nrows, i, p, n);
         pair_f32<DIM, POT, EN>(d, oi, gi, __ldg(&rec[j0].o), __ldg(&rec[j0].g), fx, fy, fz, e, w);
     }
@@ -265,7 +275,10 @@ __device__ __forceinline__ void particle_pairs_f32(const Batch& b, const RepDesc
 
 // rows of the tile's list staged in shared memory (16-byte loads, all rows
 // issued at once): the pair loop then waits only on the record gathers
-constexpr int STAGE_WORDS = 6144;  // 24 KB of list entries per block
+#ifndef SIMMD_STAGE_WORDS
+#define SIMMD_STAGE_WORDS 6144
+#endif
+constexpr int STAGE_WORDS = SIMMD_STAGE_WORDS;  // list entries staged per block (24 KB)
 
 template <int T>
 __device__ __forceinline__ int stage_rows(const Batch& b, int t, int maxcnt, unsigned* s_rows)
@@ -319,7 +332,10 @@ __device__ __forceinline__ void finish_replica(const RepDesc& d, RepState& st, c
 }
 
 template <int MODE, int PREC, int T>
-__global__ void __launch_bounds__(TILE * T, (PREC == PREC_FP32 ? 8 : 4) / T) k_force(Batch b, double* epp)
+#ifndef SIMMD_F32_MINB
+#define SIMMD_F32_MINB 8
+#endif
+__global__ void __launch_bounds__(TILE * T, (PREC == PREC_FP32 ? SIMMD_F32_MINB : 4) / T) k_force(Batch b, double* epp)
 {
     constexpr bool EN = (MODE == FMODE_ENERGY || MODE == FMODE_STEP_ENERGY);
     constexpr bool STEP = (MODE == FMODE_STEP || MODE == FMODE_STEP_ENERGY);
@@ -328,7 +344,7 @@ __global__ void __launch_bounds__(TILE * T, (PREC == PREC_FP32 ? 8 : 4) / T) k_f
     __shared__ int s_flag;
     __shared__ int s_maxcnt;
     __shared__ double s_part[32 * NV];
-    __shared__ __align__(16) unsigned s_rows[PREC == PREC_FP32 ? STAGE_WORDS : 4];
+    __shared__ __align__(16) unsigned s_rows[(PREC == PREC_FP32 && STAGE_WORDS >= 4) ? STAGE_WORDS : 4];
     const int tid = threadIdx.x;
     const int p = tid / T, sub = tid - p * T;
     for (;;) {
