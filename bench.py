@@ -620,7 +620,7 @@ def main():
     ap.add_argument("--skin", type=float, default=None, help="override the workload's skin (without autotuning)")
     ap.add_argument("--no-autotune", dest="autotune", action="store_false",
                     help="skip the autotuner (threads per particle, skin / rebuild cadence)")
-    ap.add_argument("--tune-skins", default="0.3,0.4,0.5",
+    ap.add_argument("--tune-skins", default="0.3,0.4,0.5,0.6,0.7",
                     help="skins the autotuner may choose from (the rebuild cadence); empty: keep the configured skin")
     ap.add_argument("--serve-seconds", type=float, default=30.0,
                     help="arrival window of the serving run (0: no serving run)")

@@ -14,6 +14,8 @@ import dataclasses
 import itertools
 from typing import Iterable, Optional
 
+import numpy as np
+
 from .batch import ReplicaBatch
 
 
@@ -26,14 +28,35 @@ class TuneResult:
     trials: list
 
 
+def _may_overflow(batch: ReplicaBatch, skin: float, skin_seen: float, margin: float = 1.15) -> bool:
+    """True if a replica's longest list, scaled from the longest seen so far
+    (at skins up to ``skin_seen``) by the Verlet-sphere volume, could pass its
+    max_neighbors at ``skin``"""
+    for rid, spec in batch.specs.items():
+        seen = batch.stats(rid).max_count
+        rcs = spec.verlet_force_cutoff * float(np.max(spec.D))
+        grow = ((rcs + skin) / (rcs + skin_seen)) ** spec.dims
+        if seen * grow * margin > spec.max_neighbors:
+            return True
+    return False
+
+
 def autotune(batch: ReplicaBatch, *, tpps: Iterable[int] = (1, 2, 4), skins: Optional[Iterable[float]] = None,
              graph_steps: Iterable[int] = (16,), warmup: int = 32, steps: int = 96, log=None) -> TuneResult:
-    """Grid search; ``skins`` None keeps the replicas' configured skin."""
+    """Grid search; ``skins`` None keeps the replicas' configured skin.  A
+    skin whose predicted longest list could overflow max_neighbors is
+    skipped (skins are tried in increasing order)."""
     base_skin = next(iter(batch.specs.values())).skin if batch.specs else 0.3
-    skins = [base_skin] if skins is None else list(skins)
+    skins = [base_skin] if skins is None else sorted(skins)
+    skin_seen = base_skin
     trials = []
     best = None
     for skin, tpp, gs in itertools.product(skins, tpps, graph_steps):
+        if skin > skin_seen and _may_overflow(batch, skin, skin_seen):
+            if log:
+                log("autotune: skin=%.2f skipped (lists could overflow max_neighbors)" % skin)
+            continue
+        skin_seen = max(skin_seen, skin)
         batch.set_skin(skin)
         batch.set_tuning(tpp, True, gs)
         batch.step(warmup)

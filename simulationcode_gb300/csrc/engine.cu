@@ -204,11 +204,11 @@ static int force_rebuild_all(simmd_ctx* c)
 }
 
 // device bytes of the capacity-sized arrays: per slot the state (posD 32,
-// v/F/u 72), the split record 32, cellc/orig/ncnt 12, rebuild scratch
-// (bin/rank/src 12, staged posD/v/F/orig 84), per-particle energy 8 and the
-// list 4K; per tile the partial sums, plan and owner; per cell count, start
-// and plan entry; per replica its descriptor and state
-constexpr long long SLOT_BYTES = 32 + 72 + 32 + 12 + 12 + 84 + 8;
+// v/F/u 72), the split record 32, cellc/orig/ncnt 12, the tile order 1,
+// rebuild scratch (bin/rank/src 12, staged posD/v/F/orig 84), per-particle
+// energy 8 and the list 4K; per tile the partial sums, plan and owner; per
+// cell count, start and plan entry; per replica its descriptor and state
+constexpr long long SLOT_BYTES = 32 + 72 + 32 + 12 + 1 + 12 + 84 + 8;
 constexpr long long TILE_BYTES = NPART * 8 + 4 + 4;
 constexpr long long CELL_BYTES = 4 + 4 + 8;
 
@@ -269,6 +269,7 @@ static int ensure_capacity(simmd_ctx* c, long long S_need, long long C_need, int
         TRY(grow_keep(c, &s.cellc, S_old, S_new));
         TRY(grow_keep(c, &s.orig, S_old, S_new));
         TRY(grow_keep(c, &s.ncnt, S_old, S_new));
+        TRY(grow_keep(c, &s.perm, S_old, S_new));
         TRY(grow_fresh(c, &s.bin_cell, S_old, S_new));
         TRY(grow_fresh(c, &s.bin_rank, S_old, S_new));
         TRY(grow_fresh(c, &s.src, S_old, S_new));
@@ -930,7 +931,7 @@ static void destroy_ctx(simmd_ctx* c)
     invalidate_graph(c);
     Slots& s = c->s;
     void* ptrs[] = {s.posD, s.vx, s.vy, s.vz, s.fx, s.fy, s.fz, s.ux, s.uy, s.uz, s.rec, s.cellc, s.orig, s.nbr,
-                    s.ncnt, s.bin_cell, s.bin_rank, s.src, s.t_posD, s.t_vx, s.t_vy, s.t_vz, s.t_fx, s.t_fy,
+                    s.ncnt, s.perm, s.bin_cell, s.bin_rank, s.src, s.t_posD, s.t_vx, s.t_vy, s.t_vz, s.t_fx, s.t_fy,
                     s.t_fz, s.t_orig, s.cell_count, s.cell_start, c->nbr_full, c->ncnt_full, c->epp, c->d_desc,
                     c->d_state, c->d_tile_rep, c->d_tile_part, c->d_queue, c->d_stage, c->d_noise,
                     c->d_plan_tiles, c->d_plan_cells, c->d_plan_cnt};
@@ -1421,6 +1422,7 @@ int simmd_relax(simmd_ctx* c, int64_t nsteps, double step_size, double max_disp)
         if (!c->reps[r].active) continue;
         RepState& st = c->h_state[r];
         st.fmean[0] = st.fmean[1] = st.fmean[2] = 0.0;
+        st.cfmean[0] = st.cfmean[1] = st.cfmean[2] = 0.0;
         st.vmean[0] = st.vmean[1] = st.vmean[2] = 0.0;
         st.vscale = 1.0;
         st.nonfinite = 0;

@@ -276,9 +276,9 @@ __device__ __forceinline__ void particle_pairs_f32(const Batch& b, const RepDesc
 // rows of the tile's list staged in shared memory (16-byte loads, all rows
 // issued at once): the pair loop then waits only on the record gathers
 #ifndef SIMMD_STAGE_WORDS
-#define SIMMD_STAGE_WORDS 6144
+#define SIMMD_STAGE_WORDS 2048
 #endif
-constexpr int STAGE_WORDS = SIMMD_STAGE_WORDS;  // list entries staged per block (24 KB)
+constexpr int STAGE_WORDS = SIMMD_STAGE_WORDS;  // list entries staged per block (8 KB)
 
 template <int T>
 __device__ __forceinline__ int stage_rows(const Batch& b, int t, int maxcnt, unsigned* s_rows)
@@ -320,6 +320,8 @@ __device__ __forceinline__ void finish_replica(const RepDesc& d, RepState& st, c
         m[0] = ddiv(out[0], nd);
         m[1] = ddiv(out[1], nd);
         m[2] = ddiv(out[2], nd);
+        if (d.dyn == DYN_BROWNIAN)
+            for (int k = 0; k < 3; k++) st.cfmean[k] = -(d.dt_over_gamma * m[k]);
     }
     if (EN) {
         st.epot = out[NV - 2] / 2.0;
@@ -332,6 +334,9 @@ __device__ __forceinline__ void finish_replica(const RepDesc& d, RepState& st, c
 }
 
 template <int MODE, int PREC, int T>
+#ifndef SIMMD_TILE_ORDER
+#define SIMMD_TILE_ORDER 1
+#endif
 #ifndef SIMMD_F32_MINB
 #define SIMMD_F32_MINB 8
 #endif
@@ -346,7 +351,7 @@ __global__ void __launch_bounds__(TILE * T, (PREC == PREC_FP32 ? SIMMD_F32_MINB 
     __shared__ double s_part[32 * NV];
     __shared__ __align__(16) unsigned s_rows[(PREC == PREC_FP32 && STAGE_WORDS >= 4) ? STAGE_WORDS : 4];
     const int tid = threadIdx.x;
-    const int p = tid / T, sub = tid - p * T;
+    const int p0 = tid / T, sub = tid - p0 * T;
     for (;;) {
         if (tid == 0) s_tile = atomicAdd(&b.queue[0], 1);
         __syncthreads();
@@ -358,6 +363,10 @@ __global__ void __launch_bounds__(TILE * T, (PREC == PREC_FP32 ? SIMMD_F32_MINB 
         const RepDesc& d = b.desc[r];
         if (d.prec != PREC) continue;  // the other precision's launch handles this tile
         RepState& st = b.state[r];
+        // split precision: the threads take the tile's particles in the
+        // rebuild's tile order (longest lists first), so the lanes of a warp
+        // have similar trip counts; FP64: slot order
+        const int p = (PREC == PREC_FP32 && SIMMD_TILE_ORDER) ? (int)b.s.perm[(size_t)t * TILE + p0] : p0;
         const long long i = (long long)t * TILE + p;
         const bool real = i < d.slot0 + d.n;
         const bool noise = d.dyn != DYN_NEWTONIAN && MODE != FMODE_ENERGY && d.relax_cap == 0.0;

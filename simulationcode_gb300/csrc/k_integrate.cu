@@ -163,9 +163,9 @@ __global__ void k_brownian_update(Batch b)
                 dry = dmul(c, dsub(S.fy[i], st.fmean[1]));
                 if (d.dims == 3) drz = dmul(c, dsub(S.fz[i], st.fmean[2]));
             } else {
-                drx = fma(c, S.fx[i], -c * st.fmean[0]);
-                dry = fma(c, S.fy[i], -c * st.fmean[1]);
-                if (d.dims == 3) drz = fma(c, S.fz[i], -c * st.fmean[2]);
+                drx = fma(c, S.fx[i], st.cfmean[0]);
+                dry = fma(c, S.fy[i], st.cfmean[1]);
+                if (d.dims == 3) drz = fma(c, S.fz[i], st.cfmean[2]);
             }
             if (d.relax_cap > 0.0) {  // set-up relaxation: |dr| <= relax_cap per particle
                 double m = fmax(fabs(drx), fmax(fabs(dry), fabs(drz)));

@@ -74,6 +74,7 @@ struct RepState {
     long long list_entries;       // total list length at the last rebuild
     double vmean[3];              // pending centre-of-mass velocity (Newtonian/Langevin)
     double fmean[3];              // mean force (Brownian)
+    double cfmean[3];             // -(dt/gamma) * fmean (split-precision position update)
     double vscale;                // pending velocity rescale factor
     double epot, virial, ekin;
     double fmax;
@@ -96,6 +97,7 @@ struct Slots {
     int* orig;                    // original id, -1 for padding
     unsigned* nbr;                // ELL neighbour list
     int* ncnt;                    // neighbours per slot
+    unsigned char* perm;          // per tile: particle positions by descending list length
     // rebuild scratch
     int* bin_cell;
     int* bin_rank;
