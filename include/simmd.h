@@ -175,6 +175,13 @@ int simmd_upload_r(simmd_ctx* ctx, int32_t rep, const double* r, const double* v
 int simmd_download_r(simmd_ctx* ctx, int32_t rep, double* r, double* v, double* F, double* disp);
 int simmd_set_state_r(simmd_ctx* ctx, int32_t rep, const double* r, const double* v, const double* F,
                       const double* disp);
+/* asynchronous dump feed for save_data (src/Dump.jl:60-88): the replica's
+   r, v, F (any may be NULL) as of this point of the step sequence are copied
+   to the host on a side stream while later steps run (host arrays
+   page-locked, see simmd_host_register, for the copy to overlap); one dump
+   in flight per context; simmd_dump_wait returns once it has landed */
+int simmd_dump_async(simmd_ctx* ctx, int32_t rep, double* r, double* v, double* F);
+int simmd_dump_wait(simmd_ctx* ctx);
 /* energies of every replica (one pass), then per replica */
 int simmd_energy_all(simmd_ctx* ctx);
 int simmd_stats_r(simmd_ctx* ctx, int32_t rep, simmd_stats* out);

@@ -96,6 +96,8 @@ SIGNATURES = {
     "simmd_kernel_counts": (C.c_int, [_vp, _P(C.c_int64), _P(C.c_int64)]),
     "simmd_device_bytes": (C.c_int64, [_vp]),
     "simmd_set_budget": (C.c_int, [_vp, C.c_int64]),
+    "simmd_dump_async": (C.c_int, [_vp, C.c_int32, _vp, _vp, _vp]),
+    "simmd_dump_wait": (C.c_int, [_vp]),
     "simmd_time_force": (C.c_int, [_vp, C.c_int32, _P(C.c_float)]),
     "simmd_set_profile": (C.c_int, [_vp, C.c_int32]),
     "simmd_relax": (C.c_int, [_vp, C.c_int64, C.c_double, C.c_double]),

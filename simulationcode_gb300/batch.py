@@ -114,6 +114,27 @@ class ReplicaBatch:
         _lib.check(self.lib.simmd_download_r(self.ctx, rid, _lib.ptr(r), _lib.ptr(v), _lib.ptr(F), None))
         return r, v, F
 
+    def dump_async(self, rid: int, r: np.ndarray, v: Optional[np.ndarray] = None, F: Optional[np.ndarray] = None):
+        """queue a copy of the replica's current r (v, F) into the given
+        float64 arrays (shape (N, dims), C order; page-locked with
+        host_register for the copy to overlap later steps)"""
+        s = self.specs[rid]
+        for a in (r, v, F):
+            if a is not None and (a.dtype != np.float64 or a.shape != (s.N, s.dims) or not a.flags.c_contiguous):
+                raise ValueError("dump arrays must be C-contiguous float64 of shape (N, dims)")
+        self._dump_refs = (r, v, F)   # keep them alive until the wait
+        _lib.check(self.lib.simmd_dump_async(self.ctx, rid, _lib.ptr(r), _lib.ptr(v), _lib.ptr(F)))
+
+    def dump_wait(self):
+        _lib.check(self.lib.simmd_dump_wait(self.ctx))
+        self._dump_refs = None
+
+    def host_register(self, a: np.ndarray):
+        _lib.check(self.lib.simmd_host_register(C.c_void_p(a.ctypes.data), a.nbytes))
+
+    def host_unregister(self, a: np.ndarray):
+        _lib.check(self.lib.simmd_host_unregister(C.c_void_p(a.ctypes.data)))
+
     def energies(self):
         _lib.check(self.lib.simmd_energy_all(self.ctx))
         return {rid: self.stats(rid) for rid in self.specs}

@@ -117,6 +117,12 @@ struct simmd_ctx {
     std::vector<RepState> h_state;
     double* d_stage = nullptr;  // AoS staging, 5 arrays of stage_cap doubles
     long long stage_cap = 0;
+    // asynchronous dump feed: its own staging (r, v, F), side stream, events
+    double* d_dump = nullptr;
+    long long dump_cap = 0;
+    cudaStream_t dump_stream = nullptr;
+    cudaEvent_t ev_dump_ready = nullptr, ev_dump_done = nullptr;
+    bool dump_pending = false;
     double* d_noise = nullptr;
     long long noise_cap = 0;
     long long bytes = 0;
@@ -911,6 +917,12 @@ int simmd_engine_create(int32_t device, simmd_ctx** out)
         return set_err(SIMMD_ERR_CUDA, "stream/event creation failed");
     }
     for (auto& e : c->pev) cudaEventCreate(&e);
+    if (cudaStreamCreateWithFlags(&c->dump_stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->ev_dump_ready, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->ev_dump_done, cudaEventDisableTiming) != cudaSuccess) {
+        delete c;
+        return set_err(SIMMD_ERR_CUDA, "dump stream/event creation failed");
+    }
     int st = dalloc(c, &c->d_queue, 4);
     if (st == SIMMD_OK) st = cudaMemsetAsync(c->d_queue, 0, 4 * sizeof(int), c->stream) == cudaSuccess ? 0 : SIMMD_ERR_CUDA;
     if (st == SIMMD_OK) st = dalloc(c, &c->d_plan_cnt, 4);
@@ -933,12 +945,16 @@ static void destroy_ctx(simmd_ctx* c)
     void* ptrs[] = {s.posD, s.vx, s.vy, s.vz, s.fx, s.fy, s.fz, s.ux, s.uy, s.uz, s.rec, s.cellc, s.orig, s.nbr,
                     s.ncnt, s.perm, s.bin_cell, s.bin_rank, s.src, s.t_posD, s.t_vx, s.t_vy, s.t_vz, s.t_fx, s.t_fy,
                     s.t_fz, s.t_orig, s.cell_count, s.cell_start, c->nbr_full, c->ncnt_full, c->epp, c->d_desc,
-                    c->d_state, c->d_tile_rep, c->d_tile_part, c->d_queue, c->d_stage, c->d_noise,
+                    c->d_state, c->d_tile_rep, c->d_tile_part, c->d_queue, c->d_stage, c->d_dump, c->d_noise,
                     c->d_plan_tiles, c->d_plan_cells, c->d_plan_cnt};
     for (void* p : ptrs)
         if (p) cudaFree(p);
+    if (c->dump_stream) cudaStreamSynchronize(c->dump_stream);
     cudaEventDestroy(c->ev0);
     cudaEventDestroy(c->ev1);
+    if (c->ev_dump_ready) cudaEventDestroy(c->ev_dump_ready);
+    if (c->ev_dump_done) cudaEventDestroy(c->ev_dump_done);
+    if (c->dump_stream) cudaStreamDestroy(c->dump_stream);
     for (auto& e : c->pev) cudaEventDestroy(e);
     cudaStreamDestroy(c->stream);
     delete c;
@@ -1038,6 +1054,55 @@ int simmd_download_r(simmd_ctx* c, int32_t rep, double* r, double* v, double* F,
     if (F) CK(cudaMemcpyAsync(F, dF, sizeof(double) * nd, cudaMemcpyDeviceToHost, c->stream));
     if (disp) CK(cudaMemcpyAsync(disp, du, sizeof(double) * nd, cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
+    return SIMMD_OK;
+}
+
+// save_data's copy (src/Dump.jl:60-88) off the critical path: the state is
+// converted to the host layout on the context stream (so it is the state at
+// this point of the step sequence), then copied to the host on a side
+// stream while later steps run.  Host arrays should be page-locked
+// (simmd_host_register) for the copy to overlap.  One dump is in flight at
+// a time: the next dump's conversion waits (on the device) for the previous
+// copies; simmd_dump_wait blocks until the last dump's copies are done.
+int simmd_dump_async(simmd_ctx* c, int32_t rep, double* r, double* v, double* F)
+{
+    if (!c) return set_err(SIMMD_ERR_BAD_ARG, "NULL context");
+    CK(cudaSetDevice(c->device));
+    if (rep < 0 || rep >= c->R_cap || !c->reps[rep].active) return set_err(SIMMD_ERR_NOT_FOUND, "no such replica");
+    HostRep& h = c->reps[rep];
+    const long long nd = h.p.N * h.p.dims;
+    if (nd > c->dump_cap) {
+        CK(cudaStreamSynchronize(c->dump_stream));
+        CK(cudaStreamSynchronize(c->stream));
+        dfree(c, &c->d_dump, (size_t)(3 * c->dump_cap));
+        long long cap = std::max(nd, c->dump_cap * 2);
+        TRY(dalloc(c, &c->d_dump, (size_t)(3 * cap)));
+        c->dump_cap = cap;
+        c->dump_pending = false;
+    }
+    double *dr = c->d_dump, *dv = c->d_dump + c->dump_cap, *dF = c->d_dump + 2 * c->dump_cap;
+    if (c->dump_pending) CK(cudaStreamWaitEvent(c->stream, c->ev_dump_done, 0));
+    Batch b = make_batch(c);
+    LaunchCfg lc = make_lc(c, FMODE_STEP);
+    launch_store_aos_impl(b, lc, rep, h.d, r ? dr : nullptr, v ? dv : nullptr, F ? dF : nullptr, nullptr, nullptr,
+                          nullptr);
+    CK(cudaGetLastError());
+    CK(cudaEventRecord(c->ev_dump_ready, c->stream));
+    CK(cudaStreamWaitEvent(c->dump_stream, c->ev_dump_ready, 0));
+    if (r) CK(cudaMemcpyAsync(r, dr, sizeof(double) * nd, cudaMemcpyDeviceToHost, c->dump_stream));
+    if (v) CK(cudaMemcpyAsync(v, dv, sizeof(double) * nd, cudaMemcpyDeviceToHost, c->dump_stream));
+    if (F) CK(cudaMemcpyAsync(F, dF, sizeof(double) * nd, cudaMemcpyDeviceToHost, c->dump_stream));
+    CK(cudaEventRecord(c->ev_dump_done, c->dump_stream));
+    c->dump_pending = true;
+    return SIMMD_OK;
+}
+
+int simmd_dump_wait(simmd_ctx* c)
+{
+    if (!c) return set_err(SIMMD_ERR_BAD_ARG, "NULL context");
+    CK(cudaSetDevice(c->device));
+    if (c->dump_pending) CK(cudaEventSynchronize(c->ev_dump_done));
+    c->dump_pending = false;
     return SIMMD_OK;
 }
 
