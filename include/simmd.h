@@ -54,7 +54,8 @@ enum simmd_status {
     SIMMD_ERR_NOISE_RANGE = 6,        /* host noise array shorter than the steps taken */
     SIMMD_ERR_BUDGET = 7,             /* replica does not fit the memory budget / capacity */
     SIMMD_ERR_NOT_FOUND = 8,          /* unknown replica id */
-    SIMMD_ERR_NO_DEVICE = 9           /* no CUDA device */
+    SIMMD_ERR_NO_DEVICE = 9,          /* no CUDA device */
+    SIMMD_ERR_NOT_CONVERGED = 10      /* minimiser reached max_iterations */
 };
 
 enum { SIMMD_POT_LJ = 0, SIMMD_POT_BERTHIER = 1 };
@@ -175,6 +176,17 @@ int simmd_upload_r(simmd_ctx* ctx, int32_t rep, const double* r, const double* v
 int simmd_download_r(simmd_ctx* ctx, int32_t rep, double* r, double* v, double* F, double* disp);
 int simmd_set_state_r(simmd_ctx* ctx, int32_t rep, const double* r, const double* v, const double* F,
                       const double* disp);
+/* find_inherent_structure (src/InherentStructure.jl:5-56) for every replica
+   of the context, in FP64 with the reference's arithmetic: steepest descent
+   v = F*dt, scaled so that max_i |v_i| <= max_step_size, drift with wrap
+   and displacement, rebuild on the skin trigger, until max_i |F_i| <=
+   tolerance (after that iteration's move).  Pair forces only.  iterations
+   (optional) receives each replica's iteration count, indexed by replica id.
+   Returns SIMMD_ERR_NOT_CONVERGED if a replica reached max_iterations.
+   Velocities are left unchanged (the reference reuses v_array as the step
+   buffer). */
+int simmd_inherent_structure(simmd_ctx* ctx, double tolerance, int64_t max_iterations, double max_step_size,
+                             double dt, int64_t* iterations);
 /* asynchronous dump feed for save_data (src/Dump.jl:60-88): the replica's
    r, v, F (any may be NULL) as of this point of the step sequence are copied
    to the host on a side stream while later steps run (host arrays

@@ -16,7 +16,7 @@ LIB_PATH = os.path.join(HERE, "_lib", "libsimmd.so")
 
 OK = 0
 ERR_BAD_ARG, ERR_CUDA, ERR_OOM, ERR_NEIGHBOR_OVERFLOW, ERR_NONFINITE = 1, 2, 3, 4, 5
-ERR_NOISE_RANGE, ERR_BUDGET, ERR_NOT_FOUND, ERR_NO_DEVICE = 6, 7, 8, 9
+ERR_NOISE_RANGE, ERR_BUDGET, ERR_NOT_FOUND, ERR_NO_DEVICE, ERR_NOT_CONVERGED = 6, 7, 8, 9, 10
 
 POT_LJ, POT_BERTHIER = 0, 1
 NEWTONIAN, LANGEVIN, BROWNIAN = 0, 1, 2
@@ -98,6 +98,7 @@ SIGNATURES = {
     "simmd_set_budget": (C.c_int, [_vp, C.c_int64]),
     "simmd_dump_async": (C.c_int, [_vp, C.c_int32, _vp, _vp, _vp]),
     "simmd_dump_wait": (C.c_int, [_vp]),
+    "simmd_inherent_structure": (C.c_int, [_vp, C.c_double, C.c_int64, C.c_double, C.c_double, _P(C.c_int64)]),
     "simmd_time_force": (C.c_int, [_vp, C.c_int32, _P(C.c_float)]),
     "simmd_set_profile": (C.c_int, [_vp, C.c_int32]),
     "simmd_relax": (C.c_int, [_vp, C.c_int64, C.c_double, C.c_double]),

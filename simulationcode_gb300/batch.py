@@ -99,6 +99,15 @@ class ReplicaBatch:
         """capped steepest descent r += step_size*F, |dr| <= max_disp (set-up)"""
         _lib.check(self.lib.simmd_relax(self.ctx, nsteps, step_size, max_disp))
 
+    def inherent_structure(self, tolerance=1e-6, max_iterations=10 ** 6, max_step_size=0.001, dt=0.005):
+        """minimise every replica (find_inherent_structure); returns
+        {replica id: iterations}"""
+        n = max(self.specs) + 1 if self.specs else 1
+        it = (C.c_int64 * n)()
+        _lib.check(self.lib.simmd_inherent_structure(self.ctx, float(tolerance), int(max_iterations),
+                                                     float(max_step_size), float(dt), it))
+        return {rid: int(it[rid]) for rid in self.specs}
+
     def step(self, nsteps: int):
         _lib.check(self.lib.simmd_step(self.ctx, int(nsteps), None))
 

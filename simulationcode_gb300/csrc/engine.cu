@@ -39,6 +39,8 @@ void launch_kinetic_impl(const Batch& b, const LaunchCfg& lc);
 void launch_finalize_impl(const Batch& b, const LaunchCfg& lc);
 void launch_load_aos_impl(const Batch& b, const LaunchCfg& lc, int rep, const RepDesc& hd, const double* r,
                           const double* v, const double* F, const double* D, const double* disp);
+void launch_min_iteration_impl(const Batch& b, const LaunchCfg& lc, double dt, double max_step, double tol,
+                               long long max_iters);
 void launch_store_aos_impl(const Batch& b, const LaunchCfg& lc, int rep, const RepDesc& hd, double* r,
                            double* v, double* F, double* disp, const double* epp_src, double* epp);
 void launch_set_state_impl(const Batch& b, const LaunchCfg& lc, int rep, const RepDesc& hd, const double* r,
@@ -210,11 +212,11 @@ static int force_rebuild_all(simmd_ctx* c)
 }
 
 // device bytes of the capacity-sized arrays: per slot the state (posD 32,
-// v/F/u 72), the split record 32, cellc/orig/ncnt 12, the tile order 1,
-// rebuild scratch (bin/rank/src 12, staged posD/v/F/orig 84), per-particle
-// energy 8 and the list 4K; per tile the partial sums, plan and owner; per
-// cell count, start and plan entry; per replica its descriptor and state
-constexpr long long SLOT_BYTES = 32 + 72 + 32 + 12 + 1 + 12 + 84 + 8;
+// v/F/u 72), the split record 32, cellc/orig/ncnt 12, rebuild scratch
+// (bin/rank/src 12, staged posD/v/F/orig 84), per-particle energy 8 and the
+// list 4K; per tile the partial sums, plan and owner; per cell count, start
+// and plan entry; per replica its descriptor and state
+constexpr long long SLOT_BYTES = 32 + 72 + 32 + 12 + 12 + 84 + 8;
 constexpr long long TILE_BYTES = NPART * 8 + 4 + 4;
 constexpr long long CELL_BYTES = 4 + 4 + 8;
 
@@ -275,7 +277,6 @@ static int ensure_capacity(simmd_ctx* c, long long S_need, long long C_need, int
         TRY(grow_keep(c, &s.cellc, S_old, S_new));
         TRY(grow_keep(c, &s.orig, S_old, S_new));
         TRY(grow_keep(c, &s.ncnt, S_old, S_new));
-        TRY(grow_keep(c, &s.perm, S_old, S_new));
         TRY(grow_fresh(c, &s.bin_cell, S_old, S_new));
         TRY(grow_fresh(c, &s.bin_rank, S_old, S_new));
         TRY(grow_fresh(c, &s.src, S_old, S_new));
@@ -879,6 +880,7 @@ const char* simmd_status_string(int status)
         case SIMMD_ERR_BUDGET: return "capacity or budget exceeded";
         case SIMMD_ERR_NOT_FOUND: return "replica not found";
         case SIMMD_ERR_NO_DEVICE: return "no CUDA device";
+        case SIMMD_ERR_NOT_CONVERGED: return "not converged";
         default: return "unknown status";
     }
 }
@@ -943,7 +945,7 @@ static void destroy_ctx(simmd_ctx* c)
     invalidate_graph(c);
     Slots& s = c->s;
     void* ptrs[] = {s.posD, s.vx, s.vy, s.vz, s.fx, s.fy, s.fz, s.ux, s.uy, s.uz, s.rec, s.cellc, s.orig, s.nbr,
-                    s.ncnt, s.perm, s.bin_cell, s.bin_rank, s.src, s.t_posD, s.t_vx, s.t_vy, s.t_vz, s.t_fx, s.t_fy,
+                    s.ncnt, s.bin_cell, s.bin_rank, s.src, s.t_posD, s.t_vx, s.t_vy, s.t_vz, s.t_fx, s.t_fy,
                     s.t_fz, s.t_orig, s.cell_count, s.cell_start, c->nbr_full, c->ncnt_full, c->epp, c->d_desc,
                     c->d_state, c->d_tile_rep, c->d_tile_part, c->d_queue, c->d_stage, c->d_dump, c->d_noise,
                     c->d_plan_tiles, c->d_plan_cells, c->d_plan_cnt};
@@ -1450,6 +1452,79 @@ int simmd_time_force(simmd_ctx* c, int32_t nrep, float* ms_per_launch)
     CK(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
     *ms_per_launch = ms / (float)nrep;
     return SIMMD_OK;
+}
+
+int simmd_inherent_structure(simmd_ctx* c, double tolerance, int64_t max_iterations, double max_step_size,
+                             double dt, int64_t* iterations)
+{
+    if (!c || !(tolerance > 0) || max_iterations < 1 || !(max_step_size > 0) || !(dt > 0))
+        return set_err(SIMMD_ERR_BAD_ARG, "bad argument");
+    CK(cudaSetDevice(c->device));
+    // every replica: pair forces only (a Newtonian system's random force is a
+    // no-op) in the reference's FP64 arithmetic; the lists are rebuilt first
+    // (src/InherentStructure.jl:9)
+    std::vector<RepDesc> saved;
+    for (int r = 0; r < c->R_cap; r++) {
+        saved.push_back(c->reps[r].d);
+        if (!c->reps[r].active) continue;
+        RepDesc& d = c->reps[r].d;
+        d.dyn = DYN_NEWTONIAN;
+        d.prec = PREC_FP64;
+        d.rescale = 0;
+        TRY(push_desc(c, r));
+        c->reps[r].pending_rebuild = true;
+    }
+    CK(cudaMemcpyAsync(c->h_state.data(), c->d_state, sizeof(RepState) * c->R_cap, cudaMemcpyDeviceToHost,
+                       c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    for (int r = 0; r < c->R_cap; r++) {
+        RepState& st = c->h_state[r];
+        st.min_active = c->reps[r].active ? 1 : 0;
+        st.min_done = 0;
+        st.min_iters = 0;
+        st.min_fmax = st.min_step = 0ull;
+    }
+    CK(cudaMemcpyAsync(c->d_state, c->h_state.data(), sizeof(RepState) * c->R_cap, cudaMemcpyHostToDevice,
+                       c->stream));
+    TRY(pending_rebuilds(c));
+    Batch b = make_batch(c);
+    LaunchCfg lc = make_lc(c, FMODE_FORCES);
+    int status = SIMMD_OK;
+    for (;;) {
+        for (int k = 0; k < 32; k++) {
+            launch_force_impl(b, lc, FMODE_FORCES, 1, nullptr);
+            c->n_force += 1;
+            launch_min_iteration_impl(b, lc, dt, max_step_size, tolerance, max_iterations);
+            rebuild_launch(c, b, lc);
+        }
+        CK(cudaGetLastError());
+        status = read_states(c);
+        bool all = true;
+        for (int r = 0; r < c->R_cap; r++)
+            if (c->reps[r].active && !c->h_state[r].min_done && !c->h_state[r].nonfinite) all = false;
+        if (all || status != SIMMD_OK) break;
+    }
+    for (int r = 0; r < c->R_cap; r++) {
+        if (!c->reps[r].active) continue;
+        if (iterations) iterations[r] = c->h_state[r].min_iters;
+        if (c->h_state[r].min_done == 2 && status == SIMMD_OK)
+            status = set_err(SIMMD_ERR_NOT_CONVERGED, "inherent structure: max_iterations reached");
+    }
+    // back to the replicas' own dynamics and precision
+    for (int r = 0; r < c->R_cap; r++) {
+        RepState& st = c->h_state[r];
+        st.min_active = st.min_done = 0;
+        st.min_fmax = st.min_step = 0ull;
+        st.fmean_pending = 0;
+        if (!c->reps[r].active) continue;
+        c->reps[r].d = saved[r];
+        TRY(push_desc(c, r));
+        c->reps[r].pending_rebuild = true;
+    }
+    CK(cudaMemcpyAsync(c->d_state, c->h_state.data(), sizeof(RepState) * c->R_cap, cudaMemcpyHostToDevice,
+                       c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return status;
 }
 
 int simmd_relax(simmd_ctx* c, int64_t nsteps, double step_size, double max_disp)

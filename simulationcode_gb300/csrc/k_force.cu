@@ -334,9 +334,6 @@ __device__ __forceinline__ void finish_replica(const RepDesc& d, RepState& st, c
 }
 
 template <int MODE, int PREC, int T>
-#ifndef SIMMD_TILE_ORDER
-#define SIMMD_TILE_ORDER 1
-#endif
 #ifndef SIMMD_F32_MINB
 #define SIMMD_F32_MINB 8
 #endif
@@ -351,7 +348,7 @@ __global__ void __launch_bounds__(TILE * T, (PREC == PREC_FP32 ? SIMMD_F32_MINB 
     __shared__ double s_part[32 * NV];
     __shared__ __align__(16) unsigned s_rows[(PREC == PREC_FP32 && STAGE_WORDS >= 4) ? STAGE_WORDS : 4];
     const int tid = threadIdx.x;
-    const int p0 = tid / T, sub = tid - p0 * T;
+    const int p = tid / T, sub = tid - p * T;
     for (;;) {
         if (tid == 0) s_tile = atomicAdd(&b.queue[0], 1);
         __syncthreads();
@@ -363,10 +360,7 @@ __global__ void __launch_bounds__(TILE * T, (PREC == PREC_FP32 ? SIMMD_F32_MINB 
         const RepDesc& d = b.desc[r];
         if (d.prec != PREC) continue;  // the other precision's launch handles this tile
         RepState& st = b.state[r];
-        // split precision: the threads take the tile's particles in the
-        // rebuild's tile order (longest lists first), so the lanes of a warp
-        // have similar trip counts; FP64: slot order
-        const int p = (PREC == PREC_FP32 && SIMMD_TILE_ORDER) ? (int)b.s.perm[(size_t)t * TILE + p0] : p0;
+        if (MODE == FMODE_FORCES && st.min_done) continue;  // minimiser: this replica has converged
         const long long i = (long long)t * TILE + p;
         const bool real = i < d.slot0 + d.n;
         const bool noise = d.dyn != DYN_NEWTONIAN && MODE != FMODE_ENERGY && d.relax_cap == 0.0;

@@ -191,6 +191,122 @@ __global__ void k_brownian_update(Batch b)
     }
 }
 
+// ---------------------------------------------------------------------------
+// inherent-structure minimiser (src/InherentStructure.jl:5-56)
+// ---------------------------------------------------------------------------
+__global__ void k_min_reset(Batch b)
+{
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= b.nreps) return;
+    RepState& st = b.state[r];
+    st.min_fmax = 0ull;
+    st.min_step = 0ull;
+}
+
+// max_i |F_i| and max_i |F_i dt| (stepsize before scaling), the reference's
+// rounding: v = F*dt, |v| = sqrt(v.v)
+__global__ void k_min_max(Batch b, double dt)
+{
+    for (int t = blockIdx.x; t < b.ntiles; t += gridDim.x) {
+        const int r = b.tile_rep[t];
+        if (r < 0) continue;
+        const RepDesc& d = b.desc[r];
+        RepState& st = b.state[r];
+        if (!st.min_active || st.min_done) continue;
+        const long long i = (long long)t * TILE + threadIdx.x;
+        double qf = 0.0, qs = 0.0;
+        if (i < d.slot0 + d.n) {
+            const Slots& S = b.s;
+            const double fx = S.fx[i], fy = S.fy[i], fz = d.dims == 3 ? S.fz[i] : 0.0;
+            double sf = dadd(dmul(fx, fx), dmul(fy, fy));
+            const double vx = dmul(fx, dt), vy = dmul(fy, dt), vz = dmul(fz, dt);
+            double sv = dadd(dmul(vx, vx), dmul(vy, vy));
+            if (d.dims == 3) {
+                sf = dadd(sf, dmul(fz, fz));
+                sv = dadd(sv, dmul(vz, vz));
+            }
+            qf = __dsqrt_rn(sf);
+            qs = __dsqrt_rn(sv);
+        }
+        unsigned long long bf = (unsigned long long)__double_as_longlong(qf);
+        unsigned long long bs = (unsigned long long)__double_as_longlong(qs);
+        if (!(qf == qf) || !(qs == qs)) {
+            st.nonfinite = 1;
+            bf = bs = 0x7ff0000000000000ull;
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const unsigned long long yf = __shfl_xor_sync(0xffffffffu, bf, o);
+            const unsigned long long ys = __shfl_xor_sync(0xffffffffu, bs, o);
+            bf = yf > bf ? yf : bf;
+            bs = ys > bs ? ys : bs;
+        }
+        if ((threadIdx.x & 31) == 0) {
+            atomicMax(&st.min_fmax, bf);
+            atomicMax(&st.min_step, bs);
+        }
+    }
+}
+
+// r += v with v = F*dt scaled by max_step/stepsize when stepsize >
+// max_step, wrap, displacement, skin max
+__global__ void k_min_drift(Batch b, double dt, double max_step)
+{
+    __shared__ unsigned long long s_max[TILE / 32];
+    for (int t = blockIdx.x; t < b.ntiles; t += gridDim.x) {
+        const int r = b.tile_rep[t];
+        if (r < 0) continue;
+        const RepDesc& d = b.desc[r];
+        RepState& st = b.state[r];
+        if (!st.min_active || st.min_done) continue;
+        const double stepsize = __longlong_as_double((long long)st.min_step);
+        const long long i = (long long)t * TILE + threadIdx.x;
+        double u2 = 0.0;
+        if (i < d.slot0 + d.n) {
+            const Slots& S = b.s;
+            double vx = dmul(S.fx[i], dt), vy = dmul(S.fy[i], dt), vz = d.dims == 3 ? dmul(S.fz[i], dt) : 0.0;
+            if (stepsize > max_step) {
+                const double sc = ddiv(max_step, stepsize);
+                vx = dmul(vx, sc);
+                vy = dmul(vy, sc);
+                vz = dmul(vz, sc);
+            }
+            u2 = drift_slot(b, d, i, vx, vy, vz);
+        }
+        block_max_to_state(u2, st, s_max);
+    }
+}
+
+// after the move: the iteration's error max(maxforce, stepsize) ends the
+// replica's minimisation when <= tol (one thread per replica, so every
+// kernel of an iteration sees the same flag)
+__global__ void k_min_decide(Batch b, double tol, long long max_iters)
+{
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= b.nreps) return;
+    RepState& st = b.state[r];
+    if (!b.desc[r].active || !st.min_active || st.min_done) return;
+    const double stepsize = __longlong_as_double((long long)st.min_step);
+    const double maxforce = __longlong_as_double((long long)st.min_fmax);
+    const long long it = st.min_iters + 1;
+    st.min_iters = it;
+    const double err = maxforce > stepsize ? maxforce : stepsize;
+    if (!(err > tol)) st.min_done = 1;
+    else if (it >= max_iters) st.min_done = 2;
+}
+
+// one iteration after the force pass: maxima, move, decision
+void launch_min_iteration_impl(const Batch& b, const LaunchCfg& lc, double dt, double max_step, double tol,
+                               long long max_iters)
+{
+    const int rb = (b.nreps + 127) / 128;
+    k_min_reset<<<rb, 128, 0, lc.stream>>>(b);
+    k_min_max<<<lc.grid_stream, TILE, 0, lc.stream>>>(b, dt);
+    k_min_drift<<<lc.grid_stream, TILE, 0, lc.stream>>>(b, dt, max_step);
+    k_min_decide<<<rb, 128, 0, lc.stream>>>(b, tol, max_iters);
+    if (lc.launches) *lc.launches += 4;
+}
+
 // kinetic energy of (v - vmean) with the pending COM removal applied, and
 // (rescale mode) the velocity rescale factor sqrt(kBT / kBT_current)
 template <bool RESCALE_ONLY>

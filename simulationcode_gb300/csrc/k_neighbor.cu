@@ -454,27 +454,6 @@ __global__ void __launch_bounds__(BLD_THREADS) k_rb_build(Batch b, unsigned* nbr
     }
 }
 
-// tile order for the split-precision force pass: the tile's particle
-// positions by descending list length (ties by position), so a warp takes
-// particles of similar trip counts; padding slots (no list) come last
-__global__ void k_rb_order(Batch b)
-{
-    __shared__ int keys[TILE];
-    const int ntask = plan_count(b, 0);
-    for (int k = blockIdx.x; k < ntask; k += gridDim.x) {
-        const int t = b.plan_tiles[k];
-        const long long s = (long long)t * TILE + threadIdx.x;
-        const int cnt = min(b.s.ncnt[s], 0xffff);
-        const int key = ((0xffff - cnt) << 7) | (int)threadIdx.x;
-        keys[threadIdx.x] = key;
-        __syncthreads();
-        int rank = 0;
-        for (int q = 0; q < TILE; q++) rank += (keys[q] < key) ? 1 : 0;
-        b.s.perm[(long long)t * TILE + rank] = (unsigned char)threadIdx.x;
-        __syncthreads();
-    }
-}
-
 // copy the staged (re-ordered) state back; separate kernel because the build
 // reads neighbours' staged positions
 __global__ void k_rb_copyback(Batch b)
@@ -522,10 +501,9 @@ void launch_rebuild_impl(const Batch& b, const LaunchCfg& lc, unsigned* nbr_full
     k_rb_cellsort<<<g, TILE, 0, lc.stream>>>(b);
     k_rb_gather<<<g, TILE, 0, lc.stream>>>(b, ncnt_full);
     k_rb_build<<<g, BLD_THREADS, 0, lc.stream>>>(b, nbr_full, ncnt_full, Kfull);
-    k_rb_order<<<g, TILE, 0, lc.stream>>>(b);
     k_rb_copyback<<<g, TILE, 0, lc.stream>>>(b);
     k_rb_done<<<(b.nreps + 127) / 128, 128, 0, lc.stream>>>(b);
-    if (lc.launches) *lc.launches += 10;
+    if (lc.launches) *lc.launches += 9;
 }
 
 // ---------------------------------------------------------------------------

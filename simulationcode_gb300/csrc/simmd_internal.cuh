@@ -78,6 +78,12 @@ struct RepState {
     double vscale;                // pending velocity rescale factor
     double epot, virial, ekin;
     double fmax;
+    // inherent-structure minimiser
+    unsigned long long min_fmax;  // bits of max_i |F_i| this iteration
+    unsigned long long min_step;  // bits of max_i |F_i dt| this iteration
+    long long min_iters;
+    int min_done;                 // 1 converged, 2 iteration limit
+    int min_active;               // replica takes part in the minimisation
 };
 
 // split-precision gather record (one 32-byte sector): FP32 offsets of the
@@ -97,7 +103,6 @@ struct Slots {
     int* orig;                    // original id, -1 for padding
     unsigned* nbr;                // ELL neighbour list
     int* ncnt;                    // neighbours per slot
-    unsigned char* perm;          // per tile: particle positions by descending list length
     // rebuild scratch
     int* bin_cell;
     int* bin_rank;

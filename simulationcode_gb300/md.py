@@ -202,6 +202,22 @@ def do_time_step(arrays, parameters, output, neighborlist: NeighborListStruct, s
     neighborlist._count_rebuilds(output)
 
 
+def find_inherent_structure(arrays, parameters, neighborlist: NeighborListStruct, tolerance=1e-6,
+                            max_iterations=10 ** 6, max_step_size=0.001, dt=0.005):
+    """find_inherent_structure (src/InherentStructure.jl:5-56): steepest
+    descent of the positions to the nearest local minimum on the device.
+    Returns the iteration count; raises if max_iterations is reached (the
+    reference's intent; its own error path raises a MethodError)."""
+    neighborlist._ensure(arrays, parameters)
+    neighborlist.push(arrays)
+    it = (C.c_int64 * 1)()
+    st = neighborlist._lib.simmd_inherent_structure(neighborlist.ctx, float(tolerance), int(max_iterations),
+                                                    float(max_step_size), float(dt), it)
+    neighborlist.pull(arrays)
+    _lib.check(st)
+    return int(it[0])
+
+
 def calculate_full_energy(arrays, parameters, neighborlist: NeighborListStruct):
     """calculate_full_energy (src/AuxiliaryFunctions.jl:22-34)."""
     neighborlist._ensure(arrays, parameters)
