@@ -406,34 +406,31 @@ def run_reference(args, dist):
     from oracle import build as ob, pyoracle as O
     ob.build_oracle()
     specs = W.WORKLOADS[args.workload](precision=0)
-    # the same seeded initial state; positions relaxed by the oracle's MC
-    # restatement of find_random_initial_configuration! (few sweeps)
+    # the same seeded initial state, relaxed as the GPU arm's set-up does
+    # (capped steepest descent, here the oracle's C routine), threads over
+    # replicas; the oracle releases the GIL inside its C calls
     systems = []
     for s in specs:
         p = O.make_params(s.dims, s.potential, s.dynamics, s.N, s.box_size, s.force_cutoff2, s.skin,
                           eps=s.lj_eps, sigma=s.lj_sigma, lj_rc=math.sqrt(s.force_cutoff2), zeta=s.b_zeta,
                           berthier_rc=math.sqrt(s.force_cutoff2), kBT=s.kBT, gamma=s.gamma, dt=s.dt, m=s.m)
-        r = s.r
-        if s.potential == O.POT_BERTHIER:
-            r, _ = O.random_initial_configuration(p, s.D, 3, max_disp=0.1, seed=s.seed, maxK=s.max_neighbors * 2,
-                                                  skin=0.6)
-        sysm = O.OracleSystem(p, r, s.D, v=s.v, force_cutoff=s.verlet_force_cutoff, maxK=s.max_neighbors * 2)
-        sysm.update_neighbor_lists()
+        sysm = O.OracleSystem(p, s.r, s.D, v=s.v, force_cutoff=s.verlet_force_cutoff, maxK=s.max_neighbors * 2)
         systems.append((s, sysm))
     cores = max(1, min(os.cpu_count() or 1, len(systems)))
     pool = ThreadPoolExecutor(cores)
-    step_no = [0]
 
-    def one_step():
-        k = step_no[0]
-        list(pool.map(lambda t: t[1].run(1, seed=t[0].seed, step0=k), systems))
-        step_no[0] += 1
+    def setup(t):
+        s, sysm = t
+        if s.potential == O.POT_BERTHIER and args.relax_steps > 0:
+            sysm.relax_capped(args.relax_steps, 1e-3, 0.05)
+        sysm.update_neighbor_lists()
 
-    for _ in range(args.warmup):
-        one_step()
+    list(pool.map(setup, systems))
+    # replicas are independent: each thread runs a replica's steps in one
+    # oracle call (Philox noise keyed by the step, as on the GPU)
+    list(pool.map(lambda t: t[1].run(args.warmup, seed=t[0].seed, step0=0), systems))
     t0 = time.perf_counter()
-    for _ in range(args.steps):
-        one_step()
+    list(pool.map(lambda t: t[1].run(args.steps, seed=t[0].seed, step0=args.warmup), systems))
     dt = time.perf_counter() - t0
     n = sum(s.N for s, _ in systems)
     value = n * args.steps / dt

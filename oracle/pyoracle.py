@@ -86,6 +86,7 @@ def lib():
                                                        C.c_uint64, _P_D]
         L.orc_find_inherent_structure.argtypes = [vp, vp, vp, vp, vp, vp, C.c_double, C.c_int64,
                                                   C.c_double, C.c_double, _P_I64]
+        L.orc_relax_capped.argtypes = [vp, vp, vp, vp, vp, C.c_int64, C.c_double, C.c_double]
         _lib = L
     return _lib
 
@@ -197,6 +198,13 @@ class OracleSystem:
             noise = np.ascontiguousarray(noise, dtype=np.float64)
         st = lib().orc_run_steps(C.byref(self.p), _ptr(self.r), _ptr(self.v), _ptr(self.F), _ptr(self.D),
                                  C.byref(self.nl), int(nsteps), _ptr(noise), int(seed), int(step0))
+        if st:
+            raise RuntimeError("oracle neighbor list overflow")
+
+    def relax_capped(self, steps, step_size=1e-3, max_disp=0.05):
+        """set-up only: capped steepest descent of the positions"""
+        st = lib().orc_relax_capped(C.byref(self.p), _ptr(self.r), _ptr(self.F), _ptr(self.D), C.byref(self.nl),
+                                    int(steps), float(step_size), float(max_disp))
         if st:
             raise RuntimeError("oracle neighbor list overflow")
 

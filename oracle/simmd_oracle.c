@@ -750,6 +750,38 @@ int orc_random_initial_configuration(const orc_params *p0, double *r, double *D,
     return status;
 }
 
+/* Set-up only, no counterpart in the reference: capped steepest descent of
+ * random starts, r += step_size*F with |dr_i| <= max_disp per particle, wrap,
+ * displacement, rebuild on the skin trigger (the benchmark relaxes its
+ * random initial positions this way; the reference uses MC at kBT = 10,
+ * too slow for millions of particles). */
+int orc_relax_capped(const orc_params *p, double *r, double *F, const double *D, orc_nlist *nl,
+                     int64_t steps, double step_size, double max_disp)
+{
+    const int d = p->dims;
+    const int64_t N = p->N;
+    int st = orc_update_neighbor_lists(p, r, D, nl);
+    for (int64_t it = 0; it < steps && !st; it++) {
+        orc_pair_forces_only(p, r, D, nl, F);
+        for (int64_t i = 0; i < N; i++) {
+            double dr[3] = {0.0, 0.0, 0.0};
+            double len2 = 0.0;
+            for (int k = 0; k < d; k++) {
+                dr[k] = step_size * F[d * i + k];
+                len2 += dr[k] * dr[k];
+            }
+            const double len = sqrt(len2);
+            if (!(len <= max_disp)) {
+                const double sc = (len > 0.0 && isfinite(len)) ? max_disp / len : 0.0;
+                for (int k = 0; k < d; k++) dr[k] *= sc;
+            }
+            drift_particle(p, i, dr, r, nl);
+        }
+        if (skin_exceeded(p, nl)) st = orc_update_neighbor_lists(p, r, D, nl);
+    }
+    return st;
+}
+
 /* find_inherent_structure, src/InherentStructure.jl:5-56 (steepest descent,
  * step v = F dt capped so that max |v| <= max_step_size).  Pair forces only
  * (the reference calls calculate_new_forces! with a Newtonian system, whose

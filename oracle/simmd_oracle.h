@@ -122,6 +122,8 @@ void orc_generate_diameters_berthier(int64_t N, double sigma_ratio, uint64_t see
 int orc_random_initial_configuration(const orc_params *p, double *r, double *D, orc_nlist *nl,
                                      int64_t steps, double max_disp, uint64_t seed,
                                      double *final_energy);
+int orc_relax_capped(const orc_params *p, double *r, double *F, const double *D, orc_nlist *nl,
+                     int64_t steps, double step_size, double max_disp);
 int orc_find_inherent_structure(const orc_params *p, double *r, double *v, double *F,
                                 const double *D, orc_nlist *nl, double tolerance,
                                 int64_t max_iterations, double max_step_size, double dt,

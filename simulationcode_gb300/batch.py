@@ -99,13 +99,17 @@ class ReplicaBatch:
         """capped steepest descent r += step_size*F, |dr| <= max_disp (set-up)"""
         _lib.check(self.lib.simmd_relax(self.ctx, nsteps, step_size, max_disp))
 
-    def inherent_structure(self, tolerance=1e-6, max_iterations=10 ** 6, max_step_size=0.001, dt=0.005):
+    def inherent_structure(self, tolerance=1e-6, max_iterations=10 ** 6, max_step_size=0.001, dt=0.005,
+                           allow_not_converged=False):
         """minimise every replica (find_inherent_structure); returns
-        {replica id: iterations}"""
+        {replica id: iterations}.  Raises if a replica reached
+        max_iterations unless ``allow_not_converged``."""
         n = max(self.specs) + 1 if self.specs else 1
         it = (C.c_int64 * n)()
-        _lib.check(self.lib.simmd_inherent_structure(self.ctx, float(tolerance), int(max_iterations),
-                                                     float(max_step_size), float(dt), it))
+        st = self.lib.simmd_inherent_structure(self.ctx, float(tolerance), int(max_iterations),
+                                               float(max_step_size), float(dt), it)
+        if not (allow_not_converged and st == _lib.ERR_NOT_CONVERGED):
+            _lib.check(st)
         return {rid: int(it[rid]) for rid in self.specs}
 
     def step(self, nsteps: int):

@@ -18,16 +18,20 @@ pytestmark = pytest.mark.gpu
 ARGS = dict(tolerance=1e-4, max_iterations=200000, max_step_size=0.001, dt=0.005)
 
 
-@pytest.mark.parametrize("pot,dims,N", [(1, 3, 500), (1, 2, 400), (0, 3, 216)])
-def test_inherent_structure_matches_oracle(simlib, oracle, pot, dims, N):
+# the reference's descent uses a fixed dt (v = F dt): stiff contacts need a
+# smaller one to converge (at dt = 0.005 the oracle oscillates for these)
+@pytest.mark.parametrize("pot,dims,N,dt", [(1, 3, 500, 0.005), (1, 2, 400, 1e-3), (0, 3, 216, 1e-3),
+                                           (0, 2, 400, 5e-4)])
+def test_inherent_structure_matches_oracle(simlib, oracle, pot, dims, N, dt):
     p, r, v, D, rc = make_case(pot, dims, 0, N, seed=21)
     ref = oracle.OracleSystem(p, r, D, v=v, force_cutoff=rc)
-    st, it_ref = oracle.find_inherent_structure(ref, **ARGS)
+    args = dict(ARGS, dt=dt)
+    st, it_ref = oracle.find_inherent_structure(ref, **args)
     assert st == 0
     gpu = GpuSystem(p, r, D, v=v, force_cutoff=rc)
     it = (C.c_int64 * 1)()
-    assert simlib.simmd_inherent_structure(gpu.ctx, ARGS["tolerance"], ARGS["max_iterations"],
-                                           ARGS["max_step_size"], ARGS["dt"], it) == 0
+    assert simlib.simmd_inherent_structure(gpu.ctx, args["tolerance"], args["max_iterations"],
+                                           args["max_step_size"], args["dt"], it) == 0
     rg = gpu.state()[0]
     assert np.abs(wrap_diff(rg, ref.r, p.box_size)).max() < 1e-8
     assert abs(int(it[0]) - it_ref) <= 2
@@ -50,13 +54,14 @@ def test_batch_minimisation_equals_alone(simlib):
              W.lj_spec(512, 3, _lib.NEWTONIAN, rng, precision=_lib.FP64, seed=2),
              W.berthier_spec(900, 3, _lib.LANGEVIN, rng, precision=_lib.FP32_SPLIT, seed=3)]
     W.relax_on_device(specs, 0, steps=100)
+    args = dict(ARGS, dt=1e-3, max_iterations=3000, allow_not_converged=True)
     mix = ReplicaBatch(0)
     ids = [mix.add(s) for s in specs]
-    its = mix.inherent_structure(**ARGS)
+    its = mix.inherent_structure(**args)
     for rid, s in zip(ids, specs):
         alone = ReplicaBatch(0)
         a = alone.add(s)
-        ita = alone.inherent_structure(**ARGS)
+        ita = alone.inherent_structure(**args)
         assert ita[a] == its[rid]
         assert np.array_equal(alone.state(a)[0], mix.state(rid)[0])
         alone.close()
