@@ -596,6 +596,20 @@ def run_gpu(args, dist):
             "step_breakdown_ms": {k: prof[k] / max(prof["steps"], 1) for k in ("force_ms", "kick_ms", "rebuild_ms",
                                                                                "update_ms")},
             "e2e": e2e, "gpu_launches": int(launches), "clocks": clk}
+    if any(sp.precision == 0 for sp in specs):
+        # the plain FP64 path is bound by GB300's FP64 pipe, not HBM: FP64
+        # operations of the reference pair arithmetic per list entry (3D soft
+        # spheres 45, 2D 39, LJ 3D 32, LJ 2D 24; a correctly rounded
+        # reciprocal or divide counted as 4) over the force-pass time
+        ops = 0
+        for sp, st in zip(specs, stats):
+            if sp.precision != 0:
+                continue
+            per = (45 if sp.dims == 3 else 39) if sp.potential == 1 else (32 if sp.dims == 3 else 24)
+            ops += per * int(st.list_entries)
+        line["fp64_pipe"] = {"ops_per_launch": ops, "achieved_tops": ops / (force_ms / 1000.0) / 1e12,
+                             "nominal_peak_tops": 0.625,
+                             "note": "nominal = 1.25 TFLOP/s FP64 counting an FMA as 2; DMUL/DADD issue at the FMA rate"}
     evolved = [batch.state(i)[0] for i in ids[:16]]
     batch.close()
     if dist.rank == 0 and any(s.precision != 0 for s in specs) and not args.no_compare:
