@@ -240,8 +240,10 @@ int simmd_sync(simmd_ctx* ctx);
 void* simmd_stream(simmd_ctx* ctx);          /* the context's cudaStream_t */
 int simmd_timer_start(simmd_ctx* ctx);       /* CUDA event on the context stream */
 int simmd_timer_stop(simmd_ctx* ctx, float* ms);
-int64_t simmd_launch_count(simmd_ctx* ctx);  /* kernels launched by this context */
-/* force-kernel launches and neighbour-rebuild sequences issued so far */
+int64_t simmd_launch_count(simmd_ctx* ctx);  /* kernels run by this context (synchronises) */
+/* force-kernel launches and neighbour-rebuild sequences run so far (a
+   captured step loop skips a rebuild sequence's body when no replica's
+   trigger fired; synchronises) */
 int simmd_kernel_counts(simmd_ctx* ctx, int64_t* force_launches, int64_t* rebuild_sequences);
 int64_t simmd_device_bytes(simmd_ctx* ctx);  /* device memory held */
 /* time the force pass alone: nrep launches, average ms per launch (CUDA

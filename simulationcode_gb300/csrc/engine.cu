@@ -26,7 +26,8 @@
 #include <vector>
 
 namespace simmd {
-void launch_rebuild_impl(const Batch& b, const LaunchCfg& lc, unsigned* nbr_full, int* ncnt_full, int Kfull);
+void launch_rebuild_plan_impl(const Batch& b, const LaunchCfg& lc, cudaGraphConditionalHandle cond, int use_cond);
+void launch_rebuild_body_impl(const Batch& b, const LaunchCfg& lc, unsigned* nbr_full, int* ncnt_full, int Kfull);
 void launch_export_impl(const Batch& b, const LaunchCfg& lc, int rep, const RepDesc& hd, const unsigned* lst,
                         const int* cnt, int T, long long* counts, long long* list, long long maxK, int half_only,
                         int* overflow);
@@ -125,6 +126,10 @@ struct simmd_ctx {
     cudaStream_t dump_stream = nullptr;
     cudaEvent_t ev_dump_ready = nullptr, ev_dump_done = nullptr;
     bool dump_pending = false;
+    // step-loop capture: rebuild bodies as conditional nodes
+    cudaStream_t body_stream = nullptr;
+    bool capturing = false;
+    cudaError_t capture_error = cudaSuccess;
     double* d_noise = nullptr;
     long long noise_cap = 0;
     long long bytes = 0;
@@ -688,11 +693,51 @@ static Mix batch_mix(simmd_ctx* c)
     return m;
 }
 
+// the rebuild sequence: plan, then (when some replica's trigger fired) the
+// body.  Direct launches run the body always (its kernels find an empty
+// plan); inside a stream capture of the step loop the body becomes a
+// conditional IF node whose condition the plan kernel sets.
 static void rebuild_launch(simmd_ctx* c, const Batch& b, const LaunchCfg& lc)
 {
     c->n_rebuild += 1;
-    launch_rebuild_impl(b, lc, c->keep_full ? c->nbr_full : nullptr, c->keep_full ? c->ncnt_full : nullptr,
-                        c->Kfull);
+    unsigned* nf = c->keep_full ? c->nbr_full : nullptr;
+    int* cf = c->keep_full ? c->ncnt_full : nullptr;
+    if (!c->capturing) {
+        launch_rebuild_plan_impl(b, lc, 0, 0);
+        launch_rebuild_body_impl(b, lc, nf, cf, c->Kfull);
+        return;
+    }
+    auto fail = [&](cudaError_t e) {
+        if (e != cudaSuccess && c->capture_error == cudaSuccess) c->capture_error = e;
+        return e != cudaSuccess;
+    };
+    cudaStreamCaptureStatus cs;
+    cudaGraph_t g = nullptr;
+    const cudaGraphNode_t* deps = nullptr;
+    const cudaGraphEdgeData* edges = nullptr;
+    size_t nd = 0;
+    if (fail(cudaStreamGetCaptureInfo(c->stream, &cs, nullptr, &g, &deps, &edges, &nd))) return;
+    cudaGraphConditionalHandle h;
+    if (fail(cudaGraphConditionalHandleCreate(&h, g, 0, cudaGraphCondAssignDefault))) return;
+    launch_rebuild_plan_impl(b, lc, h, 1);
+    if (fail(cudaStreamGetCaptureInfo(c->stream, &cs, nullptr, &g, &deps, &edges, &nd))) return;
+    cudaGraphNodeParams np = {};
+    np.type = cudaGraphNodeTypeConditional;
+    np.conditional.handle = h;
+    np.conditional.type = cudaGraphCondTypeIf;
+    np.conditional.size = 1;
+    cudaGraphNode_t node;
+    if (fail(cudaGraphAddNode(&node, g, deps, edges, nd, &np))) return;
+    cudaGraph_t body = np.conditional.phGraph_out[0];
+    if (fail(cudaStreamBeginCaptureToGraph(c->body_stream, body, nullptr, nullptr, 0,
+                                           cudaStreamCaptureModeThreadLocal)))
+        return;
+    LaunchCfg lb = lc;
+    lb.stream = c->body_stream;
+    launch_rebuild_body_impl(b, lb, nf, cf, c->Kfull);
+    cudaGraph_t captured = nullptr;
+    if (fail(cudaStreamEndCapture(c->body_stream, &captured))) return;
+    fail(cudaStreamUpdateCaptureDependencies(c->stream, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
 }
 
 static void enqueue_step(simmd_ctx* c, const Batch& b, const LaunchCfg& lc, const Mix& m, int fmode)
@@ -826,8 +871,15 @@ static int run_steps(simmd_ctx* c, long long nsteps, const double* noise)
             cudaGraph_t g;
             long long l0 = c->launches, f0 = c->n_force, r0 = c->n_rebuild;
             CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+            c->capturing = true;
+            c->capture_error = cudaSuccess;
             for (int s = 0; s < c->graph_steps; s++) enqueue_step(c, b, lc, m, fmode);
+            c->capturing = false;
             cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+            if (e == cudaSuccess && c->capture_error != cudaSuccess) {
+                cudaGraphDestroy(g);
+                e = c->capture_error;
+            }
             c->g_launches_per_replay = c->launches - l0;
             c->g_force_per_replay = c->n_force - f0;
             c->g_rebuild_per_replay = c->n_rebuild - r0;
@@ -919,7 +971,8 @@ int simmd_engine_create(int32_t device, simmd_ctx** out)
         return set_err(SIMMD_ERR_CUDA, "stream/event creation failed");
     }
     for (auto& e : c->pev) cudaEventCreate(&e);
-    if (cudaStreamCreateWithFlags(&c->dump_stream, cudaStreamNonBlocking) != cudaSuccess ||
+    if (cudaStreamCreateWithFlags(&c->body_stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&c->dump_stream, cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreateWithFlags(&c->ev_dump_ready, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&c->ev_dump_done, cudaEventDisableTiming) != cudaSuccess) {
         delete c;
@@ -957,6 +1010,7 @@ static void destroy_ctx(simmd_ctx* c)
     if (c->ev_dump_ready) cudaEventDestroy(c->ev_dump_ready);
     if (c->ev_dump_done) cudaEventDestroy(c->ev_dump_done);
     if (c->dump_stream) cudaStreamDestroy(c->dump_stream);
+    if (c->body_stream) cudaStreamDestroy(c->body_stream);
     for (auto& e : c->pev) cudaEventDestroy(e);
     cudaStreamDestroy(c->stream);
     delete c;
@@ -1417,13 +1471,34 @@ int simmd_timer_stop(simmd_ctx* c, float* ms)
     return SIMMD_OK;
 }
 
-int64_t simmd_launch_count(simmd_ctx* c) { return c ? c->launches : 0; }
+// rebuild bodies executed so far (device counter of k_rb_done); bodies that a
+// conditional graph node skipped are enqueued but not run
+static long long bodies_executed(simmd_ctx* c)
+{
+    unsigned long long n = 0;
+    cudaSetDevice(c->device);
+    if (cudaMemcpyAsync(&n, c->d_plan_cnt + 2, sizeof(n), cudaMemcpyDeviceToHost, c->stream) != cudaSuccess ||
+        cudaStreamSynchronize(c->stream) != cudaSuccess) {
+        cudaGetLastError();
+        return c->n_rebuild;
+    }
+    return (long long)n;
+}
+
+static const int REBUILD_BODY_LAUNCHES = 8;
+
+// kernels run: enqueued launches less the bodies that were skipped
+int64_t simmd_launch_count(simmd_ctx* c)
+{
+    if (!c) return 0;
+    return c->launches - REBUILD_BODY_LAUNCHES * (c->n_rebuild - bodies_executed(c));
+}
 
 int simmd_kernel_counts(simmd_ctx* c, int64_t* force_launches, int64_t* rebuild_sequences)
 {
     if (!c) return set_err(SIMMD_ERR_BAD_ARG, "NULL context");
     if (force_launches) *force_launches = c->n_force;
-    if (rebuild_sequences) *rebuild_sequences = c->n_rebuild;
+    if (rebuild_sequences) *rebuild_sequences = bodies_executed(c);
     return SIMMD_OK;
 }
 int64_t simmd_device_bytes(simmd_ctx* c) { return c ? c->bytes : 0; }

@@ -41,7 +41,10 @@ __device__ __forceinline__ int plan_count(const Batch& b, int which)
 // one block per replica: the tiles and cells of a rebuilding replica go to
 // the plan lists (order of replicas arbitrary, each task independent), and
 // its cell counters are zeroed
-__global__ void k_rb_plan(Batch b)
+// Inside a captured step loop the rest of the sequence is the body of a
+// conditional graph node: a planning block sets the node's condition, so a
+// step in which no replica's trigger fired skips the eight other launches.
+__global__ void k_rb_plan(Batch b, cudaGraphConditionalHandle cond, int use_cond)
 {
     const int r = blockIdx.x;
     if (r >= b.nreps) return;
@@ -51,6 +54,7 @@ __global__ void k_rb_plan(Batch b)
     if (!d.active || b.state[r].nonfinite || !need_rebuild(b.state[r], d)) return;
     __shared__ int s_tb, s_cb;
     if (threadIdx.x == 0) {
+        if (use_cond) cudaGraphSetConditional(cond, 1u);
         b.state[r].in_plan = 1;
         s_tb = atomicAdd(&b.plan_cnt[0], d.ntiles);
         s_cb = atomicAdd(&b.plan_cnt[1], d.ncell);
@@ -480,6 +484,7 @@ __global__ void k_rb_done(Batch b)
     if (r == 0) {  // every rebuild kernel of this sequence has run: the plan is spent
         b.plan_cnt[0] = 0;
         b.plan_cnt[1] = 0;
+        *reinterpret_cast<unsigned long long*>(b.plan_cnt + 2) += 1ull;  // bodies executed
     }
     if (r >= b.nreps) return;
     const RepDesc& d = b.desc[r];
@@ -491,10 +496,16 @@ __global__ void k_rb_done(Batch b)
     st.rebuilds += 1;
 }
 
-void launch_rebuild_impl(const Batch& b, const LaunchCfg& lc, unsigned* nbr_full, int* ncnt_full, int Kfull)
+void launch_rebuild_plan_impl(const Batch& b, const LaunchCfg& lc, cudaGraphConditionalHandle cond, int use_cond)
+{
+    k_rb_plan<<<b.nreps, 128, 0, lc.stream>>>(b, cond, use_cond);
+    if (lc.launches) *lc.launches += 1;
+}
+
+// the sequence after the plan (on lc.stream)
+void launch_rebuild_body_impl(const Batch& b, const LaunchCfg& lc, unsigned* nbr_full, int* ncnt_full, int Kfull)
 {
     int g = lc.grid_stream;
-    k_rb_plan<<<b.nreps, 128, 0, lc.stream>>>(b);
     k_rb_bin<<<g, TILE, 0, lc.stream>>>(b);
     k_rb_scan<<<b.nreps, 1024, 0, lc.stream>>>(b);
     k_rb_scatter<<<g, TILE, 0, lc.stream>>>(b);
@@ -503,7 +514,7 @@ void launch_rebuild_impl(const Batch& b, const LaunchCfg& lc, unsigned* nbr_full
     k_rb_build<<<g, BLD_THREADS, 0, lc.stream>>>(b, nbr_full, ncnt_full, Kfull);
     k_rb_copyback<<<g, TILE, 0, lc.stream>>>(b);
     k_rb_done<<<(b.nreps + 127) / 128, 128, 0, lc.stream>>>(b);
-    if (lc.launches) *lc.launches += 9;
+    if (lc.launches) *lc.launches += 8;
 }
 
 // ---------------------------------------------------------------------------
