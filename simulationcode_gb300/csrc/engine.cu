@@ -32,7 +32,7 @@ void launch_export_impl(const Batch& b, const LaunchCfg& lc, int rep, const RepD
                         const int* cnt, int T, long long* counts, long long* list, long long maxK, int half_only,
                         int* overflow);
 void launch_force_impl(const Batch& b, const LaunchCfg& lc, int mode, int prec_mask, double* epp);
-int force_blocks_per_sm(int T, int mode, int prec);
+int force_blocks_per_sm(int T, int mode, int prec, int parts);
 void launch_kick_drift_impl(const Batch& b, const LaunchCfg& lc);
 void launch_brownian_update_impl(const Batch& b, const LaunchCfg& lc);
 void launch_rescale_impl(const Batch& b, const LaunchCfg& lc);
@@ -222,7 +222,7 @@ static int force_rebuild_all(simmd_ctx* c)
 // list 4K; per tile the partial sums, plan and owner; per cell count, start
 // and plan entry; per replica its descriptor and state
 constexpr long long SLOT_BYTES = 32 + 72 + 32 + 12 + 12 + 84 + 8;
-constexpr long long TILE_BYTES = NPART * 8 + 4 + 4;
+constexpr long long TILE_BYTES = NPART * 8 * WARP_SLOTS + 4 + 4;
 constexpr long long CELL_BYTES = 4 + 4 + 8;
 
 static long long capacity_bytes(const simmd_ctx* c, long long S, long long C, int R, int K)
@@ -295,7 +295,7 @@ static int ensure_capacity(simmd_ctx* c, long long S_need, long long C_need, int
         TRY(grow_fresh(c, &s.t_orig, S_old, S_new));
         TRY(grow_fresh(c, &c->epp, S_old, S_new));
         long long nt_old = S_old / TILE, nt_new = S_new / TILE;
-        TRY(grow_fresh(c, &c->d_tile_part, nt_old * NPART, nt_new * NPART));
+        TRY(grow_fresh(c, &c->d_tile_part, nt_old * NPART * WARP_SLOTS, nt_new * NPART * WARP_SLOTS));
         TRY(grow_fresh(c, &c->d_plan_tiles, nt_old, nt_new));
         TRY(grow_keep(c, &c->d_tile_rep, nt_old, nt_new));
         c->h_tile_rep.resize((size_t)nt_new, -1);
@@ -381,6 +381,18 @@ static void give_range(std::vector<Range>& fl, long long start, long long len)
     fl = m;
 }
 
+// work items per tile in the force pass: split tiles of small batches until
+// there are about four items per SM (each block keeps at least one full warp)
+static int force_parts(const simmd_ctx* c)
+{
+    long long tiles = 0;
+    for (const auto& h : c->reps)
+        if (h.active) tiles += h.d.ntiles;
+    int parts = 1;
+    while (parts < MAX_PARTS && tiles * parts < 4LL * c->sm_count && (TILE / (2 * parts)) * c->T >= 32) parts *= 2;
+    return parts;
+}
+
 static Batch make_batch(simmd_ctx* c)
 {
     Batch b{};
@@ -392,6 +404,7 @@ static Batch make_batch(simmd_ctx* c)
     b.S = c->S_cap;
     b.K = c->K;
     b.tpp = c->T;
+    b.parts = force_parts(c);
     b.s = c->s;
     b.tile_part = c->d_tile_part;
     b.queue = c->d_queue;
@@ -407,8 +420,9 @@ static LaunchCfg make_lc(simmd_ctx* c, int mode)
     lc.stream = c->stream;
     long long nt = c->S_cap / TILE;
     lc.grid_stream = (int)std::max(1LL, std::min(nt, (long long)c->sm_count * 16));
-    lc.grid_force64 = c->sm_count * force_blocks_per_sm(c->T, mode, PREC_FP64);
-    lc.grid_force32 = c->sm_count * force_blocks_per_sm(c->T, mode, PREC_FP32);
+    const int parts = force_parts(c);
+    lc.grid_force64 = c->sm_count * force_blocks_per_sm(c->T, mode, PREC_FP64, parts);
+    lc.grid_force32 = c->sm_count * force_blocks_per_sm(c->T, mode, PREC_FP32, parts);
     lc.launches = &c->launches;
     return lc;
 }
@@ -823,9 +837,10 @@ static int read_states(simmd_ctx* c)
     return st;
 }
 
-static int graph_key(const Mix& m, int fmode)
+static int graph_key(const simmd_ctx* c, const Mix& m, int fmode)
 {
-    return (m.nl ? 1 : 0) | (m.br ? 2 : 0) | (m.rescale ? 4 : 0) | (m.prec_mask << 3) | (fmode << 5);
+    return (m.nl ? 1 : 0) | (m.br ? 2 : 0) | (m.rescale ? 4 : 0) | (m.prec_mask << 3) | (fmode << 5) |
+           (force_parts(c) << 8);
 }
 
 static int run_steps(simmd_ctx* c, long long nsteps, const double* noise)
@@ -865,7 +880,7 @@ static int run_steps(simmd_ctx* c, long long nsteps, const double* noise)
         h.d.host_noise = nullptr;
         TRY(push_desc(c, single));
     } else if (c->use_graphs && !c->profile && nsteps >= c->graph_steps) {
-        int key = graph_key(m, fmode);
+        int key = graph_key(c, m, fmode);
         if (!c->gexec || c->gkey != key) {
             invalidate_graph(c);
             cudaGraph_t g;

@@ -169,11 +169,11 @@ __device__ __forceinline__ void pair_f32(const RepDesc& d, const float4& oi, con
 // list entry n of the particle: from the tile's rows staged in shared memory
 // (rows < nrows), else from global memory
 template <int T>
-__device__ __forceinline__ unsigned list_entry(const Batch& b, const unsigned* s_rows, int nrows, long long i, int p,
-                                               int n)
+__device__ __forceinline__ unsigned list_entry(const Batch& b, const unsigned* s_rows, int nrows, long long i, int pl,
+                                               int ppb, int n)
 {
     const int row = n / T;
-    if (row < nrows) return s_rows[row * (TILE * T) + p * T + (n % T)] & IDX_MASK;
+    if (row < nrows) return s_rows[row * (ppb * T) + pl * T + (n % T)] & IDX_MASK;
     return __ldg(b.s.nbr + nbr_addr(n, i, T, b.K)) & IDX_MASK;
 }
 
@@ -187,7 +187,8 @@ constexpr int PAIR_UNROLL = SIMMD_PAIR_UNROLL;
 template <int DIM, int POT, bool EN, int T>
 __device__ __forceinline__ void pairs_f32(const Batch& b, const RepDesc& d, long long i, int sub,
                                           const float4 oi, const float4 gi, int cnt, float& fx, float& fy,
-                                          float& fz, float& e, float& w, const unsigned* s_rows, int nrows, int p)
+                                          float& fz, float& e, float& w, const unsigned* s_rows, int nrows, int pl,
+                                          int ppb)
 {
     const SplitRec* __restrict__ rec = b.s.rec;
     int n = sub;
@@ -195,7 +196,7 @@ __device__ __forceinline__ void pairs_f32(const Batch& b, const RepDesc& d, long
         unsigned j[PAIR_UNROLL];
         float4 o[PAIR_UNROLL], g[PAIR_UNROLL];
 #pragma unroll
-        for (int u = 0; u < PAIR_UNROLL; u++) j[u] = list_entry<T>(b, s_rows, nrows, i, p, n + u * T);
+        for (int u = 0; u < PAIR_UNROLL; u++) j[u] = list_entry<T>(b, s_rows, nrows, i, pl, ppb, n + u * T);
 #pragma unroll
         for (int u = 0; u < PAIR_UNROLL; u++) {
             o[u] = __ldg(&rec[j[u]].o);
@@ -205,7 +206,7 @@ __device__ __forceinline__ void pairs_f32(const Batch& b, const RepDesc& d, long
         for (int u = 0; u < PAIR_UNROLL; u++) pair_f32<DIM, POT, EN>(d, oi, gi, o[u], g[u], fx, fy, fz, e, w);
     }
     for (; n < cnt; n += T) {
-        const unsigned j0 = list_entry<T>(b, s_rows, nrows, i, p, n);
+        const unsigned j0 = list_entry<T>(b, s_rows, nrows, i, pl, ppb, n);
         pair_f32<DIM, POT, EN>(d, oi, gi, __ldg(&rec[j0].o), __ldg(&rec[j0].g), fx, fy, fz, e, w);
     }
 }
@@ -264,13 +265,13 @@ __device__ __forceinline__ void particle_pairs_f64(const Batch& b, const RepDesc
 template <int DIM, bool EN, int T>
 __device__ __forceinline__ void particle_pairs_f32(const Batch& b, const RepDesc& d, long long i, int sub, int cnt,
                                                    float& fx, float& fy, float& fz, float& e, float& w,
-                                                   const unsigned* s_rows, int nrows, int p)
+                                                   const unsigned* s_rows, int nrows, int pl, int ppb)
 {
     const float4 oi = b.s.rec[i].o;
     const float4 gi = b.s.rec[i].g;
     if (d.pot == POT_BERTHIER)
-        pairs_f32<DIM, POT_BERTHIER, EN, T>(b, d, i, sub, oi, gi, cnt, fx, fy, fz, e, w, s_rows, nrows, p);
-    else pairs_f32<DIM, POT_LJ, EN, T>(b, d, i, sub, oi, gi, cnt, fx, fy, fz, e, w, s_rows, nrows, p);
+        pairs_f32<DIM, POT_BERTHIER, EN, T>(b, d, i, sub, oi, gi, cnt, fx, fy, fz, e, w, s_rows, nrows, pl, ppb);
+    else pairs_f32<DIM, POT_LJ, EN, T>(b, d, i, sub, oi, gi, cnt, fx, fy, fz, e, w, s_rows, nrows, pl, ppb);
 }
 
 // rows of the tile's list staged in shared memory (16-byte loads, all rows
@@ -280,15 +281,20 @@ __device__ __forceinline__ void particle_pairs_f32(const Batch& b, const RepDesc
 #endif
 constexpr int STAGE_WORDS = SIMMD_STAGE_WORDS;  // list entries staged per block (8 KB)
 
+// A block covers the ppb particles of one part of a tile; each staged row
+// holds their ppb*T entries (one contiguous run of the tile-major row).
 template <int T>
-__device__ __forceinline__ int stage_rows(const Batch& b, int t, int maxcnt, unsigned* s_rows)
+__device__ __forceinline__ int stage_rows(const Batch& b, int t, int part, int ppb, int maxcnt, unsigned* s_rows)
 {
-    constexpr int row_words = TILE * T;
+    const int row_words = ppb * T, vpr = row_words / 4;
     const int nrows = min((maxcnt + T - 1) / T, STAGE_WORDS / row_words);
-    // the tile's rows are one contiguous run (tile-major list layout)
-    const uint4* src = reinterpret_cast<const uint4*>(b.s.nbr + (size_t)t * ((size_t)TILE * (size_t)b.K));
+    const uint4* src = reinterpret_cast<const uint4*>(b.s.nbr + (size_t)t * ((size_t)TILE * (size_t)b.K) +
+                                                      (size_t)part * row_words);
     uint4* dst = reinterpret_cast<uint4*>(s_rows);
-    for (int v = threadIdx.x; v < nrows * (row_words / 4); v += blockDim.x) dst[v] = __ldg(src + v);
+    for (int v = threadIdx.x; v < nrows * vpr; v += blockDim.x) {
+        const int row = v / vpr, c4 = v - row * vpr;
+        dst[v] = __ldg(src + (size_t)row * (TILE * T / 4) + c4);
+    }
     return nrows;
 }
 
@@ -333,10 +339,10 @@ __device__ __forceinline__ void finish_replica(const RepDesc& d, RepState& st, c
     if (noise) st.step += 1;
 }
 
-template <int MODE, int PREC, int T>
 #ifndef SIMMD_F32_MINB
-#define SIMMD_F32_MINB 8
+#define SIMMD_F32_MINB 12
 #endif
+template <int MODE, int PREC, int T>
 __global__ void __launch_bounds__(TILE * T, (PREC == PREC_FP32 ? SIMMD_F32_MINB : 4) / T) k_force(Batch b, double* epp)
 {
     constexpr bool EN = (MODE == FMODE_ENERGY || MODE == FMODE_STEP_ENERGY);
@@ -345,16 +351,21 @@ __global__ void __launch_bounds__(TILE * T, (PREC == PREC_FP32 ? SIMMD_F32_MINB 
     __shared__ int s_tile;
     __shared__ int s_flag;
     __shared__ int s_maxcnt;
-    __shared__ double s_part[32 * NV];
     __shared__ __align__(16) unsigned s_rows[(PREC == PREC_FP32 && STAGE_WORDS >= 4) ? STAGE_WORDS : 4];
     const int tid = threadIdx.x;
-    const int p = tid / T, sub = tid - p * T;
+    // work item = one part of a tile: parts per tile b.parts (a power of two,
+    // > 1 only for small batches, so that every SM gets work), ppb particles
+    // per part, blockDim = ppb * T
+    const int parts = b.parts, ppb = TILE / parts;
+    const int pl = tid / T, sub = tid - pl * T;
     for (;;) {
         if (tid == 0) s_tile = atomicAdd(&b.queue[0], 1);
         __syncthreads();
-        const int t = s_tile;
+        const int item = s_tile;
         __syncthreads();
-        if (t >= b.ntiles) break;
+        if (item >= b.ntiles * parts) break;
+        const int t = item / parts, part = item - t * parts;
+        const int p = part * ppb + pl;
         const int r = b.tile_rep[t];
         if (r < 0) continue;
         const RepDesc& d = b.desc[r];
@@ -379,11 +390,12 @@ __global__ void __launch_bounds__(TILE * T, (PREC == PREC_FP32 ? SIMMD_F32_MINB 
             __syncthreads();
             if (sub == 0 && cnt > 0) atomicMax(&s_maxcnt, cnt);
             __syncthreads();
-            const int nrows = stage_rows<T>(b, t, s_maxcnt, s_rows);
+            const int nrows = stage_rows<T>(b, t, part, ppb, s_maxcnt, s_rows);
             __syncthreads();
             if (real) {
-                if (d.dims == 3) particle_pairs_f32<3, EN, T>(b, d, i, sub, cnt, fx, fy, fz, e, w, s_rows, nrows, p);
-                else particle_pairs_f32<2, EN, T>(b, d, i, sub, cnt, fx, fy, fz, e, w, s_rows, nrows, p);
+                if (d.dims == 3)
+                    particle_pairs_f32<3, EN, T>(b, d, i, sub, cnt, fx, fy, fz, e, w, s_rows, nrows, pl, ppb);
+                else particle_pairs_f32<2, EN, T>(b, d, i, sub, cnt, fx, fy, fz, e, w, s_rows, nrows, pl, ppb);
             }
             if (T > 1) combine_lanes<float, T, EN>(fx, fy, fz, e, w);
             float q0 = 0.f, q1 = 0.f, q2 = 0.f;  // per-particle contribution to the replica sums
@@ -468,7 +480,7 @@ __global__ void __launch_bounds__(TILE * T, (PREC == PREC_FP32 ? SIMMD_F32_MINB 
                 pv[NV - 2] = de;
                 pv[NV - 1] = dw;
             }
-            last = tile_reduce<NV, true>(b, t, d, st, pv, out, s_part, &s_flag);
+            last = tile_reduce<NV, true>(b, item, d, st, pv, out, &s_flag, parts);
         } else {
             // ---- FP64: the reference's arithmetic
             double fx = 0.0, fy = 0.0, fz = 0.0, e = 0.0, w = 0.0;
@@ -525,7 +537,7 @@ __global__ void __launch_bounds__(TILE * T, (PREC == PREC_FP32 ? SIMMD_F32_MINB 
                     }
                 }
             }
-            last = tile_reduce<NV>(b, t, d, st, pv, out, s_part, &s_flag);
+            last = tile_reduce<NV>(b, item, d, st, pv, out, &s_flag, parts);
         }
         if (last && tid == 0) finish_replica<MODE, NV>(d, st, out, noise);
     }
@@ -562,11 +574,11 @@ static void* kernel_for(int mode, int T)
     }
 }
 
-int force_blocks_per_sm(int T, int mode, int prec)
+int force_blocks_per_sm(int T, int mode, int prec, int parts)
 {
     int nb = 0;
     void* k = prec == PREC_FP64 ? kernel_for<PREC_FP64>(mode, T) : kernel_for<PREC_FP32>(mode, T);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k, TILE * T, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k, (TILE / parts) * T, 0);
     return nb > 0 ? nb : 1;
 }
 
@@ -579,8 +591,8 @@ void launch_force_impl(const Batch& b, const LaunchCfg& lc, int mode, int prec_m
         Batch bb = b;
         double* ep = epp;
         void* args[] = {(void*)&bb, (void*)&ep};
-        cudaLaunchKernel(k, dim3(prec == PREC_FP64 ? lc.grid_force64 : lc.grid_force32), dim3(TILE * b.tpp), args,
-                         0, lc.stream);
+        cudaLaunchKernel(k, dim3(prec == PREC_FP64 ? lc.grid_force64 : lc.grid_force32),
+                         dim3((TILE / b.parts) * b.tpp), args, 0, lc.stream);
         if (lc.launches) *lc.launches += 1;
     }
 }

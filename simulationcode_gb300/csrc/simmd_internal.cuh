@@ -22,7 +22,9 @@ constexpr int TILE = 128;                       // slots per tile (work unit)
 constexpr int IDX_BITS = 26;
 constexpr unsigned IDX_MASK = (1u << IDX_BITS) - 1u;
 constexpr int MAX_CELLS_AXIS = 1023;
-constexpr int NPART = 8;                        // doubles of partial sums per tile
+constexpr int NPART = 8;                        // doubles of partial sums per warp slot
+constexpr int MAX_PARTS = 16;                   // work items per tile in the force pass
+constexpr int WARP_SLOTS = TILE * 4 / 32;       // warp partial-sum slots per tile (threads per particle <= 4)
 
 enum { POT_LJ = 0, POT_BERTHIER = 1 };
 enum { DYN_NEWTONIAN = 0, DYN_LANGEVIN = 1, DYN_BROWNIAN = 2 };
@@ -123,8 +125,9 @@ struct Batch {
     long long S;                  // slot capacity
     int K;                        // list rows
     int tpp;                      // threads per particle (list interleave)
+    int parts;                    // force pass: work items per tile (power of two, <= MAX_PARTS)
     Slots s;
-    double* tile_part;            // [ntiles][NPART]
+    double* tile_part;            // [ntiles][WARP_SLOTS][NPART]
     int* queue;                   // work-queue heads [4]
     // rebuild plan: tiles and cells of the replicas rebuilding this step
     int* plan_tiles;              // [ntiles]
