@@ -484,6 +484,8 @@ def run_gpu(args, dist):
         tune = autotune(batch, tpps=(1, 2, 4), skins=skins,
                         log=lambda m: print(m, file=sys.stderr, flush=True))
         args.tpp = tune.tpp
+    if not args.graphs:
+        batch.set_tuning(args.tpp, False, 16)
     batch.step(args.warmup)
     st_before = [batch.stats(i) for i in ids]
     # kernel launches of this process before the timed region (for ncu -s)
@@ -585,6 +587,7 @@ def run_gpu(args, dist):
                              if step_bytes > 129e6 else "state fits in L2 (%.0f MB; no flush)" % (step_bytes / 1e6),
                        "parallelism": "replicas only" if dist.ws > 1 else "single GPU",
                        "rebuilds_in_timed_region": rebuilds,
+                       "step_loop": "CUDA graph of 16 steps" if args.graphs else "direct launches",
                        "skin": specs[0].skin,
                        "autotune": None if tune is None else {"tpp": tune.tpp, "skin": tune.skin,
                                                               "graph_steps": tune.graph_steps,
@@ -643,6 +646,9 @@ def main():
     ap.add_argument("--no-profile-pass", action="store_true")
     ap.add_argument("--relax-steps", type=int, default=300)
     ap.add_argument("--skin", type=float, default=None, help="override the workload's skin (without autotuning)")
+    ap.add_argument("--no-graphs", dest="graphs", action="store_false",
+                    help="direct launches instead of the captured step loop (for per-kernel profiling: ncu does not "
+                         "profile kernel nodes of graphs with conditional nodes)")
     ap.add_argument("--no-autotune", dest="autotune", action="store_false",
                     help="skip the autotuner (threads per particle, skin / rebuild cadence)")
     ap.add_argument("--tune-skins", default="0.3,0.4,0.5,0.6,0.7",

@@ -381,15 +381,17 @@ static void give_range(std::vector<Range>& fl, long long start, long long len)
     fl = m;
 }
 
-// work items per tile in the force pass: split tiles of small batches until
-// there are about four items per SM (each block keeps at least one full warp)
+// work items per tile in the force pass: a batch with fewer tiles than SMs
+// splits its tiles until every SM has an item (each block keeps at least one
+// full warp); larger batches keep whole tiles, whose particles share their
+// neighbours' records in one SM's L1
 static int force_parts(const simmd_ctx* c)
 {
     long long tiles = 0;
     for (const auto& h : c->reps)
         if (h.active) tiles += h.d.ntiles;
     int parts = 1;
-    while (parts < MAX_PARTS && tiles * parts < 4LL * c->sm_count && (TILE / (2 * parts)) * c->T >= 32) parts *= 2;
+    while (parts < MAX_PARTS && tiles * parts < c->sm_count && (TILE / (2 * parts)) * c->T >= 32) parts *= 2;
     return parts;
 }
 

@@ -22,6 +22,13 @@ __device__ __forceinline__ void warp_sum(double (&v)[NV])
         for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_xor_sync(0xffffffffu, v[k], o);
 }
 
+__device__ __forceinline__ void neumaier_add(double& s, double& c, double x)
+{
+    const double t = s + x;
+    c += (fabs(s) >= fabs(x)) ? (s - t) + x : (x - t) + s;
+    s = t;
+}
+
 // Returns true in the threads of the block that must finalise the replica;
 // in that case out[] (valid in thread 0) holds the replica totals.
 // WARP_DONE: the caller has already reduced each warp (lane 0's v[] is
@@ -56,17 +63,25 @@ __device__ bool tile_reduce(const Batch& b, int item, const RepDesc& d, RepState
 #pragma unroll
             for (int k = 0; k < NV; k++) { s[k] = 0.0; c[k] = 0.0; }
             const int nslots = d.ntiles * wpt;
-            const size_t base = (size_t)d.tile0 * wpt;
-            for (int q = lane; q < nslots; q += 32) {
-                const volatile double* tp = b.tile_part + (base + q) * NPART;
+            const double* tp = b.tile_part + (size_t)d.tile0 * wpt * NPART;
+            // lane-strided slots, eight loads in flight per lane (through L2:
+            // other blocks wrote them), summed in slot order
+            constexpr int U = 8;
+            int q = lane;
+            for (; q + 32 * (U - 1) < nslots; q += 32 * U) {
+                double x[U][NV];
 #pragma unroll
-                for (int k = 0; k < NV; k++) {
-                    double x = tp[k];
-                    double tsum = s[k] + x;
-                    c[k] += (fabs(s[k]) >= fabs(x)) ? (s[k] - tsum) + x : (x - tsum) + s[k];
-                    s[k] = tsum;
-                }
+                for (int u = 0; u < U; u++)
+#pragma unroll
+                    for (int k = 0; k < NV; k++) x[u][k] = __ldcg(tp + (size_t)(q + 32 * u) * NPART + k);
+#pragma unroll
+                for (int u = 0; u < U; u++)
+#pragma unroll
+                    for (int k = 0; k < NV; k++) neumaier_add(s[k], c[k], x[u][k]);
             }
+            for (; q < nslots; q += 32)
+#pragma unroll
+                for (int k = 0; k < NV; k++) neumaier_add(s[k], c[k], __ldcg(tp + (size_t)q * NPART + k));
 #pragma unroll
             for (int k = 0; k < NV; k++) s[k] += c[k];
             warp_sum<NV>(s);
