@@ -311,7 +311,9 @@ __device__ void build_cell(const Batch& b, const RepDesc& d, RepState& st, int c
     const float rfx = (float)grid_index(((double)cx + 0.5) * d.cs, d) * d.hf,
                 rfy = (float)grid_index(((double)cy + 0.5) * d.cs, d) * d.hf,
                 rfz = (DIM == 3) ? (float)grid_index(((double)cz + 0.5) * d.cs, d) * d.hf : 0.0f;
-    const int Tb = P <= 16 ? 8 : (P <= 32 ? 4 : (P <= 64 ? 2 : 1));
+    // lanes per home particle: as many as keep the block's 128 threads busy
+    // (a power of two dividing 32, so a particle's lanes share one warp)
+    const int Tb = P <= 4 ? 32 : (P <= 8 ? 16 : (P <= 16 ? 8 : (P <= 32 ? 4 : (P <= 64 ? 2 : 1))));
     const int sub = tid % Tb;
     const int lane = tid & 31;
     const int gbase = (lane / Tb) * Tb;

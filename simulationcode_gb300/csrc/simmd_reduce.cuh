@@ -47,10 +47,10 @@ __device__ bool tile_reduce(const Batch& b, int item, const RepDesc& d, RepState
         double* dst = b.tile_part + ((size_t)t * wpt + (size_t)(part * nw + wid)) * NPART;
 #pragma unroll
         for (int k = 0; k < NV; k++) dst[k] = v[k];
-        __threadfence();
     }
     __syncthreads();
     if (tid == 0) {
+        __threadfence();  // after the barrier: publishes every warp's slot (cumulative)
         const int prev = atomicAdd(&st.done_count, 1);
         *s_flag = (prev == nitems - 1);
     }
