@@ -481,7 +481,7 @@ def run_gpu(args, dist):
     if args.autotune:
         from simulationcode_gb300.autotune import autotune
         skins = [float(x) for x in args.tune_skins.split(",")] if args.tune_skins else None
-        tune = autotune(batch, tpps=(1, 2, 4), skins=skins,
+        tune = autotune(batch, tpps=(1, 2, 4, 8), skins=skins,
                         log=lambda m: print(m, file=sys.stderr, flush=True))
         args.tpp = tune.tpp
     if not args.graphs:

@@ -229,7 +229,7 @@ int simmd_energy_virial_noalloc(const simmd_params* p, const double* r, const do
 
 /* ---- tuning, timing, plumbing ------------------------------------------ */
 
-/* threads per particle in the force pass (1, 2, 4), CUDA-graph capture of
+/* threads per particle in the force pass (1, 2, 4, 8), CUDA-graph capture of
  * the step loop (0/1) and steps per captured graph. */
 int simmd_set_tuning(simmd_ctx* ctx, int32_t threads_per_particle, int32_t use_graphs, int32_t graph_steps);
 /* change the neighbour-list skin (the rebuild cadence) of one replica (or

@@ -41,7 +41,7 @@ def _may_overflow(batch: ReplicaBatch, skin: float, skin_seen: float, margin: fl
     return False
 
 
-def autotune(batch: ReplicaBatch, *, tpps: Iterable[int] = (1, 2, 4), skins: Optional[Iterable[float]] = None,
+def autotune(batch: ReplicaBatch, *, tpps: Iterable[int] = (1, 2, 4, 8), skins: Optional[Iterable[float]] = None,
              graph_steps: Iterable[int] = (16,), warmup: int = 32, steps: int = 96, log=None) -> TuneResult:
     """Grid search; ``skins`` None keeps the replicas' configured skin.  A
     skin whose predicted longest list could overflow max_neighbors is

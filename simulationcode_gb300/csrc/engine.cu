@@ -1441,7 +1441,7 @@ int64_t simmd_replica_bytes(const simmd_params* p, int32_t max_neighbors)
 int simmd_set_tuning(simmd_ctx* c, int32_t tpp, int32_t use_graphs, int32_t graph_steps)
 {
     if (!c) return set_err(SIMMD_ERR_BAD_ARG, "NULL context");
-    if (tpp != 1 && tpp != 2 && tpp != 4) return set_err(SIMMD_ERR_BAD_ARG, "tpp must be 1, 2 or 4");
+    if (tpp != 1 && tpp != 2 && tpp != 4 && tpp != 8) return set_err(SIMMD_ERR_BAD_ARG, "tpp must be 1, 2, 4 or 8");
     CK(cudaSetDevice(c->device));
     if (tpp != c->T) {
         CK(cudaStreamSynchronize(c->stream));

@@ -11,13 +11,15 @@
 //   kick2 + centre-of-mass removal     src/MD.jl:528-542
 //   find_energy inner loops            src/AuxiliaryFunctions.jl:381-444, 477-507, 571-581
 //
-// One persistent kernel per launch and precision: blocks pull 128-slot tiles
+// One persistent kernel per launch and precision: blocks pull work items
+// (a 128-slot tile, or a part of one for batches with fewer tiles than SMs)
 // from an atomic work queue; a tile belongs to one replica, so (dims,
 // potential, dynamics) are uniform per block.  T threads per particle
-// (compile-time) split the particle's list (interleaved ELL) and combine
-// with __shfl_xor; the pair loop is unrolled by two so two gathers are in
-// flight per thread.  Every pair is visited from both sides (no atomics,
-// deterministic sums).
+// (compile-time) split the particle's list (tile-major ELL, entries of one
+// particle's T lanes adjacent) and combine with __shfl_xor; the split
+// pass stages the first list rows of its particles in shared memory and
+// gathers PAIR_UNROLL neighbour records at a time.  Every pair is visited
+// from both sides (no atomics, deterministic sums).
 //
 // FP64 path: the reference's per-pair operation order with explicit
 // round-to-nearest intrinsics, so each pair force is bit-identical to the
@@ -342,8 +344,14 @@ __device__ __forceinline__ void finish_replica(const RepDesc& d, RepState& st, c
 #ifndef SIMMD_F32_MINB
 #define SIMMD_F32_MINB 12
 #endif
+template <int PREC, int T>
+constexpr int force_min_blocks()
+{
+    return ((PREC == PREC_FP32 ? SIMMD_F32_MINB : 4) / T) > 0 ? (PREC == PREC_FP32 ? SIMMD_F32_MINB : 4) / T : 1;
+}
+
 template <int MODE, int PREC, int T>
-__global__ void __launch_bounds__(TILE * T, (PREC == PREC_FP32 ? SIMMD_F32_MINB : 4) / T) k_force(Batch b, double* epp)
+__global__ void __launch_bounds__(TILE * T, force_min_blocks<PREC, T>()) k_force(Batch b, double* epp)
 {
     constexpr bool EN = (MODE == FMODE_ENERGY || MODE == FMODE_STEP_ENERGY);
     constexpr bool STEP = (MODE == FMODE_STEP || MODE == FMODE_STEP_ENERGY);
@@ -559,6 +567,7 @@ static void* kernel_ptr(int T)
     switch (T) {
         case 2: return (void*)k_force<MODE, PREC, 2>;
         case 4: return (void*)k_force<MODE, PREC, 4>;
+        case 8: return (void*)k_force<MODE, PREC, 8>;
         default: return (void*)k_force<MODE, PREC, 1>;
     }
 }

@@ -11,7 +11,7 @@
 //   * a padded ELL neighbour list, tile-major (see nbr_addr; T = threads per
 //     particle), each entry the slot of j (low 26 bits);
 //   * per-replica descriptors (read-only) and states (flags, counters,
-//     reductions), a tile -> replica table and per-tile partial sums.
+//     reductions), a tile -> replica table and per-warp partial-sum slots.
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -24,7 +24,8 @@ constexpr unsigned IDX_MASK = (1u << IDX_BITS) - 1u;
 constexpr int MAX_CELLS_AXIS = 1023;
 constexpr int NPART = 8;                        // doubles of partial sums per warp slot
 constexpr int MAX_PARTS = 16;                   // work items per tile in the force pass
-constexpr int WARP_SLOTS = TILE * 4 / 32;       // warp partial-sum slots per tile (threads per particle <= 4)
+constexpr int MAX_TPP = 8;                      // threads per particle: 1, 2, 4 or 8
+constexpr int WARP_SLOTS = TILE * MAX_TPP / 32; // warp partial-sum slots per tile
 
 enum { POT_LJ = 0, POT_BERTHIER = 1 };
 enum { DYN_NEWTONIAN = 0, DYN_LANGEVIN = 1, DYN_BROWNIAN = 2 };

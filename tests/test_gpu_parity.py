@@ -124,7 +124,7 @@ def test_many_steps_graph_path_matches_direct(simlib, oracle):
         assert np.array_equal(x, y)
 
 
-@pytest.mark.parametrize("tpp", [2, 4])
+@pytest.mark.parametrize("tpp", [2, 4, 8])
 def test_threads_per_particle_same_forces(simlib, oracle, tpp):
     p, r, v, D, rc = make_case(1, 3, 0, 1728, seed=10)
     ref = oracle.OracleSystem(p, r, D, v=v, force_cutoff=rc)
