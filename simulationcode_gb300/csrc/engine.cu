@@ -112,6 +112,8 @@ struct simmd_ctx {
     RepState* d_state = nullptr;
     int* d_tile_rep = nullptr;
     double* d_tile_part = nullptr;
+    double* d_warp_part = nullptr;
+    int* d_tile_cnt = nullptr;
     int* d_queue = nullptr;
     int* d_plan_tiles = nullptr;
     int2* d_plan_cells = nullptr;
@@ -222,7 +224,7 @@ static int force_rebuild_all(simmd_ctx* c)
 // list 4K; per tile the partial sums, plan and owner; per cell count, start
 // and plan entry; per replica its descriptor and state
 constexpr long long SLOT_BYTES = 32 + 72 + 32 + 12 + 12 + 84 + 8;
-constexpr long long TILE_BYTES = NPART * 8 * WARP_SLOTS + 4 + 4;
+constexpr long long TILE_BYTES = NPART * 8 * (1 + WARP_SLOTS) + 4 + 4 + 4;
 constexpr long long CELL_BYTES = 4 + 4 + 8;
 
 static long long capacity_bytes(const simmd_ctx* c, long long S, long long C, int R, int K)
@@ -295,7 +297,9 @@ static int ensure_capacity(simmd_ctx* c, long long S_need, long long C_need, int
         TRY(grow_fresh(c, &s.t_orig, S_old, S_new));
         TRY(grow_fresh(c, &c->epp, S_old, S_new));
         long long nt_old = S_old / TILE, nt_new = S_new / TILE;
-        TRY(grow_fresh(c, &c->d_tile_part, nt_old * NPART * WARP_SLOTS, nt_new * NPART * WARP_SLOTS));
+        TRY(grow_fresh(c, &c->d_tile_part, nt_old * NPART, nt_new * NPART));
+        TRY(grow_fresh(c, &c->d_warp_part, nt_old * NPART * WARP_SLOTS, nt_new * NPART * WARP_SLOTS));
+        TRY(grow_fresh(c, &c->d_tile_cnt, nt_old, nt_new));
         TRY(grow_fresh(c, &c->d_plan_tiles, nt_old, nt_new));
         TRY(grow_keep(c, &c->d_tile_rep, nt_old, nt_new));
         c->h_tile_rep.resize((size_t)nt_new, -1);
@@ -409,6 +413,8 @@ static Batch make_batch(simmd_ctx* c)
     b.parts = force_parts(c);
     b.s = c->s;
     b.tile_part = c->d_tile_part;
+    b.warp_part = c->d_warp_part;
+    b.tile_cnt = c->d_tile_cnt;
     b.queue = c->d_queue;
     b.plan_tiles = c->d_plan_tiles;
     b.plan_cells = c->d_plan_cells;
@@ -1017,7 +1023,7 @@ static void destroy_ctx(simmd_ctx* c)
     void* ptrs[] = {s.posD, s.vx, s.vy, s.vz, s.fx, s.fy, s.fz, s.ux, s.uy, s.uz, s.rec, s.cellc, s.orig, s.nbr,
                     s.ncnt, s.bin_cell, s.bin_rank, s.src, s.t_posD, s.t_vx, s.t_vy, s.t_vz, s.t_fx, s.t_fy,
                     s.t_fz, s.t_orig, s.cell_count, s.cell_start, c->nbr_full, c->ncnt_full, c->epp, c->d_desc,
-                    c->d_state, c->d_tile_rep, c->d_tile_part, c->d_queue, c->d_stage, c->d_dump, c->d_noise,
+                    c->d_state, c->d_tile_rep, c->d_tile_part, c->d_warp_part, c->d_tile_cnt, c->d_queue, c->d_stage, c->d_dump, c->d_noise,
                     c->d_plan_tiles, c->d_plan_cells, c->d_plan_cnt};
     for (void* p : ptrs)
         if (p) cudaFree(p);

@@ -359,6 +359,7 @@ __global__ void __launch_bounds__(TILE * T, force_min_blocks<PREC, T>()) k_force
     __shared__ int s_tile;
     __shared__ int s_flag;
     __shared__ int s_maxcnt;
+    __shared__ double s_part[32 * NV];
     __shared__ __align__(16) unsigned s_rows[(PREC == PREC_FP32 && STAGE_WORDS >= 4) ? STAGE_WORDS : 4];
     const int tid = threadIdx.x;
     // work item = one part of a tile: parts per tile b.parts (a power of two,
@@ -488,7 +489,7 @@ __global__ void __launch_bounds__(TILE * T, force_min_blocks<PREC, T>()) k_force
                 pv[NV - 2] = de;
                 pv[NV - 1] = dw;
             }
-            last = tile_reduce<NV, true>(b, item, d, st, pv, out, &s_flag, parts);
+            last = tile_reduce<NV, true>(b, item, d, st, pv, out, s_part, &s_flag, parts);
         } else {
             // ---- FP64: the reference's arithmetic
             double fx = 0.0, fy = 0.0, fz = 0.0, e = 0.0, w = 0.0;
@@ -545,7 +546,7 @@ __global__ void __launch_bounds__(TILE * T, force_min_blocks<PREC, T>()) k_force
                     }
                 }
             }
-            last = tile_reduce<NV>(b, item, d, st, pv, out, &s_flag, parts);
+            last = tile_reduce<NV>(b, item, d, st, pv, out, s_part, &s_flag, parts);
         }
         if (last && tid == 0) finish_replica<MODE, NV>(d, st, out, noise);
     }

@@ -312,6 +312,7 @@ void launch_min_iteration_impl(const Batch& b, const LaunchCfg& lc, double dt, d
 template <bool RESCALE_ONLY>
 __global__ void k_kinetic(Batch b)
 {
+    __shared__ double s_part[32];
     __shared__ int s_flag;
     for (int t = blockIdx.x; t < b.ntiles; t += gridDim.x) {
         int r = b.tile_rep[t];
@@ -333,7 +334,7 @@ __global__ void k_kinetic(Batch b)
             v[0] = s;
         }
         double out[1];
-        if (tile_reduce<1>(b, t, d, st, v, out, &s_flag) && threadIdx.x == 0) {
+        if (tile_reduce<1>(b, t, d, st, v, out, s_part, &s_flag) && threadIdx.x == 0) {
             double ekin = dmul(out[0], d.m_half);
             if (RESCALE_ONLY) {
                 double kbt = ddiv(dmul(2.0, ekin), (double)(d.dims * d.n));
@@ -348,6 +349,7 @@ __global__ void k_kinetic(Batch b)
 // apply the pending COM removal / rescale (end of a batch of steps)
 __global__ void k_finalize(Batch b)
 {
+    __shared__ double s_part[32];
     __shared__ int s_flag;
     for (int t = blockIdx.x; t < b.ntiles; t += gridDim.x) {
         int r = b.tile_rep[t];
@@ -364,7 +366,7 @@ __global__ void k_finalize(Batch b)
             if (d.dims == 3) S.vz[i] = dmul(dsub(S.vz[i], st.vmean[2]), vs);
         }
         double v[1] = {0.0}, out[1];
-        if (tile_reduce<1>(b, t, d, st, v, out, &s_flag) && threadIdx.x == 0) {
+        if (tile_reduce<1>(b, t, d, st, v, out, s_part, &s_flag) && threadIdx.x == 0) {
             st.vmean[0] = st.vmean[1] = st.vmean[2] = 0.0;
             st.vscale = 1.0;
         }

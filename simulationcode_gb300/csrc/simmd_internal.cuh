@@ -22,7 +22,7 @@ constexpr int TILE = 128;                       // slots per tile (work unit)
 constexpr int IDX_BITS = 26;
 constexpr unsigned IDX_MASK = (1u << IDX_BITS) - 1u;
 constexpr int MAX_CELLS_AXIS = 1023;
-constexpr int NPART = 8;                        // doubles of partial sums per warp slot
+constexpr int NPART = 8;                        // doubles per partial-sum record
 constexpr int MAX_PARTS = 16;                   // work items per tile in the force pass
 constexpr int MAX_TPP = 8;                      // threads per particle: 1, 2, 4 or 8
 constexpr int WARP_SLOTS = TILE * MAX_TPP / 32; // warp partial-sum slots per tile
@@ -128,7 +128,9 @@ struct Batch {
     int tpp;                      // threads per particle (list interleave)
     int parts;                    // force pass: work items per tile (power of two, <= MAX_PARTS)
     Slots s;
-    double* tile_part;            // [ntiles][WARP_SLOTS][NPART]
+    double* tile_part;            // [ntiles][NPART] tile sums
+    double* warp_part;            // [ntiles][WARP_SLOTS][NPART] warp partials of split tiles
+    int* tile_cnt;                // [ntiles] parts of a split tile done (reset by the last)
     int* queue;                   // work-queue heads [4]
     // rebuild plan: tiles and cells of the replicas rebuilding this step
     int* plan_tiles;              // [ntiles]
