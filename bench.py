@@ -482,7 +482,8 @@ def run_gpu(args, dist):
         from simulationcode_gb300.autotune import autotune
         skins = [float(x) for x in args.tune_skins.split(",")] if args.tune_skins else None
         tune = autotune(batch, tpps=(1, 2, 4, 8), skins=skins,
-                        log=lambda m: print(m, file=sys.stderr, flush=True))
+                        log=lambda m: print(m, file=sys.stderr, flush=True),
+                        group_by=lambda sp: "%dD" % sp.dims)
         args.tpp = tune.tpp
     if not args.graphs:
         batch.set_tuning(args.tpp, False, 16)
@@ -590,6 +591,7 @@ def run_gpu(args, dist):
                        "step_loop": "CUDA graph of 16 steps" if args.graphs else "direct launches",
                        "skin": specs[0].skin,
                        "autotune": None if tune is None else {"tpp": tune.tpp, "skin": tune.skin,
+                                                              "group_skins": tune.group_skins,
                                                               "graph_steps": tune.graph_steps,
                                                               "trials": tune.trials}},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",

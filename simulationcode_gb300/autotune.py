@@ -26,6 +26,7 @@ class TuneResult:
     graph_steps: int
     ms_per_step: float
     trials: list
+    group_skins: dict = dataclasses.field(default_factory=dict)
 
 
 def _may_overflow(batch: ReplicaBatch, skin: float, skin_seen: float, margin: float = 1.15) -> bool:
@@ -42,10 +43,14 @@ def _may_overflow(batch: ReplicaBatch, skin: float, skin_seen: float, margin: fl
 
 
 def autotune(batch: ReplicaBatch, *, tpps: Iterable[int] = (1, 2, 4, 8), skins: Optional[Iterable[float]] = None,
-             graph_steps: Iterable[int] = (16,), warmup: int = 32, steps: int = 96, log=None) -> TuneResult:
-    """Grid search; ``skins`` None keeps the replicas' configured skin.  A
-    skin whose predicted longest list could overflow max_neighbors is
-    skipped (skins are tried in increasing order)."""
+             graph_steps: Iterable[int] = (16,), warmup: int = 32, steps: int = 96, log=None,
+             group_by=None) -> TuneResult:
+    """Grid search over (skin, tpp, graph steps); ``skins`` None keeps the
+    replicas' configured skin.  A skin whose predicted longest list could
+    overflow max_neighbors is skipped (skins are tried in increasing order).
+    ``group_by(spec)``: a second pass tunes the skin of each group of
+    replicas separately (the rebuild cadence that suits 2D replicas differs
+    from 3D)."""
     base_skin = next(iter(batch.specs.values())).skin if batch.specs else 0.3
     skins = [base_skin] if skins is None else sorted(skins)
     skin_seen = base_skin
@@ -71,4 +76,46 @@ def autotune(batch: ReplicaBatch, *, tpps: Iterable[int] = (1, 2, 4, 8), skins: 
     tpp, skin, gs, ms = best
     batch.set_skin(skin)
     batch.set_tuning(tpp, True, gs)
-    return TuneResult(tpp=tpp, skin=skin, graph_steps=gs, ms_per_step=ms, trials=trials)
+    group_skins = {}
+    if group_by is not None and len(skins) > 1:
+        # second pass: the skin of each group of replicas (e.g. 2D and 3D),
+        # the others kept at the best common skin
+        groups = {}
+        for rid, spec in batch.specs.items():
+            groups.setdefault(group_by(spec), []).append(rid)
+        if len(groups) > 1:
+            for key, rids in sorted(groups.items()):
+                gbest = (skin, ms)
+                for sk in skins:
+                    if sk == skin:
+                        continue
+                    if sk > skin and _may_overflow(_Subset(batch, rids), sk, skin):
+                        continue
+                    for rid in rids:
+                        batch.set_skin(sk, rid)
+                    batch.step(warmup)
+                    batch.timer_start()
+                    batch.step(steps)
+                    t = batch.timer_stop() / steps
+                    trials.append({"tpp": tpp, "skin": skin, "group": str(key), "group_skin": sk, "graph_steps": gs,
+                                   "ms_per_step": t})
+                    if log:
+                        log("autotune: group %s skin=%.2f -> %.4f ms/step" % (key, sk, t))
+                    if t < gbest[1]:
+                        gbest = (sk, t)
+                for rid in rids:
+                    batch.set_skin(gbest[0], rid)
+                group_skins[str(key)] = gbest[0]
+                ms = min(ms, gbest[1])
+    return TuneResult(tpp=tpp, skin=skin, graph_steps=gs, ms_per_step=ms, trials=trials, group_skins=group_skins)
+
+
+class _Subset:
+    """the replicas ``rids`` of a batch, for the overflow prediction"""
+
+    def __init__(self, batch, rids):
+        self._b = batch
+        self.specs = {r: batch.specs[r] for r in rids}
+
+    def stats(self, rid):
+        return self._b.stats(rid)
