@@ -111,7 +111,8 @@ struct simmd_ctx {
     RepDesc* d_desc = nullptr;
     RepState* d_state = nullptr;
     int* d_tile_rep = nullptr;
-    double* d_tile_part = nullptr;
+    double* d_red_val = nullptr;
+    int* d_red_cnt = nullptr;
     double* d_warp_part = nullptr;
     int* d_tile_cnt = nullptr;
     int* d_queue = nullptr;
@@ -224,7 +225,7 @@ static int force_rebuild_all(simmd_ctx* c)
 // list 4K; per tile the partial sums, plan and owner; per cell count, start
 // and plan entry; per replica its descriptor and state
 constexpr long long SLOT_BYTES = 32 + 72 + 32 + 12 + 12 + 84 + 8;
-constexpr long long TILE_BYTES = NPART * 8 * (1 + WARP_SLOTS) + 4 + 4 + 4;
+constexpr long long TILE_BYTES = RED_LEVELS * (RED_REC * 8 + 4) + NPART * 8 * WARP_SLOTS + 4 + 4 + 4;
 constexpr long long CELL_BYTES = 4 + 4 + 8;
 
 static long long capacity_bytes(const simmd_ctx* c, long long S, long long C, int R, int K)
@@ -297,7 +298,8 @@ static int ensure_capacity(simmd_ctx* c, long long S_need, long long C_need, int
         TRY(grow_fresh(c, &s.t_orig, S_old, S_new));
         TRY(grow_fresh(c, &c->epp, S_old, S_new));
         long long nt_old = S_old / TILE, nt_new = S_new / TILE;
-        TRY(grow_fresh(c, &c->d_tile_part, nt_old * NPART, nt_new * NPART));
+        TRY(grow_fresh(c, &c->d_red_val, RED_LEVELS * nt_old * RED_REC, RED_LEVELS * nt_new * RED_REC));
+        TRY(grow_fresh(c, &c->d_red_cnt, RED_LEVELS * nt_old, RED_LEVELS * nt_new));
         TRY(grow_fresh(c, &c->d_warp_part, nt_old * NPART * WARP_SLOTS, nt_new * NPART * WARP_SLOTS));
         TRY(grow_fresh(c, &c->d_tile_cnt, nt_old, nt_new));
         TRY(grow_fresh(c, &c->d_plan_tiles, nt_old, nt_new));
@@ -412,7 +414,8 @@ static Batch make_batch(simmd_ctx* c)
     b.tpp = c->T;
     b.parts = force_parts(c);
     b.s = c->s;
-    b.tile_part = c->d_tile_part;
+    b.red_val = c->d_red_val;
+    b.red_cnt = c->d_red_cnt;
     b.warp_part = c->d_warp_part;
     b.tile_cnt = c->d_tile_cnt;
     b.queue = c->d_queue;
@@ -1023,7 +1026,7 @@ static void destroy_ctx(simmd_ctx* c)
     void* ptrs[] = {s.posD, s.vx, s.vy, s.vz, s.fx, s.fy, s.fz, s.ux, s.uy, s.uz, s.rec, s.cellc, s.orig, s.nbr,
                     s.ncnt, s.bin_cell, s.bin_rank, s.src, s.t_posD, s.t_vx, s.t_vy, s.t_vz, s.t_fx, s.t_fy,
                     s.t_fz, s.t_orig, s.cell_count, s.cell_start, c->nbr_full, c->ncnt_full, c->epp, c->d_desc,
-                    c->d_state, c->d_tile_rep, c->d_tile_part, c->d_warp_part, c->d_tile_cnt, c->d_queue, c->d_stage, c->d_dump, c->d_noise,
+                    c->d_state, c->d_tile_rep, c->d_red_val, c->d_red_cnt, c->d_warp_part, c->d_tile_cnt, c->d_queue, c->d_stage, c->d_dump, c->d_noise,
                     c->d_plan_tiles, c->d_plan_cells, c->d_plan_cnt};
     for (void* p : ptrs)
         if (p) cudaFree(p);

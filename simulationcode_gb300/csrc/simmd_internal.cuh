@@ -25,6 +25,8 @@ constexpr int MAX_CELLS_AXIS = 1023;
 constexpr int NPART = 8;                        // doubles per partial-sum record
 constexpr int MAX_PARTS = 16;                   // work items per tile in the force pass
 constexpr int MAX_TPP = 8;                      // threads per particle: 1, 2, 4 or 8
+constexpr int RED_REC = 16;                     // doubles per reduction-tree record (sum, error) x <= 8 values
+constexpr int RED_LEVELS = 4;                   // tree levels: 32^4 tiles >= 2^24 particles
 constexpr int WARP_SLOTS = TILE * MAX_TPP / 32; // warp partial-sum slots per tile
 
 enum { POT_LJ = 0, POT_BERTHIER = 1 };
@@ -128,7 +130,8 @@ struct Batch {
     int tpp;                      // threads per particle (list interleave)
     int parts;                    // force pass: work items per tile (power of two, <= MAX_PARTS)
     Slots s;
-    double* tile_part;            // [ntiles][NPART] tile sums
+    double* red_val;              // [RED_LEVELS][ntiles][RED_REC] reduction tree values (sum, error)
+    int* red_cnt;                 // [RED_LEVELS][ntiles] members of a tree group done (reset by the last)
     double* warp_part;            // [ntiles][WARP_SLOTS][NPART] warp partials of split tiles
     int* tile_cnt;                // [ntiles] parts of a split tile done (reset by the last)
     int* queue;                   // work-queue heads [4]

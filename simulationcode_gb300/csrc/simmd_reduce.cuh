@@ -1,15 +1,17 @@
 // simmd_reduce.cuh -- deterministic per-tile / per-replica reductions.
 //
 // Canonical per-replica reduction: each tile's sum is its warps' partial
-// sums added in warp order; the block that completes a replica's last tile
-// (atomic counter) adds the replica's tile sums in tile order
-// (Neumaier-compensated per lane, then a fixed shuffle tree).  When the
-// force pass splits a tile into parts, each part writes its warps' partials
-// to the tile's warp slots and the block that completes the tile's last part
-// (per-tile counter) forms the tile sum in the same warp order.  The result
-// depends only on the replica's own particles, slot layout and threads per
-// particle -- not on the split, on which block ran which item, or on the
-// other replicas in the batch.
+// sums added in warp order (when the force pass splits a tile into parts,
+// the parts write warp slots and the block completing the tile's last part
+// adds them in that order).  Tile sums are then combined in a fixed tree:
+// groups of 32 consecutive tiles, then groups of 32 group sums, ...; the
+// block that completes a group's last member reduces the group with one
+// warp (compensated: (sum, error) pairs combined with TwoSum in a fixed
+// shuffle tree) and climbs one level.  Every level is one round trip, so a
+// replica of thousands of tiles finishes in a few, not in one warp's walk
+// over all tiles.  The result depends only on the replica's own particles,
+// slot layout and threads per particle -- not on the split, on which block
+// ran which item, or on the other replicas in the batch.
 #pragma once
 #include "simmd_internal.cuh"
 
@@ -24,11 +26,29 @@ __device__ __forceinline__ void warp_sum(double (&v)[NV])
         for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_xor_sync(0xffffffffu, v[k], o);
 }
 
-__device__ __forceinline__ void neumaier_add(double& s, double& c, double x)
+// s + e == a + b exactly (Knuth); e is the same whatever the operand order
+__device__ __forceinline__ void two_sum(double a, double b, double& s, double& e)
 {
-    const double t = s + x;
-    c += (fabs(s) >= fabs(x)) ? (s - t) + x : (x - t) + s;
-    s = t;
+    s = a + b;
+    const double bp = s - a;
+    e = (a - (s - bp)) + (b - bp);
+}
+
+// compensated warp reduction of (s, c) pairs, every lane gets the total
+template <int NV>
+__device__ __forceinline__ void warp_sum_comp(double (&s)[NV], double (&c)[NV])
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+        for (int k = 0; k < NV; k++) {
+            const double s2 = __shfl_xor_sync(0xffffffffu, s[k], o);
+            const double c2 = __shfl_xor_sync(0xffffffffu, c[k], o);
+            double t, e;
+            two_sum(s[k], s2, t, e);
+            s[k] = t;
+            c[k] = (c[k] + c2) + e;
+        }
 }
 
 // Returns true in the threads of the block that must finalise the replica;
@@ -55,6 +75,8 @@ __device__ bool tile_reduce(const Batch& b, int item, const RepDesc& d, RepState
         }
     }
     __syncthreads();
+    // ---- the tile's sum (level 0 of the tree), by thread 0 of the block
+    // that completes the tile
     if (tid == 0) {
         bool tile_done = true;
         double ts[NV];
@@ -79,37 +101,67 @@ __device__ bool tile_reduce(const Batch& b, int item, const RepDesc& d, RepState
                 b.tile_cnt[t] = 0;
             }
         }
-        int last = 0;
         if (tile_done) {
-            for (int k = 0; k < NV; k++) b.tile_part[(size_t)t * NPART + k] = ts[k];
-            __threadfence();
-            last = atomicAdd(&st.done_count, 1) == d.ntiles - 1;
-        }
-        *s_flag = last;
-    }
-    __syncthreads();
-    const bool last = *s_flag;
-    if (last) {
-        __threadfence();
-        if (wid == 0) {
-            double s[NV], c[NV];
-#pragma unroll
-            for (int k = 0; k < NV; k++) { s[k] = 0.0; c[k] = 0.0; }
-            for (int q = lane; q < d.ntiles; q += 32) {
-                const double* tp = b.tile_part + (size_t)(d.tile0 + q) * NPART;
-#pragma unroll
-                for (int k = 0; k < NV; k++) neumaier_add(s[k], c[k], __ldcg(tp + k));
+            double* dst = b.red_val + (size_t)t * RED_REC;
+            for (int k = 0; k < NV; k++) {
+                dst[k] = ts[k];
+                dst[NV + k] = 0.0;
             }
+        }
+        *s_flag = tile_done ? 1 : 0;
+    }
+    __syncthreads();
+    bool last = false;
+    // ---- climb the tree with warp 0
+    if (wid == 0 && *s_flag) {
+        int idx = t - d.tile0, n = d.ntiles;
+        double s[NV], c[NV];
+        if (n == 1) {  // a one-tile replica: its tile sum is the total
+            const double* src = b.red_val + (size_t)t * RED_REC;
 #pragma unroll
-            for (int k = 0; k < NV; k++) s[k] += c[k];
-            warp_sum<NV>(s);
+            for (int k = 0; k < NV; k++) { s[k] = src[k]; c[k] = 0.0; }
+            last = true;
+        }
+        for (int level = 0; n > 1; level++) {
+            const int g = idx >> 5, first = g << 5, m = min(32, n - first);
+            int prev = 0;
+            if (lane == 0) {
+                __threadfence();
+                prev = atomicAdd(&b.red_cnt[(size_t)level * b.ntiles + d.tile0 + g], 1);
+            }
+            prev = __shfl_sync(0xffffffffu, prev, 0);
+            if (prev != m - 1) break;  // another block completes this group
+            __threadfence();
+            const double* src = b.red_val + ((size_t)level * b.ntiles + d.tile0 + first) * RED_REC;
 #pragma unroll
-            for (int k = 0; k < NV; k++) out[k] = s[k];
-            if (lane == 0) st.done_count = 0;
+            for (int k = 0; k < NV; k++) {
+                s[k] = lane < m ? __ldcg(src + (size_t)lane * RED_REC + k) : 0.0;
+                c[k] = lane < m ? __ldcg(src + (size_t)lane * RED_REC + NV + k) : 0.0;
+            }
+            warp_sum_comp<NV>(s, c);
+            if (lane == 0) b.red_cnt[(size_t)level * b.ntiles + d.tile0 + g] = 0;
+            idx = g;
+            n = (n + 31) >> 5;
+            if (n == 1) {
+                last = true;
+            } else if (lane == 0) {
+                double* dst = b.red_val + ((size_t)(level + 1) * b.ntiles + d.tile0 + g) * RED_REC;
+#pragma unroll
+                for (int k = 0; k < NV; k++) {
+                    dst[k] = s[k];
+                    dst[NV + k] = c[k];
+                }
+            }
+        }
+        if (last && lane == 0) {
+#pragma unroll
+            for (int k = 0; k < NV; k++) out[k] = s[k] + c[k];
         }
     }
     __syncthreads();
-    return last;
+    if (tid == 0) *s_flag = last ? 1 : 0;
+    __syncthreads();
+    return *s_flag != 0;
 }
 
 }  // namespace simmd
