@@ -1,0 +1,81 @@
+"""Autotuner selection logic against a fake batch (no device): it picks the
+fastest (tpp, skin), skips skins whose predicted lists overflow
+max_neighbors, and tunes each replica group's skin in a second pass."""
+import numpy as np
+
+from simulationcode_gb300.autotune import autotune
+from simulationcode_gb300.batch import ReplicaSpec
+
+
+class Stats:
+    def __init__(self, max_count):
+        self.max_count = max_count
+
+
+class FakeBatch:
+    """step time = sum over replicas of a cost that depends on its skin and
+    the batch's threads per particle; lists grow with the skin"""
+
+    def __init__(self, specs, best2d, best3d, max_count=40):
+        self.specs = dict(enumerate(specs))
+        self.skin = {r: s.skin for r, s in self.specs.items()}
+        self.tpp = 1
+        self.best = {2: best2d, 3: best3d}
+        self.base_count = max_count
+        self.t = 0.0
+        self.calls = []
+
+    def set_skin(self, skin, rid=-1):
+        for r in self.specs:
+            if rid in (-1, r):
+                self.skin[r] = skin
+                self.specs[r].skin = skin
+
+    def set_tuning(self, tpp, graphs=True, graph_steps=16):
+        self.tpp = tpp
+
+    def _ms(self):
+        ms = 0.0
+        for r, s in self.specs.items():
+            ms += 1.0 + 5.0 * (self.skin[r] - self.best[s.dims]) ** 2
+        return ms * (1.0 + 0.1 * abs(np.log2(self.tpp) - 1))   # tpp 2 best
+
+    def step(self, n):
+        self.t += n * self._ms()
+
+    def timer_start(self):
+        self.t = 0.0
+
+    def timer_stop(self):
+        return self.t
+
+    def stats(self, rid):
+        s = self.specs[rid]
+        rcs = s.verlet_force_cutoff * float(np.max(s.D))
+        return Stats(int(self.base_count * ((rcs + self.skin[rid]) / (rcs + 0.3)) ** s.dims))
+
+
+def spec(dims, K=96):
+    N = 64
+    return ReplicaSpec(dims=dims, potential=1, dynamics=2, N=N, box_size=10.0, force_cutoff2=1.5625, skin=0.3,
+                       verlet_force_cutoff=1.25, r=np.zeros((N, dims)), D=np.full(N, 1.2), max_neighbors=K)
+
+
+def test_picks_fastest_and_tunes_groups():
+    b = FakeBatch([spec(2), spec(3), spec(2), spec(3)], best2d=0.7, best3d=0.5)
+    res = autotune(b, tpps=(1, 2, 4), skins=[0.3, 0.4, 0.5, 0.6, 0.7], warmup=1, steps=2,
+                   group_by=lambda s: "%dD" % s.dims)
+    assert res.tpp == 2
+    assert res.skin == 0.6                       # best common skin for the mix
+    assert res.group_skins == {"2D": 0.7, "3D": 0.5}
+    assert [b.skin[r] for r in range(4)] == [0.7, 0.5, 0.7, 0.5]
+
+
+def test_overflowing_skins_are_skipped():
+    # 3D lists at skin 0.3 already near max_neighbors: larger skins would overflow
+    b = FakeBatch([spec(3, K=48), spec(3, K=48)], best2d=0.7, best3d=0.7, max_count=40)
+    seen = []
+    res = autotune(b, tpps=(1,), skins=[0.3, 0.5, 0.7], warmup=1, steps=2, log=seen.append)
+    assert res.skin == 0.3
+    assert any("skipped" in m for m in seen)
+    assert all(t["skin"] == 0.3 for t in res.trials)
