@@ -562,6 +562,10 @@ static int fill_desc_smax(const simmd_params* p, double smax, RepDesc& d)
     d.Lhi_f = (float)Lhi;
     d.Llo_f = (float)(L - Lhi);
     d.rv2f = (float)d.rv2;
+    // build candidates are relative to a grid point within h/2 of the home
+    // cell centre: a home particle and a stencil candidate differ by at most
+    // 2 cs + h per axis, which needs no minimum image below L/2
+    d.build_wrap = (nc >= 3 && 2.0 * d.cs + hg + 1e-3 < 0.5 * L) ? 0 : 1;
     return SIMMD_OK;
 }
 

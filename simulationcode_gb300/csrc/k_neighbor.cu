@@ -273,7 +273,7 @@ struct BuildSmem {
     int maxcnt;
 };
 
-template <int DIM, bool FULL>
+template <int DIM, bool FULL, bool WRAP>
 __device__ void build_cell(const Batch& b, const RepDesc& d, RepState& st, int c, BuildSmem& sm,
                            unsigned* nbr_full, int* ncnt_full, int Kfull)
 {
@@ -357,11 +357,11 @@ __device__ void build_cell(const Batch& b, const RepDesc& d, RepState& st, int c
                     const int j = sm.slot[q];
                     if (j != (int)i) {
                         const float4 oj = sm.o[q];
-                        const float dxf = min_image_f32(oi.x - oj.x, d.halfLf, d.Lf);
-                        const float dyf = min_image_f32(oi.y - oj.y, d.halfLf, d.Lf);
+                        const float dxf = WRAP ? min_image_f32(oi.x - oj.x, d.halfLf, d.Lf) : oi.x - oj.x;
+                        const float dyf = WRAP ? min_image_f32(oi.y - oj.y, d.halfLf, d.Lf) : oi.y - oj.y;
                         float d2f = dxf * dxf + dyf * dyf;
                         if (DIM == 3) {
-                            const float dzf = min_image_f32(oi.z - oj.z, d.halfLf, d.Lf);
+                            const float dzf = WRAP ? min_image_f32(oi.z - oj.z, d.halfLf, d.Lf) : oi.z - oj.z;
                             d2f += dzf * dzf;
                         }
                         // FP32 classification against the reference thresholds with a
@@ -444,12 +444,15 @@ __global__ void __launch_bounds__(BLD_THREADS) k_rb_build(Batch b, unsigned* nbr
             sm.maxcnt = 0;
         }
         __syncthreads();
-        if (d.dims == 3) {
-            if (nbr_full) build_cell<3, true>(b, d, st, task.y, sm, nbr_full, ncnt_full, Kfull);
-            else build_cell<3, false>(b, d, st, task.y, sm, nbr_full, ncnt_full, Kfull);
+        if (nbr_full) {  // parity-test mode: the full list as well
+            if (d.dims == 3) build_cell<3, true, true>(b, d, st, task.y, sm, nbr_full, ncnt_full, Kfull);
+            else build_cell<2, true, true>(b, d, st, task.y, sm, nbr_full, ncnt_full, Kfull);
+        } else if (d.build_wrap) {
+            if (d.dims == 3) build_cell<3, false, true>(b, d, st, task.y, sm, nbr_full, ncnt_full, Kfull);
+            else build_cell<2, false, true>(b, d, st, task.y, sm, nbr_full, ncnt_full, Kfull);
         } else {
-            if (nbr_full) build_cell<2, true>(b, d, st, task.y, sm, nbr_full, ncnt_full, Kfull);
-            else build_cell<2, false>(b, d, st, task.y, sm, nbr_full, ncnt_full, Kfull);
+            if (d.dims == 3) build_cell<3, false, false>(b, d, st, task.y, sm, nbr_full, ncnt_full, Kfull);
+            else build_cell<2, false, false>(b, d, st, task.y, sm, nbr_full, ncnt_full, Kfull);
         }
         __syncthreads();
         if (threadIdx.x == 0 && sm.entries) {

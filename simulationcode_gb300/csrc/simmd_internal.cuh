@@ -52,7 +52,7 @@ struct RepDesc {
     double wrap_hi;            // smallest x with RN(x/L) >= 1: floor(x/L) without a divide
     double inv_two_m;          // 1/(2m), used when 2m is a power of two (exact)
     int two_m_pow2;
-    int pad2_;
+    int build_wrap;            // 0: stencil candidates never need the minimum image (2 cs + h < L/2)
     // split precision: FP32 offsets from a power-of-two grid h (exact integer shifts)
     double h, inv_h;
     float hf, Lhi_f, Llo_f, rv2f;
