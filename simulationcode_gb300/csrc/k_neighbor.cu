@@ -431,6 +431,10 @@ __device__ void build_cell(const Batch& b, const RepDesc& d, RepState& st, int c
     __syncthreads();
 }
 
+// one block per cell task of the plan; FULL: the full (Verlet) list as well
+// (parity tests), kept in its own kernel so the production kernel's register
+// budget is that of the half list alone
+template <bool FULL>
 __global__ void __launch_bounds__(BLD_THREADS) k_rb_build(Batch b, unsigned* nbr_full, int* ncnt_full, int Kfull)
 {
     __shared__ BuildSmem sm;
@@ -444,7 +448,7 @@ __global__ void __launch_bounds__(BLD_THREADS) k_rb_build(Batch b, unsigned* nbr
             sm.maxcnt = 0;
         }
         __syncthreads();
-        if (nbr_full) {  // parity-test mode: the full list as well
+        if (FULL) {
             if (d.dims == 3) build_cell<3, true, true>(b, d, st, task.y, sm, nbr_full, ncnt_full, Kfull);
             else build_cell<2, true, true>(b, d, st, task.y, sm, nbr_full, ncnt_full, Kfull);
         } else if (d.build_wrap) {
@@ -516,7 +520,8 @@ void launch_rebuild_body_impl(const Batch& b, const LaunchCfg& lc, unsigned* nbr
     k_rb_scatter<<<g, TILE, 0, lc.stream>>>(b);
     k_rb_cellsort<<<g, TILE, 0, lc.stream>>>(b);
     k_rb_gather<<<g, TILE, 0, lc.stream>>>(b, ncnt_full);
-    k_rb_build<<<g, BLD_THREADS, 0, lc.stream>>>(b, nbr_full, ncnt_full, Kfull);
+    if (nbr_full) k_rb_build<true><<<g, BLD_THREADS, 0, lc.stream>>>(b, nbr_full, ncnt_full, Kfull);
+    else k_rb_build<false><<<g, BLD_THREADS, 0, lc.stream>>>(b, nullptr, nullptr, 0);
     k_rb_copyback<<<g, TILE, 0, lc.stream>>>(b);
     k_rb_done<<<(b.nreps + 127) / 128, 128, 0, lc.stream>>>(b);
     if (lc.launches) *lc.launches += 8;
