@@ -75,45 +75,52 @@ __device__ bool tile_reduce(const Batch& b, int item, const RepDesc& d, RepState
         }
     }
     __syncthreads();
-    // ---- the tile's sum (level 0 of the tree), by thread 0 of the block
-    // that completes the tile
+    // ---- the tile's sum (level 0 of the tree), by warp 0 of the block that
+    // completes the tile (the warp partials added in warp order)
     if (tid == 0) {
-        bool tile_done = true;
+        int done = 1;
+        if (parts > 1) {
+            __threadfence();  // after the barrier: publishes every warp's slot
+            done = atomicAdd(&b.tile_cnt[t], 1) == parts - 1;
+            if (done) b.tile_cnt[t] = 0;
+        }
+        *s_flag = done;
+    }
+    __syncthreads();
+    if (wid == 0 && *s_flag) {
         double ts[NV];
         if (parts == 1) {
+#pragma unroll
             for (int k = 0; k < NV; k++) {
                 double s = 0.0;
                 for (int w = 0; w < nw; w++) s += s_part[w * NV + k];
                 ts[k] = s;
             }
         } else {
-            __threadfence();  // after the barrier: publishes every warp's slot
-            tile_done = atomicAdd(&b.tile_cnt[t], 1) == parts - 1;
-            if (tile_done) {
-                __threadfence();
-                const double* slot = b.warp_part + (size_t)t * WARP_SLOTS * NPART;
-                const int wpt = nw * parts;
-                for (int k = 0; k < NV; k++) {
-                    double s = 0.0;
-                    for (int w = 0; w < wpt; w++) s += __ldcg(slot + (size_t)w * NPART + k);
-                    ts[k] = s;
-                }
-                b.tile_cnt[t] = 0;
+            __threadfence();
+            const int wpt = nw * parts;  // <= 32
+            const double* slot = b.warp_part + (size_t)t * WARP_SLOTS * NPART;
+#pragma unroll
+            for (int k = 0; k < NV; k++) {
+                const double x = lane < wpt ? __ldcg(slot + (size_t)lane * NPART + k) : 0.0;
+                double s = 0.0;
+                for (int w = 0; w < wpt; w++) s += __shfl_sync(0xffffffffu, x, w);
+                ts[k] = s;
             }
         }
-        if (tile_done) {
+        if (lane == 0) {
             double* dst = b.red_val + (size_t)t * RED_REC;
+#pragma unroll
             for (int k = 0; k < NV; k++) {
                 dst[k] = ts[k];
                 dst[NV + k] = 0.0;
             }
         }
-        *s_flag = tile_done ? 1 : 0;
     }
-    __syncthreads();
     bool last = false;
     // ---- climb the tree with warp 0
     if (wid == 0 && *s_flag) {
+        __syncwarp();  // lane 0's tile sum visible to the warp
         int idx = t - d.tile0, n = d.ntiles;
         double s[NV], c[NV];
         if (n == 1) {  // a one-tile replica: its tile sum is the total
