@@ -191,29 +191,7 @@ def build_batch(specs, device, tpp):
     return b, ids
 
 
-def relax_specs(specs, device, steps=300, step_size=1e-3, cap=0.05):
-    """Set-up relaxation on the GPU in FP64; returns relaxed positions."""
-    from simulationcode_gb300 import _lib
-    import copy
-    tmp = []
-    for s in specs:
-        t = copy.copy(s)
-        t.precision = _lib.FP64
-        tmp.append(t)
-    b, ids = build_batch(tmp, device, 1)
-    b.rebuild()
-    b.relax(steps, step_size, cap)
-    out = [b.state(i)[0] for i in ids]
-    fmax = max(float(np.abs(b.state(i)[2]).max()) for i in ids[:64])
-    print("relaxed: max |F| over the first replicas %.3g" % fmax, file=sys.stderr, flush=True)
-    relax_launches[0] += b.launches()
-    kc = b.kernel_counts()
-    relax_counts[0] += kc[0]
-    relax_counts[1] += kc[1]
-    b.close()
-    return out
-
-
+# kernel launches of the set-up relaxation (for ncu --launch-skip counts)
 relax_launches = [0]
 relax_counts = [0, 0]
 
@@ -470,9 +448,11 @@ def run_gpu(args, dist):
     specs = rank_specs(args.workload, dist.rank, prec)
     # set-up: relax random starts on the GPU (not timed)
     if any(s.potential == _lib.POT_BERTHIER for s in specs) and args.relax_steps > 0:
-        rel = relax_specs(specs, device, steps=args.relax_steps)
-        for s, r in zip(specs, rel):
-            s.r = r
+        fmax, counts = W.relax_on_device(specs, device, steps=args.relax_steps)
+        print("relaxed: max |F| %.3g" % fmax, file=sys.stderr, flush=True)
+        relax_launches[0] += counts[0]
+        relax_counts[0] += counts[1]
+        relax_counts[1] += counts[2]
     batch, ids = build_batch(specs, device, args.tpp)
     if args.skin is not None:
         batch.set_skin(args.skin)
