@@ -344,10 +344,15 @@ __device__ __forceinline__ void finish_replica(const RepDesc& d, RepState& st, c
 #ifndef SIMMD_F32_MINB
 #define SIMMD_F32_MINB 12
 #endif
+#ifndef SIMMD_F64_MINB
+#define SIMMD_F64_MINB 4
+#endif
 template <int PREC, int T>
 constexpr int force_min_blocks()
 {
-    return ((PREC == PREC_FP32 ? SIMMD_F32_MINB : 4) / T) > 0 ? (PREC == PREC_FP32 ? SIMMD_F32_MINB : 4) / T : 1;
+    return ((PREC == PREC_FP32 ? SIMMD_F32_MINB : SIMMD_F64_MINB) / T) > 0
+               ? (PREC == PREC_FP32 ? SIMMD_F32_MINB : SIMMD_F64_MINB) / T
+               : 1;
 }
 
 template <int MODE, int PREC, int T>
