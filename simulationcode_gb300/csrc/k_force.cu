@@ -200,16 +200,15 @@ __device__ __forceinline__ void pairs_f32(const Batch& b, const RepDesc& d, long
 #pragma unroll
         for (int u = 0; u < PAIR_UNROLL; u++) j[u] = list_entry<T>(b, s_rows, nrows, i, pl, ppb, n + u * T);
 #pragma unroll
-        for (int u = 0; u < PAIR_UNROLL; u++) {
-            o[u] = __ldg(&rec[j[u]].o);
-            g[u] = __ldg(&rec[j[u]].g);
-        }
+        for (int u = 0; u < PAIR_UNROLL; u++) rec_get(rec + j[u], o[u], g[u]);
 #pragma unroll
         for (int u = 0; u < PAIR_UNROLL; u++) pair_f32<DIM, POT, EN>(d, oi, gi, o[u], g[u], fx, fy, fz, e, w);
     }
     for (; n < cnt; n += T) {
         const unsigned j0 = list_entry<T>(b, s_rows, nrows, i, pl, ppb, n);
-        pair_f32<DIM, POT, EN>(d, oi, gi, __ldg(&rec[j0].o), __ldg(&rec[j0].g), fx, fy, fz, e, w);
+        float4 o0, g0;
+        rec_get(rec + j0, o0, g0);
+        pair_f32<DIM, POT, EN>(d, oi, gi, o0, g0, fx, fy, fz, e, w);
     }
 }
 

@@ -201,6 +201,24 @@ __device__ __forceinline__ float split_dx(float oi, float oj, int mi, int mj, co
     return (a - s * d.Llo_f) + (G0 - s * d.Lhi_f);
 }
 
+// one 256-bit read-only load of a neighbour's record (sm_100 and later):
+// the record is one sector, so a warp's gather costs one request per lane
+// instead of two
+#ifndef SIMMD_REC_V8
+#define SIMMD_REC_V8 1
+#endif
+__device__ __forceinline__ void rec_get(const SplitRec* __restrict__ r, float4& o, float4& g)
+{
+#if SIMMD_REC_V8
+    asm("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+        : "=f"(o.x), "=f"(o.y), "=f"(o.z), "=f"(o.w), "=f"(g.x), "=f"(g.y), "=f"(g.z), "=f"(g.w)
+        : "l"(r));
+#else
+    o = __ldg(&r->o);
+    g = __ldg(&r->g);
+#endif
+}
+
 __device__ __forceinline__ void rec_put(SplitRec* r, float4 o, float4 g)
 {
     r->o = o;
