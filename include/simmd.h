@@ -257,6 +257,12 @@ int simmd_set_profile(simmd_ctx* ctx, int32_t enable);
 int simmd_host_register(void* ptr, int64_t bytes);
 int simmd_host_unregister(void* ptr);
 int simmd_profile_get(simmd_ctx* ctx, double* out6);
+/* self-check of the split-precision kernels' float <-> double conversions
+ * (bit operations on the integer pipes) against the hardware converter on
+ * the current device: n hashed float and double bit patterns (all classes,
+ * rounding ties, the float range edges); *mismatches = patterns whose result
+ * bits differ.  No context needed. */
+int simmd_check_conversions(int64_t n, uint64_t seed, int64_t* mismatches);
 
 #ifdef __cplusplus
 }

@@ -46,6 +46,7 @@ void launch_store_aos_impl(const Batch& b, const LaunchCfg& lc, int rep, const R
                            double* v, double* F, double* disp, const double* epp_src, double* epp);
 void launch_set_state_impl(const Batch& b, const LaunchCfg& lc, int rep, const RepDesc& hd, const double* r,
                            const double* v, const double* F, const double* disp);
+void launch_check_conversions_impl(long long n, unsigned long long seed, unsigned long long* bad, cudaStream_t s);
 }  // namespace simmd
 
 using namespace simmd;
@@ -538,6 +539,8 @@ static int fill_desc_smax(const simmd_params* p, double smax, RepDesc& d)
     d.c2f = (float)d.c2;
     d.c4f = (float)d.c4;
     d.zetaf = (float)d.zeta;
+    d.noisef = (float)d.noise_factor;
+    d.gammaf = (float)d.gamma;
     d.seed = p->seed;
     // floor(rnew/L) of the wrap (src/MD.jl:520) without a divide: RN(x/L) >= 1
     // exactly when x >= wrap_hi (found with IEEE host division)
@@ -552,6 +555,7 @@ static int fill_desc_smax(const simmd_params* p, double smax, RepDesc& d)
     double mant = std::frexp(d.two_m, &ex);
     d.two_m_pow2 = (mant == 0.5) ? 1 : 0;
     d.inv_two_m = 1.0 / d.two_m;
+    d.dt_over_two_m = d.dt * d.inv_two_m;
     // split-precision offset grid: the smallest power of two >= max(1/2, L/1022)
     double hg = 0.5;
     while (L / hg > 1022.0) hg *= 2.0;
@@ -1745,6 +1749,24 @@ int simmd_profile_get(simmd_ctx* c, double* out6)
     out6[3] = c->prof.rebuild_ms;
     out6[4] = c->prof.update_ms;
     out6[5] = (double)c->prof.steps;
+    return SIMMD_OK;
+}
+
+int simmd_check_conversions(int64_t n, uint64_t seed, int64_t* mismatches)
+{
+    if (!mismatches || n < 0) return set_err(SIMMD_ERR_BAD_ARG, "bad argument");
+    unsigned long long* d_bad = nullptr;
+    CK(cudaMalloc(&d_bad, sizeof(unsigned long long)));
+    unsigned long long h_bad = 0;
+    cudaError_t e = cudaMemset(d_bad, 0, sizeof(unsigned long long));
+    if (e == cudaSuccess) {
+        launch_check_conversions_impl(n, seed, d_bad, 0);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpy(&h_bad, d_bad, sizeof(h_bad), cudaMemcpyDeviceToHost);
+    cudaFree(d_bad);
+    if (e != cudaSuccess) return set_err(SIMMD_ERR_CUDA, std::string("conversion check: ") + cudaGetErrorString(e));
+    *mismatches = (int64_t)h_bad;
     return SIMMD_OK;
 }
 

@@ -212,11 +212,12 @@ __device__ __forceinline__ void pairs_f32(const Batch& b, const RepDesc& d, long
     }
 }
 
-// v + dt*F/(2m); the divide is an exact scaling when 2m is a power of two
+// v + dt*F/(2m).  When 2m is a power of two the divide is an exact scaling,
+// so RN(dt*F)/(2m) == RN((dt/(2m))*F) and one multiply does both
 __device__ __forceinline__ double kick(double v, double F, const RepDesc& d)
 {
-    const double t = dmul(d.dt, F);
-    return dadd(v, d.two_m_pow2 ? dmul(t, d.inv_two_m) : ddiv(t, d.two_m));
+    if (d.two_m_pow2) return dadd(v, dmul(d.dt_over_two_m, F));
+    return dadd(v, ddiv(dmul(d.dt, F), d.two_m));
 }
 
 // N(0,1) deviates of this particle for the current noise step: the host
@@ -413,7 +414,7 @@ __global__ void __launch_bounds__(TILE * T, force_min_blocks<PREC, T>()) k_force
             if (T > 1) combine_lanes<float, T, EN>(fx, fy, fz, e, w);
             float q0 = 0.f, q1 = 0.f, q2 = 0.f;  // per-particle contribution to the replica sums
             if (sub == 0 && real) {
-                if (EN && epp) epp[i] = (double)e / 2.0;
+                if (EN && epp) epp[i] = f2d(e) * 0.5;
                 if (MODE != FMODE_ENERGY) {
                     double vx = 0.0, vy = 0.0, vz = 0.0;
                     if (nl) {
@@ -422,7 +423,7 @@ __global__ void __launch_bounds__(TILE * T, force_min_blocks<PREC, T>()) k_force
                         if (d.dims == 3) vz = b.s.vz[i];
                     }
                     if (noise) {
-                        const float nf = (float)d.noise_factor;
+                        const float nf = d.noisef;
                         float z0, z1, z2 = 0.f, zz;
                         if (d.noise_mode == NOISE_HOST) {
                             double x0, x1, x2;
@@ -437,13 +438,13 @@ __global__ void __launch_bounds__(TILE * T, force_min_blocks<PREC, T>()) k_force
                         fy += nf * z1;
                         fz += nf * z2;
                         if (d.dyn == DYN_LANGEVIN) {
-                            const float mg = -(float)d.gamma;
-                            fx += mg * (float)vx;
-                            fy += mg * (float)vy;
-                            fz += mg * (float)vz;
+                            const float mg = -d.gammaf;
+                            fx += mg * d2f_rn(vx);
+                            fy += mg * d2f_rn(vy);
+                            fz += mg * d2f_rn(vz);
                         }
                     }
-                    const double Fx = fx, Fy = fy, Fz = fz;
+                    const double Fx = f2d(fx), Fy = f2d(fy), Fz = f2d(fz);
                     b.s.fx[i] = Fx;
                     b.s.fy[i] = Fy;
                     if (d.dims == 3) b.s.fz[i] = Fz;
@@ -457,9 +458,9 @@ __global__ void __launch_bounds__(TILE * T, force_min_blocks<PREC, T>()) k_force
                                 vz = kick(vz, Fz, d);
                                 b.s.vz[i] = vz;
                             }
-                            q0 = (float)vx;
-                            q1 = (float)vy;
-                            q2 = (float)vz;
+                            q0 = d2f_rn(vx);
+                            q1 = d2f_rn(vy);
+                            q2 = d2f_rn(vz);
                         } else {
                             q0 = fx;
                             q1 = fy;
@@ -478,13 +479,13 @@ __global__ void __launch_bounds__(TILE * T, force_min_blocks<PREC, T>()) k_force
                     q2 += __shfl_xor_sync(0xffffffffu, q2, o);
                 }
                 if ((tid & 31) == 0) {  // only lane 0's value is read (WARP_DONE)
-                    pv[0] = q0;
-                    pv[1] = q1;
-                    pv[2] = q2;
+                    pv[0] = f2d(q0);
+                    pv[1] = f2d(q1);
+                    pv[2] = f2d(q2);
                 }
             }
             if (EN) {
-                double de = (sub == 0 && real) ? (double)e : 0.0, dw = (sub == 0 && real) ? (double)w : 0.0;
+                double de = (sub == 0 && real) ? f2d(e) : 0.0, dw = (sub == 0 && real) ? f2d(w) : 0.0;
 #pragma unroll
                 for (int o = 16; o > 0; o >>= 1) {
                     de += __shfl_xor_sync(0xffffffffu, de, o);

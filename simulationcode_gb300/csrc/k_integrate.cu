@@ -36,8 +36,8 @@ __device__ __forceinline__ double wrap_coord(double x, const RepDesc& d)
 // its rebuild) is decided in FP32 and redone in FP64 only then
 __device__ __forceinline__ float offset_refresh(double x, float g, const RepDesc& d)
 {
-    const double o = dsub(x, (double)g);  // exact: g = m*h and |x - g| small
-    const float of = (float)o;
+    const double o = dsub(x, f2d(g));  // exact: g = m*h and |x - g| small
+    const float of = d2f_rn(o);
     if (fabsf(of) < d.halfLf * 0.9f) return of;
     double q = o;  // crossed the periodic boundary since the rebuild
     q = (q > d.halfL) ? q - d.L : q;
@@ -45,10 +45,11 @@ __device__ __forceinline__ float offset_refresh(double x, float g, const RepDesc
     return (float)q;
 }
 
+// v + dt*F/(2m); one multiply when 2m is a power of two (exact scaling)
 __device__ __forceinline__ double half_kick(double v, double F, const RepDesc& d)
 {
-    const double t = dmul(d.dt, F);
-    return dadd(v, d.two_m_pow2 ? dmul(t, d.inv_two_m) : ddiv(t, d.two_m));
+    if (d.two_m_pow2) return dadd(v, dmul(d.dt_over_two_m, F));
+    return dadd(v, ddiv(dmul(d.dt, F), d.two_m));
 }
 
 // r += dr with the reference wrap rnew - floor(rnew/L)*L, displacement update,
@@ -85,7 +86,7 @@ __device__ __forceinline__ double drift_slot(const Batch& b, const RepDesc& d, l
 __device__ __forceinline__ void block_max_to_state(double u2, RepState& st, unsigned long long* s_max)
 {
     unsigned long long bits = (unsigned long long)__double_as_longlong(u2);
-    if (!(u2 == u2) || isinf(u2)) {
+    if (nonfinite_bits(u2)) {
         st.nonfinite = 1;
         bits = 0x7ff0000000000000ull;
     }
@@ -120,15 +121,22 @@ __global__ void k_kick_drift(Batch b)
         if (i < d.slot0 + d.n) {
             const Slots& S = b.s;
             const double vs = st.vscale;
-            double vx = dmul(dsub(S.vx[i], st.vmean[0]), vs);
-            double vy = dmul(dsub(S.vy[i], st.vmean[1]), vs);
+            // the rescale multiply only when a rescale is pending (x * 1.0 == x)
+            const bool scale = __double_as_longlong(vs) != 0x3ff0000000000000ll;
+            double vx = dsub(S.vx[i], st.vmean[0]);
+            double vy = dsub(S.vy[i], st.vmean[1]);
+            if (scale) {
+                vx = dmul(vx, vs);
+                vy = dmul(vy, vs);
+            }
             vx = half_kick(vx, S.fx[i], d);
             vy = half_kick(vy, S.fy[i], d);
             S.vx[i] = vx;
             S.vy[i] = vy;
             double vz = 0.0;
             if (d.dims == 3) {
-                vz = dmul(dsub(S.vz[i], st.vmean[2]), vs);
+                vz = dsub(S.vz[i], st.vmean[2]);
+                if (scale) vz = dmul(vz, vs);
                 vz = half_kick(vz, S.fz[i], d);
                 S.vz[i] = vz;
             }
@@ -371,6 +379,48 @@ __global__ void k_finalize(Batch b)
             st.vscale = 1.0;
         }
     }
+}
+
+// ---------------------------------------------------------------------------
+// self-check: f2d / d2f_rn against the converter, bit for bit
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ unsigned long long mix64(unsigned long long x)
+{
+    x ^= x >> 30;
+    x *= 0xbf58476d1ce4e5b9ull;
+    x ^= x >> 27;
+    x *= 0x94d049bb133111ebull;
+    return x ^ (x >> 31);
+}
+
+__global__ void k_check_conversions(long long n, unsigned long long seed, unsigned long long* bad)
+{
+    unsigned long long nbad = 0;
+    for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x) {
+        const unsigned long long h = mix64(seed + 0x9e3779b97f4a7c15ull * (unsigned long long)(k + 1));
+        // widening: any float pattern
+        const float f = __uint_as_float((unsigned)h);
+        if (__double_as_longlong(f2d(f)) != __double_as_longlong((double)f)) nbad++;
+        // narrowing: a double in the float range (exponent drawn over it and
+        // a little beyond), the dropped bits often a tie or next to one
+        unsigned long long b = h;
+        const unsigned long long ef = 880ull + ((h >> 52) % 288ull);
+        b = (b & 0x800fffffffffffffull) | (ef << 52);
+        const int kind = (int)((h >> 40) & 7ull);
+        if (kind == 0) b = (b & ~0x1fffffffull) | 0x10000000ull;          // exact tie
+        else if (kind == 1) b = (b & ~0x1fffffffull) | 0x0fffffffull;     // just below
+        else if (kind == 2) b = (b & ~0x1fffffffull) | 0x10000001ull;     // just above
+        else if (kind == 3) b = (b & ~0xfffffffffffffull) | 0xfffffe0000000ull | (h & 0x1fffffffull);  // carry
+        const double x = __longlong_as_double((long long)(kind == 4 ? h : b));  // kind 4: any pattern
+        const float a = d2f_rn(x), c = (float)x;
+        if (__float_as_uint(a) != __float_as_uint(c) && !(a != a && c != c)) nbad++;
+    }
+    if (nbad) atomicAdd(bad, nbad);
+}
+
+void launch_check_conversions_impl(long long n, unsigned long long seed, unsigned long long* bad, cudaStream_t s)
+{
+    k_check_conversions<<<1024, 256, 0, s>>>(n, seed, bad);
 }
 
 void launch_kick_drift_impl(const Batch& b, const LaunchCfg& lc)

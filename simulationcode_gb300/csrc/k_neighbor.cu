@@ -268,6 +268,7 @@ struct BuildSmem {
     int ca[27];
     int cn[27];
     int pre[28];
+    float rf[3];  // the home cell's grid reference point
     int nst;
     unsigned long long entries;
     int maxcnt;
@@ -295,6 +296,14 @@ __device__ void build_cell(const Batch& b, const RepDesc& d, RepState& st, int c
         sm.ca[tid] = a;
         sm.cn[tid] = S.cell_start[d.cell0 + lin + 1] - a;
     }
+    // grid reference point near the home cell centre: candidate coordinates
+    // relative to it are small, so a pair difference is one FP32 subtract
+    // (one thread: FP64 runs on a narrow pipe)
+    if (tid == 32) {
+        sm.rf[0] = (float)grid_index(((double)cx + 0.5) * d.cs, d) * d.hf;
+        sm.rf[1] = (float)grid_index(((double)cy + 0.5) * d.cs, d) * d.hf;
+        sm.rf[2] = (DIM == 3) ? (float)grid_index(((double)cz + 0.5) * d.cs, d) * d.hf : 0.0f;
+    }
     __syncthreads();
     if (tid == 0) {
         int acc = 0;
@@ -306,11 +315,7 @@ __device__ void build_cell(const Batch& b, const RepDesc& d, RepState& st, int c
     }
     __syncthreads();
     const int M = sm.pre[nst];
-    // grid reference point near the home cell centre: candidate coordinates
-    // relative to it are small, so a pair difference is one FP32 subtract
-    const float rfx = (float)grid_index(((double)cx + 0.5) * d.cs, d) * d.hf,
-                rfy = (float)grid_index(((double)cy + 0.5) * d.cs, d) * d.hf,
-                rfz = (DIM == 3) ? (float)grid_index(((double)cz + 0.5) * d.cs, d) * d.hf : 0.0f;
+    const float rfx = sm.rf[0], rfy = sm.rf[1], rfz = sm.rf[2];
     // lanes per home particle: as many as keep the block's 128 threads busy
     // (a power of two dividing 32, so a particle's lanes share one warp)
     const int Tb = P <= 4 ? 32 : (P <= 8 ? 16 : (P <= 16 ? 8 : (P <= 32 ? 4 : (P <= 64 ? 2 : 1))));

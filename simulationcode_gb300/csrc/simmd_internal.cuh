@@ -51,12 +51,14 @@ struct RepDesc {
     double relax_cap;          // > 0: capped steepest descent (set-up relaxation), no noise
     double wrap_hi;            // smallest x with RN(x/L) >= 1: floor(x/L) without a divide
     double inv_two_m;          // 1/(2m), used when 2m is a power of two (exact)
+    double dt_over_two_m;      // dt/(2m) when 2m is a power of two (exact): one multiply per kick
     int two_m_pow2;
     int build_wrap;            // 0: stencil candidates never need the minimum image (2 cs + h < L/2)
     // split precision: FP32 offsets from a power-of-two grid h (exact integer shifts)
     double h, inv_h;
     float hf, Lhi_f, Llo_f, rv2f;
     float Lf, halfLf, csf, rc2f, rcutf, skinf, sigma2f, sigma4f, cut2f, epsf, Ucf, c0f, c2f, c4f, zetaf;
+    float noisef, gammaf;      // noise_factor, gamma rounded to FP32
     unsigned long long seed;
     const double* host_noise;  // [noise_nsteps][n][dims], original order
     long long noise_step0;
@@ -199,6 +201,43 @@ __device__ __forceinline__ float split_dx(float oi, float oj, int mi, int mj, co
     const float dx0 = a + G0;
     const float s = (dx0 > d.halfLf) ? 1.0f : ((dx0 < -d.halfLf) ? -1.0f : 0.0f);
     return (a - s * d.Llo_f) + (G0 - s * d.Lhi_f);
+}
+
+// float <-> double conversions on the integer pipes.  GB300 runs FP64
+// arithmetic and FP64 conversions on one narrow pipe (about 1/70 of the FP32
+// rate), so the split-precision kernels widen and narrow with bit operations:
+// f2d is exact, d2f_rn rounds to nearest even; both give the converter's
+// result bit for bit.  Zero and normal numbers take the inline path; the
+// rest (subnormal, out of range, inf, nan) go to the converter.
+__device__ __forceinline__ double f2d(float f)
+{
+    const unsigned u = __float_as_uint(f);
+    const unsigned a = u & 0x7fffffffu;
+    if (a - 0x00800000u < 0x7f000000u)  // exponent field 1..254
+        return __hiloint2double((int)((u & 0x80000000u) | ((a >> 3) + (896u << 20))), (int)(u << 29));
+    if (a == 0u) return __hiloint2double((int)(u & 0x80000000u), 0);
+    return (double)f;
+}
+
+__device__ __forceinline__ float d2f_rn(double x)
+{
+    const unsigned hi = (unsigned)__double2hiint(x), lo = (unsigned)__double2loint(x);
+    const unsigned ah = hi & 0x7fffffffu;
+    const int e = (int)(ah >> 20) - 896;  // the float exponent field
+    if (e >= 1 && e <= 254) {
+        unsigned f = ((unsigned)e << 23) | ((ah & 0xfffffu) << 3) | (lo >> 29);
+        const unsigned r = lo & 0x1fffffffu;  // the 29 dropped bits
+        f += (r > 0x10000000u || (r == 0x10000000u && (f & 1u))) ? 1u : 0u;  // carry may reach inf: correct
+        return __uint_as_float((hi & 0x80000000u) | f);
+    }
+    if (ah == 0u && lo == 0u) return __uint_as_float(hi & 0x80000000u);
+    return (float)x;
+}
+
+// non-finite test on the bit pattern (no FP64 compare)
+__device__ __forceinline__ bool nonfinite_bits(double x)
+{
+    return (__double_as_longlong(x) & 0x7fffffffffffffffll) >= 0x7ff0000000000000ll;
 }
 
 // one 256-bit read-only load of a neighbour's record (sm_100 and later):

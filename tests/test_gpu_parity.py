@@ -188,3 +188,15 @@ def test_conditional_rebuild_bodies_counted(simlib, oracle):
     assert 1 < a.stats().rebuilds < 96
     for x, y in zip(a.state(), b.state()):
         assert np.array_equal(x, y)
+
+
+def test_split_conversions_match_hardware(simlib):
+    """The split-precision kernels widen FP32 to FP64 and round FP64 to FP32
+    with integer bit operations (GB300 runs FP64 conversions on its narrow
+    FP64 pipe): bit-identical to the hardware converter on 2^24 hashed
+    patterns, rounding ties and carries included."""
+    import ctypes as C
+    bad = C.c_int64(-1)
+    for seed in (1, 2):
+        assert simlib.simmd_check_conversions(1 << 24, seed, C.byref(bad)) == 0
+        assert bad.value == 0
