@@ -260,8 +260,9 @@ int simmd_profile_get(simmd_ctx* ctx, double* out6);
 /* self-check of the split-precision kernels' float <-> double conversions
  * (bit operations on the integer pipes) against the hardware converter on
  * the current device: n hashed float and double bit patterns (all classes,
- * rounding ties, the float range edges); *mismatches = patterns whose result
- * bits differ.  No context needed. */
+ * rounding ties, the float range edges), and of the integer grid index
+ * against its FP64 form; *mismatches = patterns whose result bits differ.
+ * No context needed. */
 int simmd_check_conversions(int64_t n, uint64_t seed, int64_t* mismatches);
 
 #ifdef __cplusplus

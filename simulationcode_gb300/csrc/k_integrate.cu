@@ -59,13 +59,18 @@ __device__ __forceinline__ double drift_slot(const Batch& b, const RepDesc& d, l
 {
     const Slots& S = b.s;
     double ux = dadd(S.ux[i], drx), uy = dadd(S.uy[i], dry), uz = 0.0;
-    double u2 = dadd(dmul(ux, ux), dmul(uy, uy));
     S.ux[i] = ux;
     S.uy[i] = uy;
     if (d.dims == 3) {
         uz = dadd(S.uz[i], drz);
-        u2 = dadd(u2, dmul(uz, uz));
         S.uz[i] = uz;
+    }
+    double u2;
+    if (d.prec == PREC_FP64) {  // the reference's rounding of sum(abs2, disp)
+        u2 = dadd(dmul(ux, ux), dmul(uy, uy));
+        if (d.dims == 3) u2 = dadd(u2, dmul(uz, uz));
+    } else {  // split precision: fused (FP64 throughout, two fewer FP64 operations)
+        u2 = (d.dims == 3) ? __fma_rn(ux, ux, __fma_rn(uy, uy, dmul(uz, uz))) : __fma_rn(ux, ux, dmul(uy, uy));
     }
     double4_32a p = S.posD[i];
     const double x = wrap_coord(dadd(p.x, drx), d);
@@ -106,8 +111,14 @@ __device__ __forceinline__ void block_max_to_state(double u2, RepState& st, unsi
     __syncthreads();
 }
 
+// blocks per SM the position updates are compiled for (registers): more
+// warps in flight hide the FP64 and memory latency of these streaming passes
+#ifndef SIMMD_UPD_MINB
+#define SIMMD_UPD_MINB 16
+#endif
+
 // kick1 + drift for Newtonian / Langevin replicas (src/MD.jl:510-522)
-__global__ void k_kick_drift(Batch b)
+__global__ void __launch_bounds__(TILE, SIMMD_UPD_MINB) k_kick_drift(Batch b)
 {
     __shared__ unsigned long long s_max[TILE / 32];
     for (int t = blockIdx.x; t < b.ntiles; t += gridDim.x) {
@@ -151,7 +162,7 @@ __global__ void k_kick_drift(Batch b)
 // subtraction is applied again when F is downloaded), saving a store.
 // FP64 replicas: the reference's rounding, (dt/gamma)*(F - <F>); split
 // precision: one fused multiply-add (the force is FP32-accurate anyway).
-__global__ void k_brownian_update(Batch b)
+__global__ void __launch_bounds__(TILE, SIMMD_UPD_MINB) k_brownian_update(Batch b)
 {
     __shared__ unsigned long long s_max[TILE / 32];
     for (int t = blockIdx.x; t < b.ntiles; t += gridDim.x) {
@@ -382,7 +393,8 @@ __global__ void k_finalize(Batch b)
 }
 
 // ---------------------------------------------------------------------------
-// self-check: f2d / d2f_rn against the converter, bit for bit
+// self-check: f2d / d2f_rn against the converter, bit for bit, and the
+// integer grid index against its FP64 form
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ unsigned long long mix64(unsigned long long x)
 {
@@ -414,6 +426,20 @@ __global__ void k_check_conversions(long long n, unsigned long long seed, unsign
         const double x = __longlong_as_double((long long)(kind == 4 ? h : b));  // kind 4: any pattern
         const float a = d2f_rn(x), c = (float)x;
         if (__float_as_uint(a) != __float_as_uint(c) && !(a != a && c != c)) nbad++;
+        // grid index: the FP64 form floor(x/h + 0.5) clamped to [0, 1023]
+        RepDesc dd = {};
+        const int hk = -(int)((h >> 20) & 7ull);  // h = 2^0 .. 2^-7
+        dd.h = __longlong_as_double((long long)(1023 + hk) << 52);
+        const double inv_h = __longlong_as_double((long long)(1023 - hk) << 52);
+        const int gk = (int)((h >> 24) & 7ull);
+        double xg;
+        if (gk == 0) xg = __longlong_as_double((long long)h);  // any pattern
+        else if (gk == 1) xg = ((double)(long long)((h >> 27) % 2300ull) * 0.5 - 50.0) * dd.h;  // ties
+        else if (gk == 2) xg = __longlong_as_double(0x3fdfffffffffffffll) * dd.h;  // 0.5 - 2^-54
+        else xg = ((double)(long long)(h >> 11) * 0x1.0p-53 * 1100.0 - 30.0) * dd.h;
+        const double q = floor(xg * inv_h + 0.5);
+        const int gref = (q == q) ? (int)fmax(fmin(q, 1023.0), 0.0) : 0;
+        if (grid_index(xg, dd) != gref) nbad++;
     }
     if (nbad) atomicAdd(bad, nbad);
 }

@@ -80,11 +80,11 @@ __global__ void k_rb_bin(Batch b)
         int nc = d.nc;
         int c[3] = {0, 0, 0};
         double x[3] = {p.x, p.y, p.z};
-        bool finite = isfinite(p.x) && isfinite(p.y) && isfinite(p.z);
+        const bool finite = !(nonfinite_bits(p.x) || nonfinite_bits(p.y) || nonfinite_bits(p.z));
         if (!finite) b.state[r].nonfinite = 1;
         if (nc > 1 && finite) {
             for (int k2 = 0; k2 < d.dims; k2++) {
-                int ci = (int)floor(x[k2] * d.inv_cs);
+                int ci = __double2int_rd(x[k2] * d.inv_cs);  // floor, one conversion
                 ci = ci < 0 ? 0 : (ci >= nc ? nc - 1 : ci);
                 c[k2] = ci;
             }
@@ -226,10 +226,11 @@ __global__ void k_rb_gather(Batch b, int* ncnt_full)
             int cx = lin % nc, cy = (lin / nc) % nc, cz = lin / (nc * nc);
             S.cellc[nw] = pack_cell(cx, cy, cz);
             const int mx = grid_index(p.x, d), my = grid_index(p.y, d), mz = d.dims == 3 ? grid_index(p.z, d) : 0;
+            const float gx = (float)mx * d.hf, gy = (float)my * d.hf, gz = (float)mz * d.hf;
             rec_put(&S.rec[nw],
-                    make_float4(grid_offset(p.x, mx, d), grid_offset(p.y, my, d),
-                                d.dims == 3 ? grid_offset(p.z, mz, d) : 0.0f, (float)p.w),
-                    make_float4((float)mx * d.hf, (float)my * d.hf, (float)mz * d.hf, 0.0f));
+                    make_float4(grid_offset(p.x, gx, d), grid_offset(p.y, gy, d),
+                                d.dims == 3 ? grid_offset(p.z, gz, d) : 0.0f, d2f_rn(p.w)),
+                    make_float4(gx, gy, gz, 0.0f));
         } else {
             S.t_posD[nw] = make_double4_32a(0.0, 0.0, 0.0, 0.0);
             S.t_vx[nw] = S.t_vy[nw] = S.t_vz[nw] = 0.0;

@@ -171,38 +171,6 @@ __device__ __forceinline__ float min_image_f32(float dx, float halfL, float L)
 }
 
 // split precision: grid index of the FP32 offset origin (power-of-two grid h)
-__device__ __forceinline__ int grid_index(double x, const RepDesc& d)
-{
-    const double q = floor(x * d.inv_h + 0.5);
-    int m = (q == q) ? (int)fmax(fmin(q, 1023.0), 0.0) : 0;
-    return m;
-}
-
-// FP32 offset of coordinate x from its grid point m*h (m*h exact), continuous
-// across the periodic wrap
-__device__ __forceinline__ float grid_offset(double x, int m, const RepDesc& d)
-{
-    double o = x - (double)m * d.h;
-    o = (o > d.halfL) ? o - d.L : o;
-    o = (o < -d.halfL) ? o + d.L : o;
-    return (float)o;
-}
-
-__device__ __forceinline__ int grid_axis(int g, int axis) { return (g >> (10 * axis)) & 1023; }
-
-// minimum-image difference x_i - x_j of two split-precision coordinates:
-// ((o_i - o_j) - s*L_lo) + ((m_i - m_j)*h - s*L_hi) with the integer grid
-// shift and L_hi = floor(L/h)*h exact in FP32, so only the small offset
-// terms and the final sum round
-__device__ __forceinline__ float split_dx(float oi, float oj, int mi, int mj, const RepDesc& d)
-{
-    const float a = oi - oj;
-    const float G0 = (float)(mi - mj) * d.hf;
-    const float dx0 = a + G0;
-    const float s = (dx0 > d.halfLf) ? 1.0f : ((dx0 < -d.halfLf) ? -1.0f : 0.0f);
-    return (a - s * d.Llo_f) + (G0 - s * d.Lhi_f);
-}
-
 // float <-> double conversions on the integer pipes.  GB300 runs FP64
 // arithmetic and FP64 conversions on one narrow pipe (about 1/70 of the FP32
 // rate), so the split-precision kernels widen and narrow with bit operations:
@@ -238,6 +206,59 @@ __device__ __forceinline__ float d2f_rn(double x)
 __device__ __forceinline__ bool nonfinite_bits(double x)
 {
     return (__double_as_longlong(x) & 0x7fffffffffffffffll) >= 0x7ff0000000000000ll;
+}
+
+// the FP64 form floor(x/h + 0.5) clamped to [0, 1023] (h a power of two, so
+// x/h is exact), computed on the integer pipes with the same result for every
+// x: with y = x/h in [2^j, 2^(j+1)), y + 0.5 is exact unless it crosses into
+// the next binade, and there no integer is within the rounding's reach --
+// except at j = -2, where y = 0.5 - 2^-54 rounds y + 0.5 up to 1
+__device__ __forceinline__ int grid_index(double x, const RepDesc& d)
+{
+    const long long b = __double_as_longlong(x);
+    if (b <= 0) return 0;  // +0, negatives, NaNs with the sign bit
+    const int ex = (int)(b >> 52);
+    const long long mant = b & 0xfffffffffffffll;
+    if (ex == 0x7ff) return mant ? 0 : 1023;  // NaN, +inf
+    if (ex == 0) return 0;                    // subnormal: y < 0.5
+    const int hk = (int)((__double_as_longlong(d.h) >> 52) & 0x7ff) - 1023;
+    const int j = ex - 1023 - hk;
+    if (j >= 10) return 1023;
+    if (j <= -3) return 0;
+    if (j == -2) return mant == 0xfffffffffffffll ? 1 : 0;
+    const long long M = mant | (1ll << 52);
+    const int sh = 52 - j;  // 43..53
+    const long long m = (M + (1ll << (sh - 1))) >> sh;
+    return m > 1023 ? 1023 : (int)m;
+}
+
+// FP32 offset of coordinate x from its grid point g = m*h (exact in FP32 and
+// FP64), continuous across the periodic wrap: one FP64 subtract; the wrap
+// correction (|x - g| > L/2, a particle just across the box edge) in FP64
+// only when the FP32 offset is not clearly inside
+__device__ __forceinline__ float grid_offset(double x, float g, const RepDesc& d)
+{
+    double o = dsub(x, f2d(g));
+    const float of = d2f_rn(o);
+    if (fabsf(of) < d.halfLf * 0.9f) return of;
+    o = (o > d.halfL) ? o - d.L : o;
+    o = (o < -d.halfL) ? o + d.L : o;
+    return (float)o;
+}
+
+__device__ __forceinline__ int grid_axis(int g, int axis) { return (g >> (10 * axis)) & 1023; }
+
+// minimum-image difference x_i - x_j of two split-precision coordinates:
+// ((o_i - o_j) - s*L_lo) + ((m_i - m_j)*h - s*L_hi) with the integer grid
+// shift and L_hi = floor(L/h)*h exact in FP32, so only the small offset
+// terms and the final sum round
+__device__ __forceinline__ float split_dx(float oi, float oj, int mi, int mj, const RepDesc& d)
+{
+    const float a = oi - oj;
+    const float G0 = (float)(mi - mj) * d.hf;
+    const float dx0 = a + G0;
+    const float s = (dx0 > d.halfLf) ? 1.0f : ((dx0 < -d.halfLf) ? -1.0f : 0.0f);
+    return (a - s * d.Llo_f) + (G0 - s * d.Lhi_f);
 }
 
 // one 256-bit read-only load of a neighbour's record (sm_100 and later):
