@@ -264,6 +264,12 @@ int simmd_profile_get(simmd_ctx* ctx, double* out6);
  * against its FP64 form; *mismatches = patterns whose result bits differ.
  * No context needed. */
 int simmd_check_conversions(int64_t n, uint64_t seed, int64_t* mismatches);
+/* throughput probe of the current device (CUDA events, SMs x 8 blocks of
+ * 256 threads, four independent chains each), G operations/s:
+ * gops6 = {FP64 add, float->double converter, float->double bit
+ * operations, double->float converter, double->float bit operations,
+ * FP32 FMA}.  No context needed. */
+int simmd_pipe_rates(double* gops6);
 
 #ifdef __cplusplus
 }
