@@ -324,7 +324,7 @@ __device__ void build_cell(const Batch& b, const RepDesc& d, RepState& st, int c
     const int lane = tid & 31;
     const int gbase = (lane / Tb) * Tb;
     const unsigned gmask = (Tb == 32) ? 0xffffffffu : ((1u << Tb) - 1u);
-    const int K = b.K, T = b.tpp;
+    const int K = b.K, tsh = 31 - __clz(b.tpp);  // threads per particle: a power of two
     const long long SS = b.S;
     const long long halfLb = __double_as_longlong(d.halfL);
     for (int base = 0; base < P; base += BLD_THREADS / Tb) {
@@ -409,7 +409,7 @@ __device__ void build_cell(const Batch& b, const RepDesc& d, RepState& st, int c
                 const unsigned gb = (bal >> gbase) & gmask;
                 if (pred) {
                     const int pos = cnt + __popc(gb & ((1u << sub) - 1u));
-                    if (pos < K) S.nbr[nbr_addr(pos, i, T, K)] = (unsigned)sm.slot[q];
+                    if (pos < K) S.nbr[nbr_addr_sh(pos, i, tsh, K)] = (unsigned)sm.slot[q];
                 }
                 cnt += __popc(gb);
                 if (FULL) {

@@ -315,6 +315,13 @@ __device__ __forceinline__ size_t nbr_addr(int n, long long slot, int T, int K)
            (size_t)(slot % TILE) * (size_t)T + (size_t)(n % T);
 }
 
+// the same address for a runtime T = 1 << tsh (no integer division)
+__device__ __forceinline__ size_t nbr_addr_sh(int n, long long slot, int tsh, int K)
+{
+    return (size_t)(slot / TILE) * ((size_t)TILE * (size_t)K) + (size_t)(n >> tsh) * (size_t)(TILE << tsh) +
+           ((size_t)(slot % TILE) << tsh) + (size_t)(n & ((1 << tsh) - 1));
+}
+
 // ---------------------------------------------------------------------------
 // Philox4x32-10 (Salmon et al., SC'11) and Box-Muller normals
 // ---------------------------------------------------------------------------
