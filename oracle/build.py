@@ -1,4 +1,4 @@
-"""Build recipe for the CPU oracle (test infrastructure, the checker).
+"""Build recipe for the CPU oracle (test infrastructure only).
 
 Compiles oracle/simmd_oracle.c with gcc into oracle/_build/libsimmd_oracle.so.
 -ffp-contract=off keeps every floating-point expression rounded as written

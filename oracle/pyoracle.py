@@ -1,4 +1,4 @@
-"""ctypes binding of the CPU oracle (test infrastructure, the checker).
+"""ctypes binding of the CPU oracle (test infrastructure only).
 
 Only the tests, ``__graft_entry__.smoke()`` and the CPU-baseline leg of
 ``bench.py`` import this module.  Arrays follow the reference's ArrayStruct

@@ -1,6 +1,6 @@
 /*
  * simmd_oracle.c -- serial FP64 restatement of the SimulationCode.jl MD hot
- * path.  TEST INFRASTRUCTURE ONLY (the checker); see simmd_oracle.h for the
+ * path.  TEST INFRASTRUCTURE ONLY; see simmd_oracle.h for the
  * routine-by-routine reference map and the parity status ("unpinned": no
  * Julia and no reference golden vectors exist for this path).
  *

@@ -1,7 +1,7 @@
 /*
  * simmd_oracle.h -- CPU oracle for the SimulationCode.jl molecular-dynamics
  * hot path.  TEST INFRASTRUCTURE ONLY: the tests, the smoke check and the
- * CPU-baseline leg of bench.py call it as the checker; the product library
+ * CPU-baseline leg of bench.py call it to compare against; the product library
  * (libsimmd.so) never links or calls it.
  *
  * It is a plain-C, serial, FP64 restatement of the reference Julia routines
