@@ -289,12 +289,13 @@ template <int T>
 __device__ __forceinline__ int stage_rows(const Batch& b, int t, int part, int ppb, int maxcnt, unsigned* s_rows)
 {
     const int row_words = ppb * T, vpr = row_words / 4;
+    const int vsh = 31 - __clz(vpr);  // ppb and T are powers of two
     const int nrows = min((maxcnt + T - 1) / T, STAGE_WORDS / row_words);
     const uint4* src = reinterpret_cast<const uint4*>(b.s.nbr + (size_t)t * ((size_t)TILE * (size_t)b.K) +
                                                       (size_t)part * row_words);
     uint4* dst = reinterpret_cast<uint4*>(s_rows);
     for (int v = threadIdx.x; v < nrows * vpr; v += blockDim.x) {
-        const int row = v / vpr, c4 = v - row * vpr;
+        const int row = v >> vsh, c4 = v & (vpr - 1);
         dst[v] = __ldg(src + (size_t)row * (TILE * T / 4) + c4);
     }
     return nrows;
