@@ -88,26 +88,29 @@ __device__ bool tile_reduce(const Batch& b, int item, const RepDesc& d, RepState
     }
     __syncthreads();
     if (wid == 0 && *s_flag) {
-        // the warp partials in s_part (split tiles: loaded from the warp
-        // slots), summed in warp order by lane k for value k: the FP64 adds
-        // run on NV lanes, not on the whole warp
-        int nsum = nw;
-        if (parts > 1) {
-            __threadfence();
-            nsum = nw * parts;  // <= 32
-            const double* slot = b.warp_part + (size_t)t * WARP_SLOTS * NPART;
-            if (lane < nsum) {
-#pragma unroll
-                for (int k = 0; k < NV; k++) s_part[lane * NV + k] = __ldcg(slot + (size_t)lane * NPART + k);
-            }
-            __syncwarp();
-        }
-        double my = 0.0;
-        if (lane < NV)
-            for (int w = 0; w < nsum; w++) my += s_part[w * NV + lane];
         double ts[NV];
+        if (parts == 1) {
+            // whole tiles (large batches): lane k adds value k over the warps
+            // in order, so the FP64 adds run on NV lanes, not on the warp
+            double my = 0.0;
+            if (lane < NV)
+                for (int w = 0; w < nw; w++) my += s_part[w * NV + lane];
 #pragma unroll
-        for (int k = 0; k < NV; k++) ts[k] = __shfl_sync(0xffffffffu, my, k);
+            for (int k = 0; k < NV; k++) ts[k] = __shfl_sync(0xffffffffu, my, k);
+        } else {
+            // split tiles (small batches): the warp slots, one per lane,
+            // added in warp order through shuffles
+            __threadfence();
+            const int wpt = nw * parts;  // <= 32
+            const double* slot = b.warp_part + (size_t)t * WARP_SLOTS * NPART;
+#pragma unroll
+            for (int k = 0; k < NV; k++) {
+                const double x = lane < wpt ? __ldcg(slot + (size_t)lane * NPART + k) : 0.0;
+                double s = 0.0;
+                for (int w = 0; w < wpt; w++) s += __shfl_sync(0xffffffffu, x, w);
+                ts[k] = s;
+            }
+        }
         if (lane == 0) {
             double* dst = b.red_val + (size_t)t * RED_REC;
 #pragma unroll
