@@ -170,7 +170,6 @@ __device__ __forceinline__ float min_image_f32(float dx, float halfL, float L)
     return dx;
 }
 
-// split precision: grid index of the FP32 offset origin (power-of-two grid h)
 // float <-> double conversions on the integer pipes.  GB300 runs FP64
 // arithmetic and FP64 conversions on one narrow pipe (about 1/70 of the FP32
 // rate), so the split-precision kernels widen and narrow with bit operations:
@@ -208,7 +207,8 @@ __device__ __forceinline__ bool nonfinite_bits(double x)
     return (__double_as_longlong(x) & 0x7fffffffffffffffll) >= 0x7ff0000000000000ll;
 }
 
-// the FP64 form floor(x/h + 0.5) clamped to [0, 1023] (h a power of two, so
+// split precision: grid index of the FP32 offset origin (power-of-two grid
+// h), the FP64 form floor(x/h + 0.5) clamped to [0, 1023] (h a power of two, so
 // x/h is exact), computed on the integer pipes with the same result for every
 // x: with y = x/h in [2^j, 2^(j+1)), y + 0.5 is exact unless it crosses into
 // the next binade, and there no integer is within the rounding's reach --
