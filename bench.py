@@ -11,8 +11,10 @@ state, all inside the timed region.
     python bench.py [--workload c4] [--steps K] [--warmup W] [--gpus N]
     python bench.py --impl reference ...   # the reference algorithm on the host cores
 
-Multi-GPU: replicas only (independent systems, no collective); each rank
-runs the full workload on its own GPU (weak scaling), max time over ranks.
+Multi-GPU: independent replicas, no collective on the data path.  The
+replica batch is one job of 512 replicas per GPU partitioned over the ranks
+by LPT on particles x steps (weak scaling: per-GPU work fixed); a
+single-system workload runs one copy per rank.  Max time over ranks.
 """
 from __future__ import annotations
 
@@ -35,14 +37,21 @@ sys.path.insert(0, ROOT)
 MEASURED_PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
 
 
-def rank_specs(workload, rank, precision=None):
-    """the workload of one rank: replicas only (no system spans GPUs), so
-    every rank runs its own full copy of the workload with its own seeds;
-    rank 0 has the workload's canonical seeds"""
+def rank_specs(workload, rank, precision=None, world=1):
+    """the replicas of one rank.  No system spans GPUs.  The replica batch
+    (c4) is a job of 512 replicas per GPU, 512 x world in all (the first 512
+    are the one-GPU workload), partitioned over the ranks by LPT on
+    particles x steps: each rank runs its share, no collective on the data
+    path (weak scaling).  A single-system workload (c1-c3) runs one copy per
+    rank with the rank's own seed (rank 0: the canonical seed)."""
     from simulationcode_gb300 import workloads as W
     import inspect
-    fn = W.WORKLOADS[workload]
     kw = {} if precision is None else {"precision": precision}
+    if workload == "c4":
+        nrep = 512 * world
+        part = W.lpt_partition([int(n) for n in W.c4_sizes(nrep)], world)[rank]
+        return W.c4(nrep=nrep, indices=part, **kw)
+    fn = W.WORKLOADS[workload]
     if rank:
         kw["seed"] = inspect.signature(fn).parameters["seed"].default + 7919 * rank
     return fn(**kw)
@@ -445,7 +454,7 @@ def run_gpu(args, dist):
     lib = _lib.load()
     device = dist.local
     prec = {"fp64": _lib.FP64, "fp32": _lib.FP32_SPLIT}[args.precision] if args.precision else None
-    specs = rank_specs(args.workload, dist.rank, prec)
+    specs = rank_specs(args.workload, dist.rank, prec, dist.ws)
     # set-up: relax random starts on the GPU (not timed)
     if any(s.potential == _lib.POT_BERTHIER for s in specs) and args.relax_steps > 0:
         fmax, counts = W.relax_on_device(specs, device, steps=args.relax_steps)
@@ -566,7 +575,8 @@ def run_gpu(args, dist):
                        "replicas": len(specs), "threads_per_particle": args.tpp,
                        "l2": ("state larger than L2 (%.0f MB streamed per step)" % (step_bytes / 1e6))
                              if step_bytes > 129e6 else "state fits in L2 (%.0f MB; no flush)" % (step_bytes / 1e6),
-                       "parallelism": "replicas only" if dist.ws > 1 else "single GPU",
+                       "parallelism": ("LPT replica partition over %d ranks" % dist.ws) if dist.ws > 1
+                                      else "single GPU",
                        "rebuilds_in_timed_region": rebuilds,
                        "step_loop": "CUDA graph of 16 steps" if args.graphs else "direct launches",
                        "skin": specs[0].skin,

@@ -220,7 +220,12 @@ int simmd_set_budget(simmd_ctx* ctx, int64_t bytes);
  * Scratch is a fixed array inside the library, shared by every call on a
  * GPU: N must be <= SIMMD_NOALLOC_MAX_N (else SIMMD_ERR_BUDGET), and calls
  * that run concurrently on the same GPU race.  The first call on a device
- * performs a one-time symbol lookup; make it before any stream capture.
+ * performs a one-time symbol lookup, which may load the library's device
+ * code onto that GPU (lazy module loading) and so reserve its memory; make
+ * that first call before any stream capture and before measuring memory.
+ * Later calls allocate nothing.  The looked-up address is kept per device
+ * and per CUDA context: after a device reset the next call looks it up
+ * again (and is again a first call).
  * Asynchronous: synchronise the stream before reading out. */
 #define SIMMD_NOALLOC_MAX_N 1048576
 int simmd_energy_virial_noalloc(const simmd_params* p, const double* r, const double* D,
@@ -264,12 +269,6 @@ int simmd_profile_get(simmd_ctx* ctx, double* out6);
  * against its FP64 form; *mismatches = patterns whose result bits differ.
  * No context needed. */
 int simmd_check_conversions(int64_t n, uint64_t seed, int64_t* mismatches);
-/* throughput probe of the current device (CUDA events, SMs x 8 blocks of
- * 256 threads, four independent chains each), G operations/s:
- * gops6 = {FP64 add, float->double converter, float->double bit
- * operations, double->float converter, double->float bit operations,
- * FP32 FMA}.  No context needed. */
-int simmd_pipe_rates(double* gops6);
 
 #ifdef __cplusplus
 }

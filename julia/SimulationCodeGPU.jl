@@ -18,7 +18,7 @@ module SimulationCodeGPU
 
 export GPUNeighborList, gpu_update_neighbor_lists!, gpu_calculate_new_forces!, gpu_do_time_steps!,
        gpu_calculate_full_energy, gpu_find_inherent_structure!, gpu_dump_async, gpu_dump_wait,
-       gpu_perform_molecular_dynamics!, gpu_check_conversions, gpu_pipe_rates
+       gpu_perform_molecular_dynamics!, gpu_check_conversions
 
 const libsimmd = get(ENV, "SIMMD_LIB", "libsimmd.so")
 
@@ -195,14 +195,6 @@ function gpu_check_conversions(n::Integer=1 << 24, seed::Integer=1)
     bad = Ref{Int64}(-1)
     check(ccall((:simmd_check_conversions, libsimmd), Cint, (Int64, UInt64, Ref{Int64}), n, seed, bad))
     bad[]
-end
-
-"""G ops/s of the FP64 adder, the converters, the bit-level conversions and
-the FP32 FMA pipe on the current device"""
-function gpu_pipe_rates()
-    r = zeros(6)
-    check(ccall((:simmd_pipe_rates, libsimmd), Cint, (Ptr{Float64},), r))
-    (fp64_add=r[1], f2d_converter=r[2], f2d_bits=r[3], d2f_converter=r[4], d2f_bits=r[5], fp32_fma=r[6])
 end
 
 end # module

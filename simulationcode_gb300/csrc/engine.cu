@@ -47,7 +47,6 @@ void launch_store_aos_impl(const Batch& b, const LaunchCfg& lc, int rep, const R
 void launch_set_state_impl(const Batch& b, const LaunchCfg& lc, int rep, const RepDesc& hd, const double* r,
                            const double* v, const double* F, const double* disp);
 void launch_check_conversions_impl(long long n, unsigned long long seed, unsigned long long* bad, cudaStream_t s);
-int run_pipe_rates(int blocks, int threads, double* scratch, double* gops, cudaStream_t s);
 }  // namespace simmd
 
 using namespace simmd;
@@ -1768,21 +1767,6 @@ int simmd_check_conversions(int64_t n, uint64_t seed, int64_t* mismatches)
     cudaFree(d_bad);
     if (e != cudaSuccess) return set_err(SIMMD_ERR_CUDA, std::string("conversion check: ") + cudaGetErrorString(e));
     *mismatches = (int64_t)h_bad;
-    return SIMMD_OK;
-}
-
-int simmd_pipe_rates(double* gops6)
-{
-    if (!gops6) return set_err(SIMMD_ERR_BAD_ARG, "NULL argument");
-    int dev = 0, sms = 0;
-    CK(cudaGetDevice(&dev));
-    CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    const int blocks = sms * 8, threads = 256;
-    double* scratch = nullptr;
-    CK(cudaMalloc(&scratch, sizeof(double) * (size_t)blocks * threads));
-    const int err = run_pipe_rates(blocks, threads, scratch, gops6, 0);
-    cudaFree(scratch);
-    if (err) return set_err(SIMMD_ERR_CUDA, "pipe-rate probe failed");
     return SIMMD_OK;
 }
 

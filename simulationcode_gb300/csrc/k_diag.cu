@@ -1,8 +1,6 @@
-// k_diag.cu -- device self-checks and pipe-rate probes (not on the
-// simulation path): the bit-level conversions and grid index of the
-// split-precision kernels against the hardware / FP64 forms, and the
-// throughput of the FP64 pipe, the converters and the FP32 FMA pipe, which
-// decide where the split path may spend FP64 work.
+// k_diag.cu -- device self-check (not on the simulation path): the
+// bit-level conversions and grid index of the split-precision kernels
+// against the hardware converter and the FP64 forms.
 #include "simmd_internal.cuh"
 
 namespace simmd {
@@ -60,111 +58,6 @@ __global__ void k_check_conversions(long long n, unsigned long long seed, unsign
 void launch_check_conversions_impl(long long n, unsigned long long seed, unsigned long long* bad, cudaStream_t s)
 {
     k_check_conversions<<<1024, 256, 0, s>>>(n, seed, bad);
-}
-
-// ---------------------------------------------------------------------------
-// pipe rates: RATE_ITERS x 4 independent chains per thread
-// ---------------------------------------------------------------------------
-constexpr int RATE_ITERS = 2048;
-
-template <int OP>
-__global__ void k_rate(double* out, double a, float af)
-{
-    const int tid = blockIdx.x * blockDim.x + threadIdx.x;
-    double r = 0.0;
-    if (OP == 0) {  // FP64 add
-        double x0 = tid, x1 = x0 + 1.0, x2 = x0 + 2.0, x3 = x0 + 3.0;
-        for (int i = 0; i < RATE_ITERS; i++) {
-            x0 = __dadd_rn(x0, a);
-            x1 = __dadd_rn(x1, a);
-            x2 = __dadd_rn(x2, a);
-            x3 = __dadd_rn(x3, a);
-        }
-        r = x0 + x1 + x2 + x3;
-    } else if (OP == 1 || OP == 2) {  // float -> double: converter, bit operations
-        float f0 = (float)tid, f1 = f0 + 1.f, f2 = f0 + 2.f, f3 = f0 + 3.f;
-        long long acc = 0;
-        for (int i = 0; i < RATE_ITERS; i++) {
-            if (OP == 1)
-                acc ^= __double_as_longlong((double)f0) ^ __double_as_longlong((double)f1) ^
-                       __double_as_longlong((double)f2) ^ __double_as_longlong((double)f3);
-            else
-                acc ^= __double_as_longlong(f2d(f0)) ^ __double_as_longlong(f2d(f1)) ^ __double_as_longlong(f2d(f2)) ^
-                       __double_as_longlong(f2d(f3));
-            f0 += af;
-            f1 += af;
-            f2 += af;
-            f3 += af;
-        }
-        r = (double)acc;
-    } else if (OP == 3 || OP == 4) {  // double -> float: converter, bit operations
-        long long b0 = __double_as_longlong(1.0 + tid * 1e-7), b1 = b0 + 977, b2 = b0 + 1931, b3 = b0 + 2897;
-        const long long step = __double_as_longlong(a) & 0xffffll;
-        unsigned acc = 0;
-        for (int i = 0; i < RATE_ITERS; i++) {
-            const double d0 = __longlong_as_double(b0), d1 = __longlong_as_double(b1), d2 = __longlong_as_double(b2),
-                         d3 = __longlong_as_double(b3);
-            if (OP == 3)
-                acc ^= __float_as_uint((float)d0) ^ __float_as_uint((float)d1) ^ __float_as_uint((float)d2) ^
-                       __float_as_uint((float)d3);
-            else
-                acc ^= __float_as_uint(d2f_rn(d0)) ^ __float_as_uint(d2f_rn(d1)) ^ __float_as_uint(d2f_rn(d2)) ^
-                       __float_as_uint(d2f_rn(d3));
-            b0 += step;
-            b1 += step;
-            b2 += step;
-            b3 += step;
-        }
-        r = (double)acc;
-    } else {  // FP32 FMA
-        float x0 = (float)tid, x1 = x0 + 1.f, x2 = x0 + 2.f, x3 = x0 + 3.f;
-        for (int i = 0; i < RATE_ITERS; i++) {
-            x0 = fmaf(x0, af, af);
-            x1 = fmaf(x1, af, af);
-            x2 = fmaf(x2, af, af);
-            x3 = fmaf(x3, af, af);
-        }
-        r = (double)(x0 + x1 + x2 + x3);
-    }
-    out[tid] = r;  // one slot per thread: keeps the chains live
-}
-
-// out[k] = G operations per second of probe k (0 FP64 add, 1/2 float->double
-// converter / bits, 3/4 double->float converter / bits, 5 FP32 FMA); out
-// holds blocks*threads doubles of scratch
-int run_pipe_rates(int blocks, int threads, double* scratch, double* gops, cudaStream_t s)
-{
-    cudaEvent_t e0, e1;
-    if (cudaEventCreate(&e0) != cudaSuccess) return 1;
-    if (cudaEventCreate(&e1) != cudaSuccess) {
-        cudaEventDestroy(e0);
-        return 1;
-    }
-    int err = 0;
-    const double ops = (double)blocks * threads * RATE_ITERS * 4.0;
-    for (int rep = 0; rep < 2 && !err; rep++)  // the first pass warms up
-        for (int k = 0; k < 6 && !err; k++) {
-            cudaEventRecord(e0, s);
-            switch (k) {
-            case 0: k_rate<0><<<blocks, threads, 0, s>>>(scratch, 1e-9, 1e-3f); break;
-            case 1: k_rate<1><<<blocks, threads, 0, s>>>(scratch, 1e-9, 1e-3f); break;
-            case 2: k_rate<2><<<blocks, threads, 0, s>>>(scratch, 1e-9, 1e-3f); break;
-            case 3: k_rate<3><<<blocks, threads, 0, s>>>(scratch, 3.0e-300, 1e-3f); break;
-            case 4: k_rate<4><<<blocks, threads, 0, s>>>(scratch, 3.0e-300, 1e-3f); break;
-            default: k_rate<5><<<blocks, threads, 0, s>>>(scratch, 1e-9, 0.999f); break;
-            }
-            cudaEventRecord(e1, s);
-            if (cudaEventSynchronize(e1) != cudaSuccess || cudaGetLastError() != cudaSuccess) {
-                err = 1;
-                break;
-            }
-            float ms = 0.f;
-            cudaEventElapsedTime(&ms, e0, e1);
-            if (rep == 1) gops[k] = ms > 0.f ? ops / ((double)ms * 1e6) : 0.0;
-        }
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
-    return err;
 }
 
 }  // namespace simmd

@@ -20,8 +20,11 @@
 // (different streams, no ordering between them) race and give wrong sums.
 // The completion counter is cleared at the start of each call.  The first
 // call on a device looks up the array's device address
-// (cudaGetSymbolAddress) with that device current; make that first call
-// before any stream capture.
+// (cudaGetSymbolAddress) with that device current; that lookup may load the
+// library's device code onto the GPU (lazy module loading), so make that
+// first call before any stream capture.  The address is cached per device
+// and per CUDA context: after a device reset (cudaDeviceReset, CUDA.jl's
+// device_reset!) the next call runs in a new context and looks it up again.
 #include "../../include/simmd.h"
 #include "simmd_internal.cuh"
 
@@ -39,6 +42,38 @@ static __device__ __align__(256) double g_noalloc_scratch[NA_HEADER + 2 * NA_MAX
 
 static std::mutex g_na_mutex;
 static double* g_na_ptr[NA_MAX_DEVICES] = {};
+static unsigned long long g_na_ctx[NA_MAX_DEVICES] = {};
+
+// unique id of the calling thread's current CUDA context (0: no context yet,
+// or the driver does not report one), through the runtime's driver entry
+// points so that the library needs no link to libcuda
+typedef int (*CtxGetCurrentFn)(void**);
+typedef int (*CtxGetIdFn)(void*, unsigned long long*);
+
+static unsigned long long current_ctx_id()
+{
+    static CtxGetCurrentFn get_cur = nullptr;
+    static CtxGetIdFn get_id = nullptr;
+    static bool looked = false;
+    if (!looked) {
+        looked = true;
+        void* f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_cur = reinterpret_cast<CtxGetCurrentFn>(f);
+        f = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_id = reinterpret_cast<CtxGetIdFn>(f);
+        cudaGetLastError();
+    }
+    if (!get_cur || !get_id) return 0ull;
+    void* ctx = nullptr;
+    unsigned long long id = 0ull;
+    if (get_cur(&ctx) != 0 || !ctx || get_id(ctx, &id) != 0) return 0ull;
+    return id;
+}
 
 struct NAParams {
     double L, rc2, sigma2, sigma4, lj_cut2, eps, Uc, c0, c2, c4, zeta;
@@ -190,6 +225,8 @@ __global__ void __launch_bounds__(NA_BLOCK) k_energy_noalloc(NAParams p, int N, 
 using simmd::NAParams;
 using simmd::g_na_mutex;
 using simmd::g_na_ptr;
+using simmd::g_na_ctx;
+using simmd::current_ctx_id;
 using simmd::NA_MAX_DEVICES;
 using simmd::NA_BLOCK;
 using simmd::k_energy_noalloc;
@@ -211,14 +248,19 @@ extern "C" int simmd_energy_virial_noalloc(const simmd_params* prm, const double
     double* scratch = nullptr;
     {
         std::lock_guard<std::mutex> g(g_na_mutex);
-        if (!g_na_ptr[dev]) {  // set-up, once per device, with that device current
+        const unsigned long long ctx = current_ctx_id();
+        if (!g_na_ptr[dev] || ctx == 0ull || ctx != g_na_ctx[dev]) {
+            // set-up, once per device (and again in a new context), with that
+            // device current
             void* ptr = nullptr;
             cudaError_t e = cudaGetSymbolAddress(&ptr, simmd::g_noalloc_scratch);
             if (e != cudaSuccess || !ptr) {
                 cudaGetLastError();
+                g_na_ptr[dev] = nullptr;
                 return SIMMD_ERR_CUDA;
             }
             g_na_ptr[dev] = static_cast<double*>(ptr);
+            g_na_ctx[dev] = current_ctx_id();  // the lookup has made the context current
         }
         scratch = g_na_ptr[dev];
     }

@@ -2,24 +2,42 @@
 
 Function names follow the reference (Julia's trailing ``!`` becomes a
 trailing ``_``); arguments and error behaviour are the same, so a script
-written against the reference reads the same here.  Every computation runs in
-the CUDA kernels of libsimmd through its C ABI (``_lib``); the host arrays of
-``ArrayStruct`` are kept in sync at each call boundary.
+written against the reference reads the same here.  The reference reaches
+its hot path through generic functions that dispatch on their arguments'
+types; this module keeps that shape: ``update_neighbor_lists_``,
+``calculate_new_forces_``, ``do_time_step``, ``run_short_MD_equilibration_``,
+``calculate_full_energy``, ``compute_potential_energy_`` and
+``calculate_full_energy_no_neigh`` dispatch on the neighbour-list object,
+and the driver ``perform_molecular_dynamics_`` is the reference's loop,
+unchanged, written against those generic functions.  With the device-backed
+``NeighborListStruct`` of this module every computation runs in the CUDA
+kernels of libsimmd through its C ABI (``_lib``); any object with the same
+methods (a test's CPU oracle, for instance) can take its place.
+
+Step batching: when the callback is the no-op (``callback=None``, the
+reference's ``cb(x...) = nothing``), ``do_time_step`` on the device list
+records the step instead of running it, and the recorded steps run in one
+device call (CUDA-graph step loop, no host round trip per step) at the next
+step whose state the host can see: a dump step, a log step, the last step,
+or any call that reads the state through the neighbour list.  With any
+other callback every step runs and is copied back before the callback.
 
 Reference map (SimulationCode.jl):
-  initialize_neighbor_struct   src/DataStructs.jl:349-378
-  update_neighbor_lists!       src/NeighborLists.jl:24-53
-  calculate_new_forces!        src/MD.jl:262-316
-  do_time_step                 src/MD.jl:429-471, 499-554
-  rescale_velocities!          src/MD.jl:391-402
-  run_short_MD_equilibration!  src/MD.jl:579-586
-  print_log_data               src/MD.jl:610-650
-  perform_molecular_dynamics!  src/MD.jl:680-719
-  calculate_full_energy        src/AuxiliaryFunctions.jl:22-34
-  find_kinetic_energy          src/AuxiliaryFunctions.jl:57-65
-  compute_potential_energy!    src/AuxiliaryFunctions.jl:186-196
-  logdata                      src/AuxiliaryFunctions.jl:637-646
-  create_when_to_save_array    src/Dump.jl:18-31
+  initialize_neighbor_struct     src/DataStructs.jl:349-378
+  update_neighbor_lists!         src/NeighborLists.jl:24-53
+  calculate_new_forces!          src/MD.jl:262-316
+  do_time_step                   src/MD.jl:429-471, 499-554
+  rescale_velocities!            src/MD.jl:391-402
+  run_short_MD_equilibration!    src/MD.jl:579-586
+  print_log_data                 src/MD.jl:610-650
+  perform_molecular_dynamics!    src/MD.jl:680-719
+  calculate_full_energy          src/AuxiliaryFunctions.jl:22-34
+  find_kinetic_energy            src/AuxiliaryFunctions.jl:57-65
+  calculate_full_energy_no_neigh src/AuxiliaryFunctions.jl:86-110
+  compute_potential_energy!      src/AuxiliaryFunctions.jl:186-196
+  logdata                        src/AuxiliaryFunctions.jl:637-646
+  create_when_to_save_array      src/Dump.jl:18-31
+  save_data                      src/Dump.jl:60-88
 """
 from __future__ import annotations
 
@@ -67,13 +85,46 @@ def make_params(parameters: ParameterStruct, skin: float, force_cutoff: float, *
     return p
 
 
+def logdata(t: int) -> bool:
+    """logdata (src/AuxiliaryFunctions.jl:637-646)."""
+    if t == 0:
+        return True
+    l10 = math.log10(t)
+    return l10 >= 3 and t % (10 ** int(math.floor(l10))) == 0
+
+
+def create_when_to_save_array(log_factor, N_starts, N_max):
+    """create_when_to_save_array (src/Dump.jl:18-31)."""
+    start_times = list(range(0, N_max + 1, max(N_max // N_starts, 1)))
+    when = list(start_times)
+    for s in start_times:
+        t = 1
+        while t <= N_max:
+            when.append(t + s)
+            t = int(math.ceil(t * log_factor))
+    when.append(N_max)
+    return sorted(set(w for w in when if w <= N_max))
+
+
+def _dump_step(parameters, step):
+    di = parameters.dump_info
+    return di is not None and di.save and step in di._when_set()
+
+
 class NeighborListStruct:
     """NeighborListStruct (src/DataStructs.jl:243-257), device-backed.
 
     Holds the scalars of the reference struct; the lists, displacements and
     cell data live on the GPU in the libsimmd context created on first use.
     ``neighbor_numbers_half`` / ``neighbor_list_half`` etc. export the
-    device lists in the reference layout on access."""
+    device lists in the reference layout on access.
+
+    Host/device protocol: the host arrays of ``ArrayStruct`` are pushed to
+    the device before each device operation (``simmd_set_state``, lists
+    kept) and copied back after it, except while steps are recorded for a
+    batched run (``pending``): then the host arrays are those of the last
+    copy-back and are neither read nor written until the recorded steps
+    run."""
 
     def __init__(self, skin_distance, box_size, force_cutoff, N, D_array, dims, maxneighbours=200,
                  precision=_lib.FP64):
@@ -94,6 +145,9 @@ class NeighborListStruct:
         self._lib = _lib.load()
         self._rebuilds_seen = 0
         self.keep_full_list = False
+        self.pending = 0           # recorded steps not yet run on the device
+        self.device_calls = 0      # simmd_step calls made (batching evidence)
+        self._output = None        # OutputStruct of the recorded steps
 
     # -- device context ---------------------------------------------------
     def _ensure(self, arrays: ArrayStruct, parameters: ParameterStruct):
@@ -104,6 +158,7 @@ class NeighborListStruct:
         ctx = C.c_void_p()
         _lib.check(self._lib.simmd_create(C.byref(p), C.byref(ctx)))
         self.ctx = ctx
+        self._params = p
         if self.keep_full_list:
             _lib.check(self._lib.simmd_set_full_list(ctx, 1))
         _lib.check(self._lib.simmd_upload(ctx, _lib.ptr(arrays.r_array), _lib.ptr(arrays.v_array),
@@ -125,10 +180,122 @@ class NeighborListStruct:
         _lib.check(self._lib.simmd_stats_get(self.ctx, C.byref(st)))
         return st
 
-    def _count_rebuilds(self, output: OutputStruct):
+    def _count_rebuilds(self, output):
+        output = output if output is not None else self._output
         rb = self.stats().rebuilds
-        output.N_neighbor_list_rebuilds += rb - self._rebuilds_seen
+        if output is not None:
+            output.N_neighbor_list_rebuilds += rb - self._rebuilds_seen
         self._rebuilds_seen = rb
+
+    def _begin(self, arrays, parameters, output):
+        """before a device operation: create the context, run recorded
+        steps, push the host arrays"""
+        self._ensure(arrays, parameters)
+        if self.pending:
+            self._run(arrays, output, 0)
+        self.push(arrays)
+
+    def _run(self, arrays, output, extra):
+        """run the recorded steps plus ``extra`` from the host state of the
+        last copy-back, then copy back"""
+        n = self.pending + extra
+        self.pending = 0
+        if n == 0:
+            return
+        self.push(arrays)
+        _lib.check(self._lib.simmd_step(self.ctx, int(n), None))
+        self.device_calls += 1
+        self.pull(arrays)
+        self._count_rebuilds(output)
+
+    def flush(self, arrays, parameters, output):
+        """run the recorded steps now (the host arrays become current)"""
+        if self.pending:
+            self._ensure(arrays, parameters)
+            self._run(arrays, output, 0)
+
+    # -- the reference's hot-path functions, device methods ----------------
+    def update_neighbor_lists_(self, arrays, parameters, output):
+        self._begin(arrays, parameters, output)
+        _lib.check(self._lib.simmd_rebuild(self.ctx))
+        self.pull(arrays)
+        self._count_rebuilds(output)
+
+    def calculate_new_forces_(self, arrays, parameters, noise=None):
+        self._begin(arrays, parameters, None)
+        nz = _lib.f64(noise, (parameters.N, parameters.system.dims)) if noise is not None else None
+        _lib.check(self._lib.simmd_forces(self.ctx, _lib.ptr(nz), _lib.ptr(arrays.F_array)))
+        if nz is not None:
+            arrays.random_displacement[:] = nz
+
+    def do_time_step(self, arrays, parameters, output, system, noise=None, nsteps=1):
+        self._ensure(arrays, parameters)
+        if noise is None and nsteps == 1 and parameters.callback is None:
+            # batch: record the step unless the host sees the state after it
+            # (output.steps_done is advanced by the driver after this call)
+            step = output.steps_done + 1
+            self._output = output
+            if not (_dump_step(parameters, step) or logdata(step) or step >= parameters.N_steps):
+                self.pending += 1
+                return
+            self._run(arrays, output, 1)
+            return
+        self._begin(arrays, parameters, output)
+        nz = None
+        if noise is not None:
+            nz = _lib.f64(noise, (nsteps, parameters.N, parameters.system.dims))
+        _lib.check(self._lib.simmd_step(self.ctx, int(nsteps), _lib.ptr(nz)))
+        self.device_calls += 1
+        self.pull(arrays)
+        self._count_rebuilds(output)
+
+    def run_short_MD_equilibration_(self, arrays, parameters, output):
+        self.update_neighbor_lists_(arrays, parameters, output)
+        if parameters.N_MD_equilibration_steps > 0:
+            self.do_time_step(arrays, parameters, output, parameters.system,
+                              nsteps=parameters.N_MD_equilibration_steps)
+
+    def calculate_full_energy(self, arrays, parameters):
+        self._begin(arrays, parameters, None)
+        e = C.c_double()
+        _lib.check(self._lib.simmd_energy(self.ctx, C.byref(e), None, None))
+        return e.value
+
+    def calculate_virial(self, arrays, parameters):
+        self._begin(arrays, parameters, None)
+        w = C.c_double()
+        _lib.check(self._lib.simmd_energy(self.ctx, None, C.byref(w), None))
+        return w.value
+
+    def compute_potential_energy_(self, arrays, parameters, output):
+        self._begin(arrays, parameters, output)
+        _lib.check(self._lib.simmd_potential_energy_array(self.ctx, _lib.ptr(arrays.potential_energy_array)))
+
+    def calculate_full_energy_no_neigh(self, arrays, parameters):
+        """the reference's E_pot_test cross-check: the energy of the current
+        positions from lists built afresh (a temporary context: cell binning
+        and Verlet build of the positions as they are now, then the energy
+        pass), independent of the running lists and their skin bookkeeping"""
+        self._begin(arrays, parameters, None)
+        tmp = C.c_void_p()
+        _lib.check(self._lib.simmd_create(C.byref(self._params), C.byref(tmp)))
+        try:
+            _lib.check(self._lib.simmd_upload(tmp, _lib.ptr(arrays.r_array), None, None, _lib.ptr(arrays.D_array),
+                                              None))
+            e = C.c_double()
+            _lib.check(self._lib.simmd_energy(tmp, C.byref(e), None, None))
+        finally:
+            self._lib.simmd_destroy(tmp)
+        return e.value
+
+    def find_inherent_structure(self, arrays, parameters, tolerance, max_iterations, max_step_size, dt):
+        self._begin(arrays, parameters, None)
+        it = (C.c_int64 * 1)()
+        st = self._lib.simmd_inherent_structure(self.ctx, float(tolerance), int(max_iterations),
+                                                float(max_step_size), float(dt), it)
+        self.pull(arrays)
+        _lib.check(st)
+        return int(it[0])
 
     def _export(self, which):
         K = self.maxneighbours
@@ -168,132 +335,89 @@ def initialize_neighbor_struct(skin_distance, box_size, force_cutoff, N, D_array
     return NeighborListStruct(skin_distance, box_size, force_cutoff, N, D_array, dims, maxneighbours, precision)
 
 
-def update_neighbor_lists_(arrays, parameters, output, neighborlist: NeighborListStruct):
+# ---------------------------------------------------------------------------
+# generic functions: dispatch on the neighbour list, as the reference's
+# methods dispatch on their argument types
+# ---------------------------------------------------------------------------
+def update_neighbor_lists_(arrays, parameters, output, neighborlist):
     """update_neighbor_lists! (src/NeighborLists.jl:24-53)."""
-    neighborlist._ensure(arrays, parameters)
-    neighborlist.push(arrays)
-    _lib.check(neighborlist._lib.simmd_rebuild(neighborlist.ctx))
-    neighborlist.pull(arrays)
-    neighborlist._count_rebuilds(output)
+    neighborlist.update_neighbor_lists_(arrays, parameters, output)
 
 
-def calculate_new_forces_(arrays, parameters, neighborlist: NeighborListStruct, noise=None):
+def calculate_new_forces_(arrays, parameters, neighborlist, noise=None):
     """calculate_new_forces! (src/MD.jl:262-316).  ``noise`` (N, dims): the
     N(0,1) deviates of this call's random force (default: the Philox stream)."""
-    neighborlist._ensure(arrays, parameters)
-    neighborlist.push(arrays)
-    nz = _lib.f64(noise, (parameters.N, parameters.system.dims)) if noise is not None else None
-    _lib.check(neighborlist._lib.simmd_forces(neighborlist.ctx, _lib.ptr(nz), _lib.ptr(arrays.F_array)))
-    if nz is not None:
-        arrays.random_displacement[:] = nz
+    neighborlist.calculate_new_forces_(arrays, parameters, noise)
 
 
-def do_time_step(arrays, parameters, output, neighborlist: NeighborListStruct, system=None, noise=None,
-                 nsteps=1):
+def do_time_step(arrays, parameters, output, neighborlist, system=None, noise=None, nsteps=1):
     """do_time_step (src/MD.jl:429-471, 499-554); ``nsteps`` > 1 runs that
     many steps in one device call.  ``noise``: (nsteps, N, dims) deviates."""
-    neighborlist._ensure(arrays, parameters)
-    neighborlist.push(arrays)
-    nz = None
-    if noise is not None:
-        nz = _lib.f64(noise, (nsteps, parameters.N, parameters.system.dims))
-    _lib.check(neighborlist._lib.simmd_step(neighborlist.ctx, int(nsteps), _lib.ptr(nz)))
-    neighborlist.pull(arrays)
-    neighborlist._count_rebuilds(output)
+    neighborlist.do_time_step(arrays, parameters, output, parameters.system if system is None else system,
+                              noise=noise, nsteps=nsteps)
 
 
-def find_inherent_structure(arrays, parameters, neighborlist: NeighborListStruct, tolerance=1e-6,
-                            max_iterations=10 ** 6, max_step_size=0.001, dt=0.005):
+def run_short_MD_equilibration_(arrays, parameters, output, neighborlist):
+    """run_short_MD_equilibration! (src/MD.jl:579-586)."""
+    neighborlist.run_short_MD_equilibration_(arrays, parameters, output)
+
+
+def calculate_full_energy(arrays, parameters, neighborlist):
+    """calculate_full_energy (src/AuxiliaryFunctions.jl:22-34)."""
+    return neighborlist.calculate_full_energy(arrays, parameters)
+
+
+def calculate_virial(arrays, parameters, neighborlist):
+    """W = sum over pairs of r_ij . F_ij (not in the reference)."""
+    return neighborlist.calculate_virial(arrays, parameters)
+
+
+def compute_potential_energy_(arrays, parameters, output, neighborlist):
+    """compute_potential_energy! (src/AuxiliaryFunctions.jl:186-196)."""
+    neighborlist.compute_potential_energy_(arrays, parameters, output)
+
+
+def calculate_full_energy_no_neigh(arrays, parameters, neighborlist):
+    """calculate_full_energy_no_neigh (src/AuxiliaryFunctions.jl:86-110):
+    the energy without the running neighbour lists (E_pot_test)."""
+    return neighborlist.calculate_full_energy_no_neigh(arrays, parameters)
+
+
+def find_inherent_structure(arrays, parameters, neighborlist, tolerance=1e-6, max_iterations=10 ** 6,
+                            max_step_size=0.001, dt=0.005):
     """find_inherent_structure (src/InherentStructure.jl:5-56): steepest
     descent of the positions to the nearest local minimum on the device.
     Returns the iteration count; raises if max_iterations is reached (the
     reference's intent; its own error path raises a MethodError)."""
-    neighborlist._ensure(arrays, parameters)
-    neighborlist.push(arrays)
-    it = (C.c_int64 * 1)()
-    st = neighborlist._lib.simmd_inherent_structure(neighborlist.ctx, float(tolerance), int(max_iterations),
-                                                    float(max_step_size), float(dt), it)
-    neighborlist.pull(arrays)
-    _lib.check(st)
-    return int(it[0])
-
-
-def calculate_full_energy(arrays, parameters, neighborlist: NeighborListStruct):
-    """calculate_full_energy (src/AuxiliaryFunctions.jl:22-34)."""
-    neighborlist._ensure(arrays, parameters)
-    neighborlist.push(arrays)
-    e = C.c_double()
-    _lib.check(neighborlist._lib.simmd_energy(neighborlist.ctx, C.byref(e), None, None))
-    return e.value
-
-
-def calculate_virial(arrays, parameters, neighborlist: NeighborListStruct):
-    """W = sum over pairs of r_ij . F_ij (not in the reference)."""
-    neighborlist._ensure(arrays, parameters)
-    neighborlist.push(arrays)
-    w = C.c_double()
-    _lib.check(neighborlist._lib.simmd_energy(neighborlist.ctx, None, C.byref(w), None))
-    return w.value
+    return neighborlist.find_inherent_structure(arrays, parameters, tolerance, max_iterations, max_step_size, dt)
 
 
 def find_kinetic_energy(arrays, parameters, output):
-    """find_kinetic_energy (src/AuxiliaryFunctions.jl:57-65): host O(N) sum."""
+    """find_kinetic_energy (src/AuxiliaryFunctions.jl:57-65)."""
     v = arrays.v_array
-    output.kinetic_energy = float(((v * v).sum(1)).sum()) * (parameters.system.m / 2.0)
-
-
-def compute_potential_energy_(arrays, parameters, output, neighborlist: NeighborListStruct):
-    """compute_potential_energy! (src/AuxiliaryFunctions.jl:186-196)."""
-    neighborlist._ensure(arrays, parameters)
-    neighborlist.push(arrays)
-    _lib.check(neighborlist._lib.simmd_potential_energy_array(neighborlist.ctx,
-                                                              _lib.ptr(arrays.potential_energy_array)))
+    # the reference's order: per particle sum(v.^2), accumulated in turn
+    ekin = float(np.cumsum((v * v).sum(1))[-1])
+    output.kinetic_energy = ekin * (parameters.system.m / 2.0)
 
 
 def rescale_velocities_(v_array, parameters):
     """rescale_velocities! (src/MD.jl:391-402)."""
     dims = parameters.system.dims
-    ekin = float((v_array * v_array).sum()) * (parameters.system.m / 2.0)
+    ekin = float(np.cumsum((v_array * v_array).sum(1))[-1])
+    ekin *= parameters.system.m / 2.0
     kbt = 2 * ekin / (dims * parameters.N)
     v_array *= math.sqrt(parameters.system.kBT / kbt)
 
 
-def run_short_MD_equilibration_(arrays, parameters, output, neighborlist):
-    """run_short_MD_equilibration! (src/MD.jl:579-586)."""
-    update_neighbor_lists_(arrays, parameters, output, neighborlist)
-    if parameters.N_MD_equilibration_steps > 0:
-        do_time_step(arrays, parameters, output, neighborlist, nsteps=parameters.N_MD_equilibration_steps)
-
-
-def logdata(t: int) -> bool:
-    """logdata (src/AuxiliaryFunctions.jl:637-646)."""
-    if t == 0:
-        return True
-    l10 = math.log10(t)
-    return l10 >= 3 and t % (10 ** int(math.floor(l10))) == 0
-
-
-def create_when_to_save_array(log_factor, N_starts, N_max):
-    """create_when_to_save_array (src/Dump.jl:18-31)."""
-    start_times = list(range(0, N_max + 1, max(N_max // N_starts, 1)))
-    when = list(start_times)
-    for s in start_times:
-        t = 1
-        while t <= N_max:
-            when.append(t + s)
-            t = int(math.ceil(t * log_factor))
-    when.append(N_max)
-    return sorted(set(w for w in when if w <= N_max))
-
-
 def save_data(arrays, parameters, output, neighborlist, restarted):
     """save_data (src/Dump.jl:60-88): at dump steps rebuild the lists (when not
-    restarted, as the reference does) and hand the arrays to the writer."""
+    restarted, as the reference does) and hand the arrays to the writer (the
+    reference writes them to HDF5)."""
     di = parameters.dump_info
-    if di is None or not di.save or output.steps_done not in set(di.when_to_save_array):
+    if di is None or not (di.save and output.steps_done in di._when_set()):
         return
-    if not restarted:
-        update_neighbor_lists_(arrays, parameters, output, neighborlist)
+    elif not restarted:
+        update_neighbor_lists_(arrays, parameters, output, neighborlist)  # for complete reproducibility
     out = {}
     if di.save_r:
         out["positions"] = arrays.r_array.copy()
@@ -310,39 +434,49 @@ def save_data(arrays, parameters, output, neighborlist, restarted):
         di.writer(output.steps_done, out)
 
 
-def print_log_data(arrays, parameters, output, neighborlist, start_time):
-    """print_log_data (src/MD.jl:610-650) without q4/q6/F2s (out of scope)."""
-    output.potential_energy = calculate_full_energy(arrays, parameters, neighborlist)
-    if isinstance(parameters.system, Brownian):
-        output.kinetic_energy = 0.0
-    else:
-        find_kinetic_energy(arrays, parameters, output)
+def print_log_data(arrays, parameters, output, neighborlist, start_time, log=print):
+    """print_log_data (src/MD.jl:610-650) without q4/q6/F2s (out of scope),
+    with the E_pot_test cross-check.  Returns the logged values."""
     el = time.time() - start_time
-    eta = el / max(output.steps_done, 1) * (parameters.N_steps - output.steps_done)
-    print("%d/%d, ETA = %.1f, E = %.2f,  E_pot = %.12f,  E_kin = %.2f, kT = %.3f" % (
-        output.steps_done, parameters.N_steps, eta, output.potential_energy + output.kinetic_energy,
-        output.potential_energy, output.kinetic_energy,
-        output.kinetic_energy * 2 / parameters.system.dims / parameters.N), flush=True)
+    remaining = el / max(output.steps_done, 1) * (parameters.N_steps - output.steps_done)
+    output.potential_energy = calculate_full_energy(arrays, parameters, neighborlist)
+    if not isinstance(parameters.system, Brownian):
+        find_kinetic_energy(arrays, parameters, output)
+    else:
+        output.kinetic_energy = 0.0
+    energy_no_neigh = calculate_full_energy_no_neigh(arrays, parameters, neighborlist)
+    if log is not None:
+        log("%d/%d, ETA = %.1f, E = %.2f,  E_pot = %.12f,  E_pot_test = %.12f,  E_kin = %.2f, kT = %.3f" % (
+            output.steps_done, parameters.N_steps, remaining, output.potential_energy + output.kinetic_energy,
+            output.potential_energy, energy_no_neigh, output.kinetic_energy,
+            output.kinetic_energy * 2 / parameters.system.dims / parameters.N))
+    return {"step": output.steps_done, "E_pot": output.potential_energy, "E_pot_test": energy_no_neigh,
+            "E_kin": output.kinetic_energy}
 
 
 def perform_molecular_dynamics_(arrays, parameters, output, neighborlist, restarted=False,
-                                equilibrate_velocities=True, new_file=True, log=True, rng=None):
-    """perform_molecular_dynamics! (src/MD.jl:680-719).
+                                equilibrate_velocities=True, new_file=True, log=print, rng=None):
+    """perform_molecular_dynamics! (src/MD.jl:680-719), the reference's loop.
 
-    Steps between host-visible events (callback, dump steps, log steps) run
-    in one device call; with ``callback=None`` (the reference's no-op
-    ``cb(x...) = nothing``) only dump and log steps synchronise."""
+    ``rng`` draws the velocity randomisation (the reference's ``randn!`` on
+    the global generator; default: seeded by ``parameters.random_seed``).
+    ``log`` receives the printed lines (None: silent).  Returns the list of
+    logged values (one dict per log step)."""
+    say = log if log is not None else (lambda m: None)
+    say("\n\nStarting MD procedure")
     arrays.r_old_array[:] = arrays.r_array
     sysm = parameters.system
     if not restarted and equilibrate_velocities and not isinstance(sysm, Brownian):
         rng = rng if rng is not None else np.random.default_rng(parameters.random_seed)
-        arrays.v_array[:] = rng.standard_normal(arrays.v_array.shape) * math.sqrt(sysm.kBT / sysm.m)
+        arrays.v_array[:] = rng.standard_normal(arrays.v_array.shape)
+        arrays.v_array *= math.sqrt(sysm.kBT / sysm.m)
     if not restarted:
         output.steps_done = 0
+    say("Running production MD")
     update_neighbor_lists_(arrays, parameters, output, neighborlist)
     if equilibrate_velocities:
         run_short_MD_equilibration_(arrays, parameters, output, neighborlist)
-        if not isinstance(sysm, Brownian):
+        if not isinstance(sysm, Brownian):  # a Brownian system has no velocities
             rescale_velocities_(arrays.v_array, parameters)
     output.potential_energy = calculate_full_energy(arrays, parameters, neighborlist)
     output.N_neighbor_list_rebuilds = 0
@@ -351,40 +485,19 @@ def perform_molecular_dynamics_(arrays, parameters, output, neighborlist, restar
     cb = parameters.callback
     if cb is not None:
         cb(arrays, parameters, output, neighborlist)
-    di = parameters.dump_info
-    dump_steps = set(di.when_to_save_array) if (di is not None and di.save) else set()
-    start = time.time()
+    start_time = time.time()
+    logged = []
     while output.steps_done < parameters.N_steps:
-        # next host-visible step
-        t = output.steps_done + 1
-        if cb is None:
-            nxt = parameters.N_steps
-            for s in dump_steps:
-                if t <= s < nxt:
-                    nxt = s
-            if log:
-                k = t
-                while k < nxt and not logdata(k):
-                    k = _next_log(k, nxt)
-                nxt = min(nxt, k)
-            n = max(nxt - output.steps_done, 1)
-        else:
-            n = 1
-        do_time_step(arrays, parameters, output, neighborlist, nsteps=n)
-        output.steps_done += n
+        do_time_step(arrays, parameters, output, neighborlist, parameters.system)
+        output.steps_done += 1
         if cb is not None:
             cb(arrays, parameters, output, neighborlist)
         save_data(arrays, parameters, output, neighborlist, restarted)
-        if log and logdata(output.steps_done):
-            print_log_data(arrays, parameters, output, neighborlist, start)
-    if log:
-        print("MD procedure complete")
-        print("Number of neighbor lists built = %d" % output.N_neighbor_list_rebuilds)
-
-
-def _next_log(k, limit):
-    """smallest t > k with logdata(t), capped at limit."""
-    if k < 1000:
-        return min(limit, 1000)
-    p = 10 ** int(math.floor(math.log10(k)))
-    return min(limit, (k // p + 1) * p)
+        if logdata(output.steps_done):
+            logged.append(print_log_data(arrays, parameters, output, neighborlist, start_time, log))
+    flush = getattr(neighborlist, "flush", None)
+    if flush is not None:  # N_steps <= steps_done on entry leaves nothing recorded; kept for safety
+        flush(arrays, parameters, output)
+    say("MD procedure complete")
+    say("Number of neighbor lists built = %d" % output.N_neighbor_list_rebuilds)
+    return logged

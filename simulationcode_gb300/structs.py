@@ -92,6 +92,14 @@ class DumpInfo:
     save_Epot: bool = False
     writer: Optional[Callable[[int, dict], None]] = None
 
+    def _when_set(self) -> frozenset:
+        """when_to_save_array as a set (membership test of save_data)"""
+        key = tuple(self.when_to_save_array)
+        if getattr(self, "_when_key", None) != key:
+            self._when_key = key
+            self._when = frozenset(key)
+        return self._when
+
 
 @dataclasses.dataclass
 class ParameterStruct:

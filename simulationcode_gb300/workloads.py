@@ -110,15 +110,34 @@ def c4_sizes(nrep=512, seed=4, lo=500, hi=16384):
     return np.floor(np.exp(rng.uniform(math.log(lo), math.log(hi), nrep))).astype(int)
 
 
-def c4(precision=_lib.FP32_SPLIT, seed=4, nrep=512):
+def c4(precision=_lib.FP32_SPLIT, seed=4, nrep=512, indices=None):
+    """the batch of ``nrep`` replicas; ``indices``: only those replicas (each
+    replica depends only on (seed, its index), so a subset equals the same
+    replicas of the whole batch)"""
     sizes = c4_sizes(nrep, seed)
     specs = []
-    for k, N in enumerate(sizes):
+    for k in (range(nrep) if indices is None else indices):
         rng = np.random.default_rng(seed * 100003 + k)
         dims = 2 if k % 2 == 0 else 3
-        specs.append(berthier_spec(int(N), dims, _lib.BROWNIAN, rng, dt=1e-3, precision=precision,
+        specs.append(berthier_spec(int(sizes[k]), dims, _lib.BROWNIAN, rng, dt=1e-3, precision=precision,
                                    seed=seed * 1000 + k))
     return specs
+
+
+def lpt_partition(work, nparts):
+    """longest-processing-time assignment of independent replicas to
+    ``nparts`` GPUs: replicas in decreasing order of work (particles x
+    steps), each to the GPU with the least work so far (ties: the lower
+    GPU index, then the lower replica index); returns one sorted list of
+    replica indices per GPU"""
+    import heapq
+    heap = [(0, g) for g in range(nparts)]
+    parts = [[] for _ in range(nparts)]
+    for k in sorted(range(len(work)), key=lambda k: (-work[k], k)):
+        load, g = heapq.heappop(heap)
+        parts[g].append(k)
+        heapq.heappush(heap, (load + work[k], g))
+    return [sorted(p) for p in parts]
 
 
 def c5_draw(rng, nmin=256, nmax=65536, smin=10 ** 3, smax=10 ** 5):

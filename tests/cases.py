@@ -56,3 +56,27 @@ def make_case(pot, dims, dyn, N, *, rho=None, skin=0.3, seed=0, mc_sweeps=40, dt
         v = rng.standard_normal((N, dims)) * math.sqrt(kBT)
         v -= v.mean(0)
     return p, r, v, D, rc
+
+
+def md_case(N=1000, dims=3, *, dt=0.002, N_steps=1000, N_eq=20, log_factor=1.5, N_starts=2, seed=3,
+            callback=None):
+    """(arrays, parameters, output, dumps) of an LJ system (rho = 1,
+    jittered simple lattice, eps = sigma = 1, rc = 2.5, Newtonian) set up
+    through the reference's structs for perform_molecular_dynamics!, with a
+    dump schedule from create_when_to_save_array whose writer records every
+    dump into ``dumps``"""
+    from simulationcode_gb300 import md
+    from simulationcode_gb300.structs import ArrayStruct, DumpInfo, LJ, Newtonian, OutputStruct, ParameterStruct
+    rng = np.random.default_rng(seed)
+    L = float(N) ** (1.0 / dims)
+    U = LJ(1.0, 1.0, 2.5)
+    dumps = {}
+    di = DumpInfo(True, "unused.h5", md.create_when_to_save_array(log_factor, N_starts, N_steps),
+                  save_r=True, save_v=True, save_F=True, save_Epot=True,
+                  writer=lambda step, d: dumps.__setitem__(step, d))
+    params = ParameterStruct(N_eq, seed, 1.0, N, L, N_steps, 0.0, 0.1, U.rc ** 2, 0.0,
+                             Newtonian(0.1, dt, 1.0, False, dims), U, dump_info=di, callback=callback)
+    arrays = ArrayStruct(N, dims)
+    arrays.r_array[:] = lattice_positions(N, dims, L, 0.05, rng)
+    arrays.D_array[:] = 1.0
+    return arrays, params, OutputStruct(), dumps

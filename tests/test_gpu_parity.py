@@ -200,11 +200,3 @@ def test_split_conversions_match_hardware(simlib):
     for seed in (1, 2):
         assert simlib.simmd_check_conversions(1 << 24, seed, C.byref(bad)) == 0
         assert bad.value == 0
-
-
-def test_pipe_rate_probe_runs(simlib):
-    """The pipe-rate probe returns a positive rate for each of its six
-    probes (the figures themselves are hardware facts, not checked)."""
-    from simulationcode_gb300 import devinfo
-    r = devinfo.pipe_rates()
-    assert len(r) == 6 and all(v > 0 for v in r.values())
