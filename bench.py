@@ -191,6 +191,28 @@ def force_bytes_per_launch(specs, stats):
     return total
 
 
+def state_bytes(specs):
+    """bytes of the particle state every step reads and writes (positions,
+    velocities, forces, displacements in FP64), for the L2 statement"""
+    return sum(s.N * 8 * s.dims * 4 for s in specs)
+
+
+def workload_config(workload, specs, n_particles, n_replicas, tuned):
+    """the ``config`` object both arms print: the workload, its size and the
+    tuning's skins (the rebuild cadence), identical in the GPU arm and the
+    reference arm"""
+    from simulationcode_gb300 import workloads as W
+    from simulationcode_gb300.autotune import group_key, skin_for
+    skins = {}
+    for s in specs:
+        skins[group_key(s)] = skin_for(tuned, s)
+    sb = state_bytes(specs)
+    return {"workload": workload, "description": W.DESCRIPTIONS[workload], "particles": int(n_particles),
+            "replicas": int(n_replicas), "skins": dict(sorted(skins.items())),
+            "l2": ("state larger than L2 (%.0f MB of particle state per step), no flush" % (sb / 1e6))
+                  if sb > 129e6 else "state fits in L2 (%.0f MB of particle state)" % (sb / 1e6)}
+
+
 def build_batch(specs, device, tpp):
     from simulationcode_gb300.batch import ReplicaBatch
     b = ReplicaBatch(device, tpp=tpp, graphs=True, graph_steps=16)
@@ -389,10 +411,14 @@ def run_reference(args, dist):
     restatement of the Julia routines; Julia itself is not available) on the
     host cores, threads over replicas."""
     from concurrent.futures import ThreadPoolExecutor
-    from simulationcode_gb300 import workloads as W
+    from simulationcode_gb300 import autotune as AT, workloads as W
     from oracle import build as ob, pyoracle as O
     ob.build_oracle()
     specs = W.WORKLOADS[args.workload](precision=0)
+    # the GPU arm's tuning: the same skin (rebuild cadence) per replica group
+    tuned = AT.load_tuned(args.workload) if args.autotune == "stored" else None
+    for s in specs:
+        s.skin = AT.skin_for(tuned, s)
     # bounded sample: a prefix of the replicas sized so that set-up, warm-up
     # and timed steps take about two minutes at a conservative 1e6
     # particle-steps/s per thread
@@ -439,8 +465,8 @@ def run_reference(args, dist):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * dt / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic", "impl": "reference",
-            "config": {"workload": args.workload, "description": W.DESCRIPTIONS[args.workload],
-                       "particles": n, "replicas": len(systems), "parallelism": "threads over replicas"},
+            "config": workload_config(args.workload, [s for s, _ in systems], n, len(systems), tuned or {}),
+            "run": {"parallelism": "threads over replicas", "threads": cores},
             "cpu_baseline": {"value": value, "unit": "particle-steps/s", "cores": cores, "kind": "port",
                              "sample": "%s, %d timed steps" % (sample, args.steps)},
             "e2e": {"value": value, "unit": "particle-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -462,18 +488,25 @@ def run_gpu(args, dist):
         relax_launches[0] += counts[0]
         relax_counts[0] += counts[1]
         relax_counts[1] += counts[2]
+    from simulationcode_gb300 import autotune as AT
+    tuned = AT.load_tuned(args.workload) if args.autotune == "stored" else None
+    if tuned is not None:
+        args.tpp = int(tuned.get("tpp", args.tpp))
     batch, ids = build_batch(specs, device, args.tpp)
     if args.skin is not None:
         batch.set_skin(args.skin)
+        tuned = None
     batch.rebuild()
     tune = None
-    if args.autotune:
-        from simulationcode_gb300.autotune import autotune
+    if tuned is not None:
+        AT.apply_tuned(batch, tuned, graphs=args.graphs)
+    elif args.autotune == "live":
         skins = [float(x) for x in args.tune_skins.split(",")] if args.tune_skins else None
-        tune = autotune(batch, tpps=(1, 2, 4, 8), skins=skins,
-                        log=lambda m: print(m, file=sys.stderr, flush=True),
-                        group_by=lambda sp: "%dD" % sp.dims)
+        tune = AT.autotune(batch, tpps=(1, 2, 4, 8), skins=skins,
+                           log=lambda m: print(m, file=sys.stderr, flush=True), group_by=AT.group_key)
         args.tpp = tune.tpp
+        tuned = AT.as_tuned(tune, batch)
+        print("TUNED %s %s" % (args.workload, json.dumps(tuned)), file=sys.stderr, flush=True)
     if not args.graphs:
         batch.set_tuning(args.tpp, False, 16)
     batch.step(args.warmup)
@@ -526,42 +559,44 @@ def run_gpu(args, dist):
             traffic = None
 
     # e2e through the C ABI: host (page-locked) arrays -> device, K steps,
-    # device -> host, for every replica
-    host = []
-    h2d = d2h = 0
-    for s in specs:
-        r = np.ascontiguousarray(s.r, dtype=np.float64)
-        v = np.ascontiguousarray(s.v if s.v is not None else np.zeros_like(r))
-        D = np.ascontiguousarray(s.D, dtype=np.float64)
-        F = np.zeros_like(r)
-        outs = [np.zeros_like(r) for _ in range(3)]
-        for a in [r, v, D, F] + outs:
-            lib.simmd_host_register(C.c_void_p(a.ctypes.data), a.nbytes)
-        host.append((r, v, D, F, outs))
-        h2d += r.nbytes + D.nbytes + (v.nbytes if s.dynamics != 2 else 0)
-        d2h += r.nbytes + F.nbytes + (v.nbytes if s.dynamics != 2 else 0)
+    # device -> host, every replica at once (simmd_upload_all /
+    # simmd_download_all: one copy per array, one synchronisation)
+    total, offs = batch.transfer_layout()
+    any_v = any(s.dynamics != 2 for s in specs)
+    r_all = np.zeros(total)
+    v_all = np.zeros(total) if any_v else None
+    D_all = np.zeros(sum(s.N for s in specs))
+    outs = [np.zeros(total), np.zeros(total) if any_v else None, np.zeros(total)]
+    doff = 0
+    for rid, s in sorted(zip(ids, specs), key=lambda t: t[0]):
+        o = offs[rid]
+        r_all[o:o + s.N * s.dims] = np.asarray(s.r, dtype=np.float64).reshape(-1)
+        if any_v and s.v is not None:
+            v_all[o:o + s.N * s.dims] = np.asarray(s.v, dtype=np.float64).reshape(-1)
+        D_all[doff:doff + s.N] = s.D
+        doff += s.N
+    host = [a for a in [r_all, v_all, D_all] + outs if a is not None]
+    for a in host:
+        _lib.check(lib.simmd_host_register(C.c_void_p(a.ctypes.data), a.nbytes))
+    h2d = r_all.nbytes + D_all.nbytes + (v_all.nbytes if any_v else 0)
+    d2h = outs[0].nbytes + outs[2].nbytes + (outs[1].nbytes if any_v else 0)
     e2e_steps = args.steps
     dist.barrier()
     if args.no_e2e:
         e2e_steps = 0
     t0 = time.perf_counter()
-    for rid, s, (r, v, D, F, outs) in zip(ids, specs, host):
-        _lib.check(lib.simmd_upload_r(batch.ctx, rid, _lib.ptr(r), _lib.ptr(v) if s.dynamics != 2 else None,
-                                      None, _lib.ptr(D), None))
+    batch.upload_all(r_all, D_all, v=v_all)
     if e2e_steps:
         _lib.check(lib.simmd_step(batch.ctx, e2e_steps, None))
-    for rid, s, (r, v, D, F, outs) in zip(ids, specs, host):
-        _lib.check(lib.simmd_download_r(batch.ctx, rid, _lib.ptr(outs[0]),
-                                        _lib.ptr(outs[1]) if s.dynamics != 2 else None, _lib.ptr(outs[2]), None))
+    batch.download_all(outs[0], outs[1], outs[2])
     e2e_s = dist.max(time.perf_counter() - t0)
-    for (r, v, D, F, outs) in host:
-        for a in [r, v, D, F] + outs:
-            lib.simmd_host_unregister(C.c_void_p(a.ctypes.data))
+    for a in host:
+        lib.simmd_host_unregister(C.c_void_p(a.ctypes.data))
     e2e_steps = max(e2e_steps, 1)
     e2e = {"value": n_all * e2e_steps / e2e_s, "unit": "particle-steps/s",
            "h2d_bytes_per_step": h2d / e2e_steps, "d2h_bytes_per_step": d2h / e2e_steps,
-           "what": "simmd_upload_r (r, v, D from page-locked host) + simmd_step(K) + simmd_download_r (r, v, F) "
-                   "for every replica, wall clock"}
+           "what": "simmd_upload_all (r, %sD of every replica from page-locked host arrays) + simmd_step(K) + "
+                   "simmd_download_all (r, %sF), wall clock" % ("v, " if any_v else "", "v, " if any_v else "")}
 
     # bytes streamed per step: force launch + positions, velocities, forces,
     # displacements of the integrator pass
@@ -570,20 +605,17 @@ def run_gpu(args, dist):
     line = {"metric": "particle-steps/s", "value": value, "unit": "particle-steps/s", "n_gpus": dist.ws,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": dtype, "data": "synthetic",
-            "config": {"workload": args.workload, "description": W.DESCRIPTIONS[args.workload],
-                       "particles": int(n_all), "particles_per_rank": n,
-                       "replicas": len(specs), "threads_per_particle": args.tpp,
-                       "l2": ("state larger than L2 (%.0f MB streamed per step)" % (step_bytes / 1e6))
-                             if step_bytes > 129e6 else "state fits in L2 (%.0f MB; no flush)" % (step_bytes / 1e6),
-                       "parallelism": ("LPT replica partition over %d ranks" % dist.ws) if dist.ws > 1
-                                      else "single GPU",
-                       "rebuilds_in_timed_region": rebuilds,
-                       "step_loop": "CUDA graph of 16 steps" if args.graphs else "direct launches",
-                       "skin": specs[0].skin,
-                       "autotune": None if tune is None else {"tpp": tune.tpp, "skin": tune.skin,
-                                                              "group_skins": tune.group_skins,
-                                                              "graph_steps": tune.graph_steps,
-                                                              "trials": tune.trials}},
+            "config": workload_config(args.workload, specs, n_all, int(dist.sum(len(specs))), tuned or {}),
+            "run": {"particles_per_rank": n, "replicas_per_rank": len(specs), "threads_per_particle": args.tpp,
+                    "bytes_streamed_per_step": step_bytes,
+                    "parallelism": ("LPT replica partition over %d ranks" % dist.ws) if dist.ws > 1
+                                   else "single GPU",
+                    "rebuilds_in_timed_region": rebuilds,
+                    "step_loop": "CUDA graph of 16 steps" if args.graphs else "direct launches",
+                    "tuning": {"source": {"stored": "simulationcode_gb300/tuned.json (autotuner result)",
+                                          "live": "autotuner, this run"}.get(args.autotune, "none"),
+                               "tuned": tuned,
+                               "trials": None if tune is None else tune.trials}},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
                          "kernel": "k_force", "force_ms_per_launch": force_ms,
@@ -641,8 +673,10 @@ def main():
     ap.add_argument("--no-graphs", dest="graphs", action="store_false",
                     help="direct launches instead of the captured step loop (for per-kernel profiling: ncu does not "
                          "profile kernel nodes of graphs with conditional nodes)")
-    ap.add_argument("--no-autotune", dest="autotune", action="store_false",
-                    help="skip the autotuner (threads per particle, skin / rebuild cadence)")
+    ap.add_argument("--autotune", default="stored", choices=["stored", "live", "off"],
+                    help="tuning (threads per particle, per-group skin = rebuild cadence): the autotuner's stored "
+                         "result (simulationcode_gb300/tuned.json, the default, shared with the reference arm), "
+                         "a live autotuner run, or none")
     ap.add_argument("--tune-skins", default="0.3,0.4,0.5,0.6,0.7",
                     help="skins the autotuner may choose from (the rebuild cadence); empty: keep the configured skin")
     ap.add_argument("--serve-seconds", type=float, default=30.0,

@@ -176,6 +176,22 @@ int simmd_upload_r(simmd_ctx* ctx, int32_t rep, const double* r, const double* v
 int simmd_download_r(simmd_ctx* ctx, int32_t rep, double* r, double* v, double* F, double* disp);
 int simmd_set_state_r(simmd_ctx* ctx, int32_t rep, const double* r, const double* v, const double* F,
                       const double* disp);
+/* Batched host transfers (no counterpart in the reference, which holds one
+ * system): every replica of the context in one call, with one host <->
+ * device copy per array and one synchronisation.  Host layout: the active
+ * replicas in increasing replica id, each its ArrayStruct block (dims x N
+ * AoS) one after the other; D: each replica's N diameters one after the
+ * other.  simmd_transfer_layout returns the total number of doubles of a
+ * dims x N array (-1: NULL context) and, if offsets is not NULL, fills
+ * offsets[rep] for rep < n with the replica's first double (-1 for ids not
+ * in use).  simmd_upload_all = simmd_upload_r of every
+ * replica (r, D required; v, F, disp may be NULL = zeros); simmd_download_all
+ * = simmd_download_r of every replica (any pointer may be NULL).  Host
+ * arrays page-locked with simmd_host_register transfer at full link speed. */
+int64_t simmd_transfer_layout(simmd_ctx* ctx, int32_t n, int64_t* offsets);
+int simmd_upload_all(simmd_ctx* ctx, const double* r, const double* v, const double* F, const double* D,
+                     const double* disp);
+int simmd_download_all(simmd_ctx* ctx, double* r, double* v, double* F, double* disp);
 /* find_inherent_structure (src/InherentStructure.jl:5-56) for every replica
    of the context, in FP64 with the reference's arithmetic: steepest descent
    v = F*dt, scaled so that max_i |v_i| <= max_step_size, drift with wrap

@@ -12,6 +12,8 @@ from __future__ import annotations
 
 import dataclasses
 import itertools
+import json
+import os
 from typing import Iterable, Optional
 
 import numpy as np
@@ -119,3 +121,47 @@ class _Subset:
 
     def stats(self, rid):
         return self._b.stats(rid)
+
+
+TUNED_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "tuned.json")
+
+
+def group_key(spec) -> str:
+    """the replica group of the per-group skin: '2D' or '3D'"""
+    return "%dD" % spec.dims
+
+
+def load_tuned(workload: str, path: str = TUNED_PATH) -> Optional[dict]:
+    """the stored tuning of a workload ({"tpp", "graph_steps", "skins"}) or
+    None"""
+    try:
+        with open(path) as f:
+            return json.load(f).get(workload)
+    except (OSError, ValueError):
+        return None
+
+
+def skin_for(tuned: Optional[dict], spec) -> float:
+    """the skin a stored tuning gives a replica (its configured skin if none)"""
+    if tuned is None:
+        return spec.skin
+    return float(tuned.get("skins", {}).get(group_key(spec), spec.skin))
+
+
+def apply_tuned(batch: ReplicaBatch, tuned: dict, graphs: bool = True):
+    """set a batch to a stored tuning: per-group skins, threads per particle,
+    steps per captured graph"""
+    for rid, spec in list(batch.specs.items()):
+        sk = skin_for(tuned, spec)
+        if sk != spec.skin:
+            batch.set_skin(sk, rid)
+    batch.set_tuning(int(tuned.get("tpp", 1)), graphs, int(tuned.get("graph_steps", 16)))
+
+
+def as_tuned(result: TuneResult, batch: ReplicaBatch) -> dict:
+    """a TuneResult in the stored form"""
+    skins = {}
+    for spec in batch.specs.values():
+        skins[group_key(spec)] = float(spec.skin)
+    return {"tpp": result.tpp, "graph_steps": result.graph_steps, "skins": skins}
+

@@ -119,6 +119,27 @@ class ReplicaBatch:
         """step, returning the status instead of raising (serving loop)."""
         return int(self.lib.simmd_step(self.ctx, int(nsteps), None))
 
+    def transfer_layout(self):
+        """batched host layout of upload_all / download_all: (total rows,
+        {replica id: first row}) of a (rows, dims_r) stack of every replica's
+        (N, dims) block in replica-id order, as flat float64 offsets"""
+        n = max(self.specs) + 1 if self.specs else 1
+        off = np.full(n, -1, np.int64)
+        total = int(self.lib.simmd_transfer_layout(self.ctx, n, _lib.ptr(off)))
+        return total, {rid: int(off[rid]) for rid in self.specs}
+
+    def upload_all(self, r: np.ndarray, D: np.ndarray, v: Optional[np.ndarray] = None,
+                   F: Optional[np.ndarray] = None):
+        """simmd_upload_all: every replica from flat float64 arrays in the
+        batched layout (r, v, F: the replicas' (N, dims) blocks in id order;
+        D: their N diameters in id order)"""
+        _lib.check(self.lib.simmd_upload_all(self.ctx, _lib.ptr(r), _lib.ptr(v), _lib.ptr(F), _lib.ptr(D), None))
+
+    def download_all(self, r: Optional[np.ndarray] = None, v: Optional[np.ndarray] = None,
+                     F: Optional[np.ndarray] = None):
+        """simmd_download_all into flat float64 arrays in the batched layout"""
+        _lib.check(self.lib.simmd_download_all(self.ctx, _lib.ptr(r), _lib.ptr(v), _lib.ptr(F), None))
+
     def state(self, rid: int):
         s = self.specs[rid]
         r = np.zeros((s.N, s.dims))

@@ -947,6 +947,68 @@ static int run_steps(simmd_ctx* c, long long nsteps, const double* noise)
 }
 
 // ---------------------------------------------------------------------------
+// batched host transfers: every active replica in one call, host layout =
+// the replicas in id order, each its dims x N block (and N-element block)
+// ---------------------------------------------------------------------------
+// offsets of the active replicas in the batched layout; true when some
+// replica's offsets changed (the device descriptors must be refreshed)
+static bool xfer_layout(simmd_ctx* c, long long* nvec, long long* nsc)
+{
+    long long off = 0, soff = 0;
+    bool changed = false;
+    for (int r = 0; r < c->R_cap; r++) {
+        HostRep& h = c->reps[r];
+        if (!h.active) continue;
+        if (h.d.xfer_off != off || h.d.xfer_soff != soff) changed = true;
+        h.d.xfer_off = off;
+        h.d.xfer_soff = soff;
+        off += h.p.N * h.p.dims;
+        soff += h.p.N;
+    }
+    *nvec = off;
+    *nsc = soff;
+    return changed;
+}
+
+// every replica's descriptor in one copy (staged in a host vector the
+// asynchronous copy reads, so kept until the stream synchronises)
+static int push_all_desc(simmd_ctx* c, std::vector<RepDesc>& staging)
+{
+    staging.resize((size_t)c->R_cap);
+    for (int r = 0; r < c->R_cap; r++) staging[(size_t)r] = c->reps[r].d;
+    CK(cudaMemcpyAsync(c->d_desc, staging.data(), sizeof(RepDesc) * (size_t)c->R_cap, cudaMemcpyHostToDevice,
+                       c->stream));
+    return SIMMD_OK;
+}
+
+// a replica's descriptor from its (new) diameters: the Verlet radius and
+// the cell grid follow max(D); slots, tiles and transfer offsets stay
+static int refresh_desc(simmd_ctx* c, int rep, const double* D)
+{
+    HostRep& h = c->reps[rep];
+    RepDesc d;
+    TRY(fill_desc(&h.p, D, d));
+    h.smax = max_diameter(D, h.p.N);
+    if (d.ncell != h.d.ncell) {
+        give_range(c->free_cells, h.d.cell0, h.d.ncell + 1);
+        long long cstart;
+        if (!take_range(c->free_cells, d.ncell + 1, &cstart)) {
+            TRY(ensure_capacity(c, c->S_cap, c->C_cap + d.ncell + 1, c->R_cap, c->K));
+            if (!take_range(c->free_cells, d.ncell + 1, &cstart)) return set_err(SIMMD_ERR_BUDGET, "cells");
+        }
+        d.cell0 = (int)cstart;
+    } else {
+        d.cell0 = h.d.cell0;
+    }
+    d.slot0 = h.d.slot0;
+    d.tile0 = h.d.tile0;
+    d.xfer_off = h.d.xfer_off;
+    d.xfer_soff = h.d.xfer_soff;
+    h.d = d;
+    return SIMMD_OK;
+}
+
+// ---------------------------------------------------------------------------
 // C ABI
 // ---------------------------------------------------------------------------
 extern "C" {
@@ -1096,23 +1158,7 @@ int simmd_upload_r(simmd_ctx* c, int32_t rep, const double* r, const double* v, 
         return SIMMD_OK;
     }
     // the Verlet radius depends on max(D): refresh the descriptor and cells
-    RepDesc d;
-    TRY(fill_desc(&h.p, D, d));
-    h.smax = max_diameter(D, h.p.N);
-    if (d.ncell != h.d.ncell) {
-        give_range(c->free_cells, h.d.cell0, h.d.ncell + 1);
-        long long cstart;
-        if (!take_range(c->free_cells, d.ncell + 1, &cstart)) {
-            TRY(ensure_capacity(c, c->S_cap, c->C_cap + d.ncell + 1, c->R_cap, c->K));
-            if (!take_range(c->free_cells, d.ncell + 1, &cstart)) return set_err(SIMMD_ERR_BUDGET, "cells");
-        }
-        d.cell0 = (int)cstart;
-    } else {
-        d.cell0 = h.d.cell0;
-    }
-    d.slot0 = h.d.slot0;
-    d.tile0 = h.d.tile0;
-    h.d = d;
+    TRY(refresh_desc(c, rep, D));
     TRY(push_desc(c, rep));
     TRY(reset_state(c, rep, true));
     return upload_rep(c, rep, r, v, F, D, disp);
@@ -1227,6 +1273,91 @@ int simmd_set_state(simmd_ctx* c, const double* r, const double* v, const double
 int simmd_download(simmd_ctx* c, double* r, double* v, double* F, double* disp)
 {
     return simmd_download_r(c, 0, r, v, F, disp);
+}
+
+int64_t simmd_transfer_layout(simmd_ctx* c, int32_t n, int64_t* offsets)
+{
+    if (!c) return -1;
+    long long nv = 0, ns = 0;
+    xfer_layout(c, &nv, &ns);
+    if (offsets)
+        for (int r = 0; r < n; r++)
+            offsets[r] = (r < c->R_cap && c->reps[r].active) ? c->reps[r].d.xfer_off : -1;
+    return nv;
+}
+
+int simmd_upload_all(simmd_ctx* c, const double* r, const double* v, const double* F, const double* D,
+                     const double* disp)
+{
+    if (!c || !r || !D) return set_err(SIMMD_ERR_BAD_ARG, "NULL argument");
+    CK(cudaSetDevice(c->device));
+    long long nv = 0, ns = 0;
+    xfer_layout(c, &nv, &ns);
+    if (nv == 0) return set_err(SIMMD_ERR_NOT_FOUND, "no replica");
+    for (int rep = 0; rep < c->R_cap; rep++) {
+        if (!c->reps[rep].active) continue;
+        TRY(refresh_desc(c, rep, D + c->reps[rep].d.xfer_soff));
+        c->reps[rep].pending_rebuild = true;
+    }
+    std::vector<RepDesc> dstage;
+    TRY(push_all_desc(c, dstage));
+    // every replica's state as reset_state(keep_counters) leaves it, in one
+    // round trip
+    CK(cudaMemcpyAsync(c->h_state.data(), c->d_state, sizeof(RepState) * (size_t)c->R_cap, cudaMemcpyDeviceToHost,
+                       c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    for (int rep = 0; rep < c->R_cap; rep++) {
+        if (!c->reps[rep].active) continue;
+        RepState& st = c->h_state[(size_t)rep];
+        const long long step = st.step, rb = st.rebuilds;
+        const int mc = st.maxcount;
+        memset(&st, 0, sizeof(st));
+        st.step = step;
+        st.rebuilds = rb;
+        st.maxcount = mc;
+        st.vscale = 1.0;
+        st.force_rebuild = 1;
+    }
+    CK(cudaMemcpyAsync(c->d_state, c->h_state.data(), sizeof(RepState) * (size_t)c->R_cap, cudaMemcpyHostToDevice,
+                       c->stream));
+    TRY(ensure_stage(c, nv));
+    double* stg = c->d_stage;
+    double *dr = stg, *dv = stg + c->stage_cap, *dF = stg + 2 * c->stage_cap, *dD = stg + 3 * c->stage_cap,
+           *du = stg + 4 * c->stage_cap;
+    CK(cudaMemcpyAsync(dr, r, sizeof(double) * nv, cudaMemcpyHostToDevice, c->stream));
+    if (v) CK(cudaMemcpyAsync(dv, v, sizeof(double) * nv, cudaMemcpyHostToDevice, c->stream));
+    if (F) CK(cudaMemcpyAsync(dF, F, sizeof(double) * nv, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(dD, D, sizeof(double) * ns, cudaMemcpyHostToDevice, c->stream));
+    if (disp) CK(cudaMemcpyAsync(du, disp, sizeof(double) * nv, cudaMemcpyHostToDevice, c->stream));
+    Batch b = make_batch(c);
+    LaunchCfg lc = make_lc(c, FMODE_STEP);
+    launch_load_all(b, lc, dr, v ? dv : nullptr, F ? dF : nullptr, dD, disp ? du : nullptr);
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(c->stream));
+    return SIMMD_OK;
+}
+
+int simmd_download_all(simmd_ctx* c, double* r, double* v, double* F, double* disp)
+{
+    if (!c) return set_err(SIMMD_ERR_BAD_ARG, "NULL context");
+    CK(cudaSetDevice(c->device));
+    long long nv = 0, ns = 0;
+    std::vector<RepDesc> dstage;
+    if (xfer_layout(c, &nv, &ns)) TRY(push_all_desc(c, dstage));
+    if (nv == 0) return set_err(SIMMD_ERR_NOT_FOUND, "no replica");
+    TRY(ensure_stage(c, nv));
+    double* stg = c->d_stage;
+    double *dr = stg, *dv = stg + c->stage_cap, *dF = stg + 2 * c->stage_cap, *du = stg + 4 * c->stage_cap;
+    Batch b = make_batch(c);
+    LaunchCfg lc = make_lc(c, FMODE_STEP);
+    launch_store_all(b, lc, r ? dr : nullptr, v ? dv : nullptr, F ? dF : nullptr, disp ? du : nullptr);
+    CK(cudaGetLastError());
+    if (r) CK(cudaMemcpyAsync(r, dr, sizeof(double) * nv, cudaMemcpyDeviceToHost, c->stream));
+    if (v) CK(cudaMemcpyAsync(v, dv, sizeof(double) * nv, cudaMemcpyDeviceToHost, c->stream));
+    if (F) CK(cudaMemcpyAsync(F, dF, sizeof(double) * nv, cudaMemcpyDeviceToHost, c->stream));
+    if (disp) CK(cudaMemcpyAsync(disp, du, sizeof(double) * nv, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return SIMMD_OK;
 }
 
 int simmd_rebuild(simmd_ctx* c)

@@ -537,6 +537,106 @@ __global__ void k_set_state(Batch b, int rep, const double* r, const double* v, 
     }
 }
 
+// every active replica at once, batched host layout: replica r's dims x N
+// block at xfer_off, its N-element block at xfer_soff (replicas in id
+// order); one thread per slot of the replicas' tiles
+__global__ void k_load_all(Batch b, const double* r, const double* v, const double* F, const double* D,
+                           const double* disp)
+{
+    for (int t = blockIdx.x; t < b.ntiles; t += gridDim.x) {
+        const int rep = b.tile_rep[t];
+        if (rep < 0) continue;
+        const RepDesc& d = b.desc[rep];
+        if (!d.active) continue;
+        const long long s = (long long)t * TILE + threadIdx.x;
+        const long long k = s - d.slot0;
+        Slots& S = b.s;
+        const int dm = d.dims;
+        if (k < d.n) {
+            const double* rr = r + d.xfer_off + k * dm;
+            S.posD[s] = make_double4_32a(rr[0], rr[1], dm == 3 ? rr[2] : 0.0, D[d.xfer_soff + k]);
+            const double* vv = v ? v + d.xfer_off + k * dm : nullptr;
+            const double* ff = F ? F + d.xfer_off + k * dm : nullptr;
+            const double* uu = disp ? disp + d.xfer_off + k * dm : nullptr;
+            S.vx[s] = vv ? vv[0] : 0.0;
+            S.vy[s] = vv ? vv[1] : 0.0;
+            S.vz[s] = (vv && dm == 3) ? vv[2] : 0.0;
+            S.fx[s] = ff ? ff[0] : 0.0;
+            S.fy[s] = ff ? ff[1] : 0.0;
+            S.fz[s] = (ff && dm == 3) ? ff[2] : 0.0;
+            S.ux[s] = uu ? uu[0] : 0.0;
+            S.uy[s] = uu ? uu[1] : 0.0;
+            S.uz[s] = (uu && dm == 3) ? uu[2] : 0.0;
+            S.orig[s] = (int)k;
+        } else {
+            S.posD[s] = make_double4_32a(0.0, 0.0, 0.0, 0.0);
+            S.vx[s] = S.vy[s] = S.vz[s] = 0.0;
+            S.fx[s] = S.fy[s] = S.fz[s] = 0.0;
+            S.ux[s] = S.uy[s] = S.uz[s] = 0.0;
+            S.orig[s] = -1;
+        }
+        S.ncnt[s] = 0;
+        S.cellc[s] = 0;
+        rec_put(&S.rec[s], make_float4(0.f, 0.f, 0.f, 0.f), make_float4(0.f, 0.f, 0.f, 0.f));
+    }
+}
+
+__global__ void k_store_all(Batch b, double* r, double* v, double* F, double* disp)
+{
+    for (int t = blockIdx.x; t < b.ntiles; t += gridDim.x) {
+        const int rep = b.tile_rep[t];
+        if (rep < 0) continue;
+        const RepDesc& d = b.desc[rep];
+        if (!d.active) continue;
+        const long long s = (long long)t * TILE + threadIdx.x;
+        if (s >= d.slot0 + d.n) continue;
+        const Slots& S = b.s;
+        const int dm = d.dims;
+        const long long o = d.xfer_off + (long long)S.orig[s] * dm;
+        if (r) {
+            const double4_32a p = S.posD[s];
+            r[o] = p.x;
+            r[o + 1] = p.y;
+            if (dm == 3) r[o + 2] = p.z;
+        }
+        if (v) {
+            v[o] = S.vx[s];
+            v[o + 1] = S.vy[s];
+            if (dm == 3) v[o + 2] = S.vz[s];
+        }
+        if (F) {
+            const RepState& st = b.state[rep];
+            if (d.dyn == DYN_BROWNIAN && st.fmean_pending) {  // F - <F> of the last Brownian step
+                F[o] = dsub(S.fx[s], st.fmean[0]);
+                F[o + 1] = dsub(S.fy[s], st.fmean[1]);
+                if (dm == 3) F[o + 2] = dsub(S.fz[s], st.fmean[2]);
+            } else {
+                F[o] = S.fx[s];
+                F[o + 1] = S.fy[s];
+                if (dm == 3) F[o + 2] = S.fz[s];
+            }
+        }
+        if (disp) {
+            disp[o] = S.ux[s];
+            disp[o + 1] = S.uy[s];
+            if (dm == 3) disp[o + 2] = S.uz[s];
+        }
+    }
+}
+
+void launch_load_all(const Batch& b, const LaunchCfg& lc, const double* r, const double* v, const double* F,
+                     const double* D, const double* disp)
+{
+    k_load_all<<<lc.grid_stream, TILE, 0, lc.stream>>>(b, r, v, F, D, disp);
+    if (lc.launches) *lc.launches += 1;
+}
+
+void launch_store_all(const Batch& b, const LaunchCfg& lc, double* r, double* v, double* F, double* disp)
+{
+    k_store_all<<<lc.grid_stream, TILE, 0, lc.stream>>>(b, r, v, F, disp);
+    if (lc.launches) *lc.launches += 1;
+}
+
 void launch_set_state_impl(const Batch& b, const LaunchCfg& lc, int rep, const RepDesc& hd, const double* r,
                            const double* v, const double* F, const double* disp)
 {

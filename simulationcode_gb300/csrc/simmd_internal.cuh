@@ -60,6 +60,8 @@ struct RepDesc {
     float Lf, halfLf, csf, rc2f, rcutf, skinf, sigma2f, sigma4f, cut2f, epsf, Ucf, c0f, c2f, c4f, zetaf;
     float noisef, gammaf;      // noise_factor, gamma rounded to FP32
     unsigned long long seed;
+    long long xfer_off;        // batched host transfers: offset of this replica's dims x N block
+    long long xfer_soff;       // ... and of its N-element block (D)
     const double* host_noise;  // [noise_nsteps][n][dims], original order
     long long noise_step0;
     int noise_nsteps;
@@ -414,6 +416,9 @@ void launch_force(const Batch& b, const LaunchCfg& lc, int mode);
 void launch_brownian_update(const Batch& b, const LaunchCfg& lc);
 void launch_finalize(const Batch& b, const LaunchCfg& lc, int has_rescale);
 void launch_kinetic(const Batch& b, const LaunchCfg& lc);
+void launch_load_all(const Batch& b, const LaunchCfg& lc, const double* r, const double* v, const double* F,
+                     const double* D, const double* disp);
+void launch_store_all(const Batch& b, const LaunchCfg& lc, double* r, double* v, double* F, double* disp);
 void launch_export_list(const Batch& b, const LaunchCfg& lc, int rep, const RepDesc& hd,
                         long long* counts, long long* list, long long maxK, int half_only);
 

@@ -7,6 +7,7 @@ import subprocess
 import sys
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+sys.path.insert(0, ROOT)
 
 
 def test_reference_arm_json_line():
@@ -24,6 +25,9 @@ def test_reference_arm_json_line():
     assert d["metric"] == d["unit"] == "particle-steps/s"
     assert d["steps"] == 3 and d["warmup"] == 3 and d["higher_is_better"] is True
     assert d["value"] > 0 and d["config"]["workload"] == "c1"
+    # the GPU arm's stored tuning: the same skins in both arms' config
+    from simulationcode_gb300.autotune import load_tuned
+    assert d["config"]["skins"] == load_tuned("c1")["skins"]
     cb = d["cpu_baseline"]
     assert cb["value"] == d["value"] and cb["kind"] in ("port", "reference") and cb["cores"] >= 1 and cb["sample"]
     e = d["e2e"]

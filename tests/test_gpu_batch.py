@@ -100,3 +100,51 @@ def test_split_precision_nve_drift(simlib):
     # the split-precision path adds no drift beyond the FP64 path's (the
     # reference arithmetic), within the 1e-4 per particle per 1e5 steps budget
     assert abs(out["fp32"]) <= abs(out["fp64"]) + 1e-4, out
+
+
+def test_batched_host_transfers_equal_per_replica_calls(simlib):
+    """simmd_upload_all / simmd_download_all (every replica in one call, the
+    replicas' blocks in id order) give the same device state and the same
+    host arrays as simmd_upload_r / simmd_download_r replica by replica, bit
+    for bit, also after a replica has been removed (the layout closes up)."""
+    specs = _relaxed(_mixed_specs(seed=3))
+    a, b = ReplicaBatch(0), ReplicaBatch(0)
+    ia = [a.add(s) for s in specs]
+    ib = [b.add(s) for s in specs]
+    for batch, ids in ((a, ia), (b, ib)):
+        batch.rebuild()
+        batch.step(5)
+        batch.remove(ids[1])
+    keep = [k for k in range(len(specs)) if k != 1]
+    rng = np.random.default_rng(4)
+    new = {k: (np.mod(specs[k].r + rng.uniform(-0.01, 0.01, specs[k].r.shape), specs[k].box_size),
+               rng.standard_normal(specs[k].r.shape) * 0.3) for k in keep}
+    # per replica on a
+    for k in keep:
+        s = specs[k]
+        _lib.check(a.lib.simmd_upload_r(a.ctx, ia[k], _lib.ptr(new[k][0]), _lib.ptr(new[k][1]), None,
+                                        _lib.ptr(np.ascontiguousarray(s.D)), None))
+    # all at once on b
+    total, offs = b.transfer_layout()
+    assert sorted(offs) == [ib[k] for k in keep]
+    r_all, v_all = np.zeros(total), np.zeros(total)
+    D_all = np.concatenate([specs[k].D for k in keep])
+    for k in keep:
+        o, n = offs[ib[k]], specs[k].N * specs[k].dims
+        r_all[o:o + n] = new[k][0].reshape(-1)
+        v_all[o:o + n] = new[k][1].reshape(-1)
+    assert total == sum(specs[k].N * specs[k].dims for k in keep)
+    b.upload_all(r_all, D_all, v=v_all)
+    for batch in (a, b):
+        batch.step(23)
+    r_o, v_o, F_o = np.zeros(total), np.zeros(total), np.zeros(total)
+    b.download_all(r_o, v_o, F_o)
+    for k in keep:
+        o, n = offs[ib[k]], specs[k].N * specs[k].dims
+        ra, va, Fa = a.state(ia[k])
+        assert np.array_equal(ra.reshape(-1), r_o[o:o + n])
+        assert np.array_equal(va.reshape(-1), v_o[o:o + n])
+        assert np.array_equal(Fa.reshape(-1), F_o[o:o + n])
+        assert a.stats(ia[k]).rebuilds == b.stats(ib[k]).rebuilds
+    a.close()
+    b.close()
