@@ -203,6 +203,27 @@ int simmd_download_all(simmd_ctx* ctx, double* r, double* v, double* F, double* 
    buffer). */
 int simmd_inherent_structure(simmd_ctx* ctx, double tolerance, int64_t max_iterations, double max_step_size,
                              double dt, int64_t* iterations);
+/* Swap Monte Carlo: nsweeps calls of do_MC_step! (src/MC.jl:139-156) with
+   do_translation_step! (:21-47) and do_swap_step! (:67-110) for every
+   replica of the context, each replica's chain serial as in the reference
+   (particles in id order, each move decided on the state the previous ones
+   left), FP64 find_energy over the full Verlet list
+   (src/AuxiliaryFunctions.jl:546-584), Metropolis at the replica's kBT.  A
+   translation displaces by U[-max_displacement, max_displacement) per
+   component; with probability swap_probability the move is a swap with a
+   uniformly drawn partner instead (the reference's draw ceil(rand()/N)
+   always gives particle 1; the uniform partner is its evident intent),
+   tried only when the diameters differ by at most 0.2.  Draws: Philox
+   keyed by the replica's seed, the particle and the sweep.  The lists are
+   rebuilt inside a sweep when a particle's displacement passes skin/2, as
+   the reference does.  Enables the full list (simmd_set_full_list).
+   simmd_mc_stats: counts4 = {translations accepted, tried, swaps accepted,
+   tried} and dE = the sum of the accepted moves' energy changes (what the
+   reference adds to output.potential_energy), since the replica was added;
+   simmd_download_diameters: the replica's diameters in original order. */
+int simmd_mc_sweeps(simmd_ctx* ctx, int64_t nsweeps, double max_displacement, double swap_probability);
+int simmd_mc_stats(simmd_ctx* ctx, int32_t rep, int64_t* counts4, double* dE);
+int simmd_download_diameters(simmd_ctx* ctx, int32_t rep, double* D);
 /* asynchronous dump feed for save_data (src/Dump.jl:60-88): the replica's
    r, v, F (any may be NULL) as of this point of the step sequence are copied
    to the host on a side stream while later steps run (host arrays
@@ -253,6 +274,11 @@ int simmd_energy_virial_noalloc(const simmd_params* p, const double* r, const do
 /* threads per particle in the force pass (1, 2, 4, 8), CUDA-graph capture of
  * the step loop (0/1) and steps per captured graph. */
 int simmd_set_tuning(simmd_ctx* ctx, int32_t threads_per_particle, int32_t use_graphs, int32_t graph_steps);
+/* tile shape of the force pass: particles per work item (one block of
+ * particles x threads_per_particle threads): 128 (a whole tile), 64 or 32,
+ * or 0 = automatic (whole tiles, split only when a batch has fewer tiles
+ * than SMs).  Results are unchanged. */
+int simmd_set_work_item(simmd_ctx* ctx, int32_t particles);
 /* change the neighbour-list skin (the rebuild cadence) of one replica (or
  * every replica: rep = -1); the lists are rebuilt before the next force
  * evaluation.  Results are unchanged up to the order of the force sums. */
@@ -281,8 +307,8 @@ int simmd_profile_get(simmd_ctx* ctx, double* out6);
 /* self-check of the split-precision kernels' float <-> double conversions
  * (bit operations on the integer pipes) against the hardware converter on
  * the current device: n hashed float and double bit patterns (all classes,
- * rounding ties, the float range edges), and of the integer grid index
- * against its FP64 form; *mismatches = patterns whose result bits differ.
+ * rounding ties, the float range edges); *mismatches = patterns whose
+ * result bits differ.
  * No context needed. */
 int simmd_check_conversions(int64_t n, uint64_t seed, int64_t* mismatches);
 

@@ -87,6 +87,9 @@ def lib():
         L.orc_find_inherent_structure.argtypes = [vp, vp, vp, vp, vp, vp, C.c_double, C.c_int64,
                                                   C.c_double, C.c_double, _P_I64]
         L.orc_relax_capped.argtypes = [vp, vp, vp, vp, vp, C.c_int64, C.c_double, C.c_double]
+        L.orc_mc_uniforms.argtypes = [C.c_uint64, C.c_uint64, C.c_int64, vp]
+        L.orc_mc_sweeps.argtypes = [vp, vp, vp, vp, C.c_int64, C.c_double, C.c_double, C.c_uint64, C.c_uint64,
+                                    vp, _P_D]
         _lib = L
     return _lib
 
@@ -208,6 +211,19 @@ class OracleSystem:
         if st:
             raise RuntimeError("oracle neighbor list overflow")
 
+    def mc_sweeps(self, nsweeps, max_disp, swap_prob, seed, sweep0=0):
+        """nsweeps of do_MC_step! (translation and swap moves, Philox-keyed
+        draws); returns (counts [translations accepted, tried, swaps
+        accepted, tried], sum of accepted dE).  Uses the full list."""
+        counts = np.zeros(4, np.int64)
+        de = C.c_double(0.0)
+        st = lib().orc_mc_sweeps(C.byref(self.p), _ptr(self.r), _ptr(self.D), C.byref(self.nl), int(nsweeps),
+                                 float(max_disp), float(swap_prob), int(seed), int(sweep0), _ptr(counts),
+                                 C.byref(de))
+        if st:
+            raise RuntimeError("oracle neighbor list overflow")
+        return counts, de.value
+
     def half_pairs(self):
         """Unordered pair set of the half (force) list as a sorted (P,2) int64 array."""
         return _pairs(self.nn_half, self.list_half)
@@ -234,6 +250,12 @@ def philox4x32_10(ctr, key):
     o = np.zeros(4, np.uint32)
     lib().orc_philox4x32_10(_ptr(c), _ptr(k), _ptr(o))
     return o
+
+
+def mc_uniforms(seed, sweep, i):
+    out = np.zeros(6)
+    lib().orc_mc_uniforms(int(seed), int(sweep), int(i), _ptr(out))
+    return out
 
 
 def philox_normals(seed, step, N, dims):

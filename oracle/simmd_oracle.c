@@ -750,6 +750,108 @@ int orc_random_initial_configuration(const orc_params *p0, double *r, double *D,
     return status;
 }
 
+/* ------------------------------------------------------------------ */
+/* swap Monte Carlo: do_MC_step! (src/MC.jl:139-156) with               */
+/* do_translation_step! (:21-47) and do_swap_step! (:67-110)            */
+/* ------------------------------------------------------------------ */
+
+/* the six uniforms in [0,1) of particle i in MC sweep `sweep`: counter
+ * (i, 2 + k, sweep_lo, sweep_hi) for k = 0, 1, 2, key (seed_lo, seed_hi);
+ * u[0] move choice, u[1] acceptance, u[2..4] the displacement components,
+ * u[5] the swap partner */
+void orc_mc_uniforms(uint64_t seed, uint64_t sweep, int64_t i, double u[6])
+{
+    uint32_t key[2] = {(uint32_t)seed, (uint32_t)(seed >> 32)};
+    for (uint32_t k = 0; k < 3; k++) {
+        uint32_t ctr[4] = {(uint32_t)i, 2u + k, (uint32_t)sweep, (uint32_t)(sweep >> 32)};
+        uint32_t o[4];
+        orc_philox4x32_10(ctr, key, o);
+        u[2 * k] = (double)(((uint64_t)o[0] << 21) | (o[1] >> 11)) * 0x1.0p-53;
+        u[2 * k + 1] = (double)(((uint64_t)o[2] << 21) | (o[3] >> 11)) * 0x1.0p-53;
+    }
+}
+
+/* nsweeps calls of do_MC_step! on the system (r, D, nl with the full list).
+ * Random numbers from orc_mc_uniforms(seed, sweep0 + s, i) instead of the
+ * global generator; the displacement component is u * 2 * max_disp -
+ * max_disp as populate_random_displacement_array! (src/AuxiliaryFunctions.jl:
+ * 610-615); the swap partner is floor(u * N) (0-based), the evident intent of
+ * the reference's ceil(Int64, rand()/N), which always gives particle 1.
+ * counts[4] += {translations accepted, translations tried, swaps accepted,
+ * swaps tried}; *dE_sum += the energy changes of accepted moves in order
+ * (output.potential_energy += dE). */
+int orc_mc_sweeps(const orc_params *p, double *r, double *D, orc_nlist *nl, int64_t nsweeps, double max_disp,
+                  double swap_prob, uint64_t seed, uint64_t sweep0, int64_t counts[4], double *dE_sum)
+{
+    const int d = p->dims;
+    const double L = p->box_size;
+    const double h = p->skin / 2.0;
+    int status = 0;
+    for (int64_t s = 0; s < nsweeps; s++) {
+        for (int64_t i = 0; i < p->N; i++) {
+            double u[6];
+            orc_mc_uniforms(seed, sweep0 + (uint64_t)s, i, u);
+            if (u[0] > swap_prob) {  /* do_translation_step! */
+                double rold[3] = {0, 0, 0}, rnew[3] = {0, 0, 0}, dr[3] = {0, 0, 0};
+                for (int k = 0; k < d; k++) {
+                    rold[k] = r[d * i + k];
+                    dr[k] = u[2 + k] * 2.0 * max_disp - max_disp;
+                }
+                double e_old = orc_find_energy(p, i, rold, D[i], r, D, nl);
+                for (int k = 0; k < d; k++) {
+                    double x = rold[k] + dr[k];
+                    x -= floor(x / L) * L;
+                    rnew[k] = x;
+                }
+                double e_new = orc_find_energy(p, i, rnew, D[i], r, D, nl);
+                double dE = e_new - e_old;
+                double bf = exp(-dE / p->kBT);
+                if (bf > 1.0) bf = 1.0;
+                counts[1]++;
+                if (bf > u[1]) {
+                    counts[0]++;
+                    for (int k = 0; k < d; k++) {
+                        r[d * i + k] = rnew[k];
+                        nl->disp[d * i + k] += dr[k];
+                    }
+                    double s2 = nl->disp[d * i] * nl->disp[d * i] + nl->disp[d * i + 1] * nl->disp[d * i + 1];
+                    if (d == 3) s2 = s2 + nl->disp[d * i + 2] * nl->disp[d * i + 2];
+                    nl->disp2[i] = s2;
+                    *dE_sum += dE;
+                }
+                if (nl->disp2[i] > h * h) {
+                    int rc = orc_update_neighbor_lists(p, r, D, nl);
+                    if (rc && !status) status = rc;
+                }
+            } else {  /* do_swap_step! */
+                int64_t j = (int64_t)(u[5] * (double)p->N);
+                if (j >= p->N) j = p->N - 1;
+                if (j == i) continue;
+                const double Di = D[i], Dj = D[j];
+                if (fabs(Di - Dj) > 0.2) continue;
+                double ei_old = orc_find_energy(p, i, r + d * i, Di, r, D, nl);
+                double ej_old = orc_find_energy(p, j, r + d * j, Dj, r, D, nl);
+                D[i] = Dj;
+                D[j] = Di;
+                double ei_new = orc_find_energy(p, i, r + d * i, D[i], r, D, nl);
+                double ej_new = orc_find_energy(p, j, r + d * j, D[j], r, D, nl);
+                double dE = (ei_new + ej_new) - (ei_old + ej_old);
+                double bf = exp(-dE / p->kBT);
+                if (bf > 1.0) bf = 1.0;
+                counts[3]++;
+                if (bf > u[1]) {
+                    counts[2]++;
+                    *dE_sum += dE;
+                } else {
+                    D[i] = Di;
+                    D[j] = Dj;
+                }
+            }
+        }
+    }
+    return status;
+}
+
 /* Set-up only, no counterpart in the reference: capped steepest descent of
  * random starts, r += step_size*F with |dr_i| <= max_disp per particle, wrap,
  * displacement, rebuild on the skin trigger (the benchmark relaxes its

@@ -13,6 +13,7 @@
  *   src/AuxiliaryFunctions.jl:22-65, 86-110, 186-196, 311-315, 381-584
  *   src/InitialConfiguration.jl:1-11, 43-114; src/MC.jl:21-47, 139-156 (fixtures)
  *   src/InherentStructure.jl:5-56                     steepest-descent minimiser
+ *   src/MC.jl:21-156                                  swap Monte Carlo (translation and swap moves)
  *
  * Parity status: UNPINNED.  The reference is pure Julia, ships no tests, no
  * golden vectors and no fixtures, and Julia is not available where this
@@ -122,6 +123,10 @@ void orc_generate_diameters_berthier(int64_t N, double sigma_ratio, uint64_t see
 int orc_random_initial_configuration(const orc_params *p, double *r, double *D, orc_nlist *nl,
                                      int64_t steps, double max_disp, uint64_t seed,
                                      double *final_energy);
+/* swap Monte Carlo sweeps (do_MC_step!, src/MC.jl:21-156), Philox-keyed draws */
+void orc_mc_uniforms(uint64_t seed, uint64_t sweep, int64_t i, double u[6]);
+int orc_mc_sweeps(const orc_params *p, double *r, double *D, orc_nlist *nl, int64_t nsweeps, double max_disp,
+                  double swap_prob, uint64_t seed, uint64_t sweep0, int64_t counts[4], double *dE_sum);
 int orc_relax_capped(const orc_params *p, double *r, double *F, const double *D, orc_nlist *nl,
                      int64_t steps, double step_size, double max_disp);
 int orc_find_inherent_structure(const orc_params *p, double *r, double *v, double *F,

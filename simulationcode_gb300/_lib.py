@@ -90,6 +90,7 @@ SIGNATURES = {
     "simmd_stats_r": (C.c_int, [_vp, C.c_int32, _P(Stats)]),
     "simmd_replica_bytes": (C.c_int64, [_P(Params), C.c_int32]),
     "simmd_set_tuning": (C.c_int, [_vp, C.c_int32, C.c_int32, C.c_int32]),
+    "simmd_set_work_item": (C.c_int, [_vp, C.c_int32]),
     "simmd_set_skin": (C.c_int, [_vp, C.c_int32, C.c_double]),
     "simmd_sync": (C.c_int, [_vp]),
     "simmd_stream": (_vp, [_vp]),
@@ -105,6 +106,9 @@ SIGNATURES = {
     "simmd_time_force": (C.c_int, [_vp, C.c_int32, _P(C.c_float)]),
     "simmd_set_profile": (C.c_int, [_vp, C.c_int32]),
     "simmd_relax": (C.c_int, [_vp, C.c_int64, C.c_double, C.c_double]),
+    "simmd_mc_sweeps": (C.c_int, [_vp, C.c_int64, C.c_double, C.c_double]),
+    "simmd_mc_stats": (C.c_int, [_vp, C.c_int32, _vp, _P(C.c_double)]),
+    "simmd_download_diameters": (C.c_int, [_vp, C.c_int32, _vp]),
     "simmd_host_register": (C.c_int, [_vp, C.c_int64]),
     "simmd_host_unregister": (C.c_int, [_vp]),
     "simmd_energy_virial_noalloc": (C.c_int, [_P(Params), _vp, _vp, _vp, _vp, C.c_int64, _vp, _vp]),

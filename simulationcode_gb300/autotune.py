@@ -1,7 +1,7 @@
-"""Autotuner for a loaded ReplicaBatch: threads per particle in the force pass
-(tile shape TILE x T), the skin (the rebuild cadence: a larger skin means
-longer lists but fewer rebuilds) and the number of steps per captured CUDA
-graph.
+"""Autotuner for a loaded ReplicaBatch: the force pass's tile shape (particles
+per work item x threads per particle), the skin (the rebuild cadence: a
+larger skin means longer lists but fewer rebuilds, per replica group) and
+the number of steps per captured CUDA graph.
 
 Each candidate is timed on the live batch with CUDA events over a short run
 after a short warm-up; the trial steps are ordinary MD steps of the batch
@@ -29,6 +29,7 @@ class TuneResult:
     ms_per_step: float
     trials: list
     group_skins: dict = dataclasses.field(default_factory=dict)
+    work_item: int = 0
 
 
 def _may_overflow(batch: ReplicaBatch, skin: float, skin_seen: float, margin: float = 1.15) -> bool:
@@ -46,7 +47,7 @@ def _may_overflow(batch: ReplicaBatch, skin: float, skin_seen: float, margin: fl
 
 def autotune(batch: ReplicaBatch, *, tpps: Iterable[int] = (1, 2, 4, 8), skins: Optional[Iterable[float]] = None,
              graph_steps: Iterable[int] = (16,), warmup: int = 32, steps: int = 96, log=None,
-             group_by=None) -> TuneResult:
+             group_by=None, work_items: Iterable[int] = (0, 64, 32)) -> TuneResult:
     """Grid search over (skin, tpp, graph steps); ``skins`` None keeps the
     replicas' configured skin.  A skin whose predicted longest list could
     overflow max_neighbors is skipped (skins are tried in increasing order).
@@ -78,6 +79,24 @@ def autotune(batch: ReplicaBatch, *, tpps: Iterable[int] = (1, 2, 4, 8), skins: 
     tpp, skin, gs, ms = best
     batch.set_skin(skin)
     batch.set_tuning(tpp, True, gs)
+    # tile shape: particles per force-pass work item at the best (skin, tpp);
+    # 0 = whole 128-particle tiles (split only for batches smaller than the GPU)
+    item, item_ms = 0, ms
+    for wi in work_items:
+        if wi == 0 or wi * tpp < 32:
+            continue
+        batch.set_work_item(wi)
+        batch.step(warmup)
+        batch.timer_start()
+        batch.step(steps)
+        t = batch.timer_stop() / steps
+        trials.append({"tpp": tpp, "skin": skin, "graph_steps": gs, "work_item": wi, "ms_per_step": t})
+        if log:
+            log("autotune: work item %d particles -> %.4f ms/step" % (wi, t))
+        if t < item_ms:
+            item, item_ms = wi, t
+    batch.set_work_item(item)
+    ms = item_ms
     group_skins = {}
     if group_by is not None and len(skins) > 1:
         # second pass: the skin of each group of replicas (e.g. 2D and 3D),
@@ -109,7 +128,8 @@ def autotune(batch: ReplicaBatch, *, tpps: Iterable[int] = (1, 2, 4, 8), skins: 
                     batch.set_skin(gbest[0], rid)
                 group_skins[str(key)] = gbest[0]
                 ms = min(ms, gbest[1])
-    return TuneResult(tpp=tpp, skin=skin, graph_steps=gs, ms_per_step=ms, trials=trials, group_skins=group_skins)
+    return TuneResult(tpp=tpp, skin=skin, graph_steps=gs, ms_per_step=ms, trials=trials, group_skins=group_skins,
+                      work_item=item)
 
 
 class _Subset:
@@ -156,6 +176,7 @@ def apply_tuned(batch: ReplicaBatch, tuned: dict, graphs: bool = True):
         if sk != spec.skin:
             batch.set_skin(sk, rid)
     batch.set_tuning(int(tuned.get("tpp", 1)), graphs, int(tuned.get("graph_steps", 16)))
+    batch.set_work_item(int(tuned.get("work_item", 0)))
 
 
 def as_tuned(result: TuneResult, batch: ReplicaBatch) -> dict:
@@ -163,5 +184,5 @@ def as_tuned(result: TuneResult, batch: ReplicaBatch) -> dict:
     skins = {}
     for spec in batch.specs.values():
         skins[group_key(spec)] = float(spec.skin)
-    return {"tpp": result.tpp, "graph_steps": result.graph_steps, "skins": skins}
+    return {"tpp": result.tpp, "graph_steps": result.graph_steps, "skins": skins, "work_item": result.work_item}
 

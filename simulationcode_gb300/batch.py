@@ -140,6 +140,25 @@ class ReplicaBatch:
         """simmd_download_all into flat float64 arrays in the batched layout"""
         _lib.check(self.lib.simmd_download_all(self.ctx, _lib.ptr(r), _lib.ptr(v), _lib.ptr(F), None))
 
+    def mc_sweeps(self, nsweeps: int, max_displacement: float, swap_probability: float):
+        """swap Monte Carlo: nsweeps of do_MC_step! for every replica (serial
+        chain per replica, FP64 find_energy, rebuilds inside sweeps)"""
+        _lib.check(self.lib.simmd_mc_sweeps(self.ctx, int(nsweeps), float(max_displacement),
+                                            float(swap_probability)))
+
+    def mc_stats(self, rid: int):
+        """(counts [translations accepted, tried, swaps accepted, tried],
+        sum of accepted dE)"""
+        counts = np.zeros(4, np.int64)
+        de = C.c_double()
+        _lib.check(self.lib.simmd_mc_stats(self.ctx, rid, _lib.ptr(counts), C.byref(de)))
+        return counts, de.value
+
+    def diameters(self, rid: int) -> np.ndarray:
+        D = np.zeros(self.specs[rid].N)
+        _lib.check(self.lib.simmd_download_diameters(self.ctx, rid, _lib.ptr(D)))
+        return D
+
     def state(self, rid: int):
         s = self.specs[rid]
         r = np.zeros((s.N, s.dims))
@@ -222,6 +241,10 @@ class ReplicaBatch:
 
     def set_tuning(self, tpp: int, graphs: bool = True, graph_steps: int = 16):
         _lib.check(self.lib.simmd_set_tuning(self.ctx, tpp, int(graphs), graph_steps))
+
+    def set_work_item(self, particles: int):
+        """force-pass tile shape: particles per work item (128, 64, 32; 0 = automatic)"""
+        _lib.check(self.lib.simmd_set_work_item(self.ctx, int(particles)))
 
     def close(self):
         if self.ctx:

@@ -47,6 +47,9 @@ void launch_store_aos_impl(const Batch& b, const LaunchCfg& lc, int rep, const R
 void launch_set_state_impl(const Batch& b, const LaunchCfg& lc, int rep, const RepDesc& hd, const double* r,
                            const double* v, const double* F, const double* disp);
 void launch_check_conversions_impl(long long n, unsigned long long seed, unsigned long long* bad, cudaStream_t s);
+void launch_mc_sweeps_impl(const Batch& b, const LaunchCfg& lc, const unsigned* nbr_full, const int* ncnt_full,
+                           double max_disp, double swap_prob);
+void launch_store_diameters_impl(const Batch& b, const LaunchCfg& lc, int rep, const RepDesc& hd, double* D);
 }  // namespace simmd
 
 using namespace simmd;
@@ -99,6 +102,7 @@ struct simmd_ctx {
     int T = 1;
     int use_graphs = 1;
     int graph_steps = 16;
+    int min_parts = 1;  // force pass: at least this many work items per tile (tile shape)
     int keep_full = 0;
     int Kfull = 0;
     int profile = 0;
@@ -221,11 +225,11 @@ static int force_rebuild_all(simmd_ctx* c)
 }
 
 // device bytes of the capacity-sized arrays: per slot the state (posD 32,
-// v/F/u 72), the split record 32, cellc/orig/ncnt 12, rebuild scratch
+// v/F/u 72), the split record 16, cellc/orig/inv/ncnt 16, rebuild scratch
 // (bin/rank/src 12, staged posD/v/F/orig 84), per-particle energy 8 and the
 // list 4K; per tile the partial sums, plan and owner; per cell count, start
 // and plan entry; per replica its descriptor and state
-constexpr long long SLOT_BYTES = 32 + 72 + 32 + 12 + 12 + 84 + 8;
+constexpr long long SLOT_BYTES = 32 + 72 + 16 + 16 + 12 + 84 + 8;
 constexpr long long TILE_BYTES = RED_LEVELS * (RED_REC * 8 + 4) + NPART * 8 * WARP_SLOTS + 4 + 4 + 4;
 constexpr long long CELL_BYTES = 4 + 4 + 8;
 
@@ -285,6 +289,7 @@ static int ensure_capacity(simmd_ctx* c, long long S_need, long long C_need, int
         TRY(grow_keep(c, &s.rec, S_old, S_new));
         TRY(grow_keep(c, &s.cellc, S_old, S_new));
         TRY(grow_keep(c, &s.orig, S_old, S_new));
+        TRY(grow_keep(c, &s.inv, S_old, S_new));
         TRY(grow_keep(c, &s.ncnt, S_old, S_new));
         TRY(grow_fresh(c, &s.bin_cell, S_old, S_new));
         TRY(grow_fresh(c, &s.bin_rank, S_old, S_new));
@@ -398,6 +403,7 @@ static int force_parts(const simmd_ctx* c)
     for (const auto& h : c->reps)
         if (h.active) tiles += h.d.ntiles;
     int parts = 1;
+    while (parts < c->min_parts && (TILE / (2 * parts)) * c->T >= 32) parts *= 2;
     while (parts < MAX_PARTS && tiles * parts < c->sm_count && (TILE / (2 * parts)) * c->T >= 32) parts *= 2;
     return parts;
 }
@@ -556,20 +562,22 @@ static int fill_desc_smax(const simmd_params* p, double smax, RepDesc& d)
     d.two_m_pow2 = (mant == 0.5) ? 1 : 0;
     d.inv_two_m = 1.0 / d.two_m;
     d.dt_over_two_m = d.dt * d.inv_two_m;
-    // split-precision offset grid: the smallest power of two >= max(1/2, L/1022)
-    double hg = 0.5;
-    while (L / hg > 1022.0) hg *= 2.0;
-    d.h = hg;
-    d.inv_h = 1.0 / hg;
-    double Lhi = std::floor(L / hg) * hg;
-    d.hf = (float)hg;
-    d.Lhi_f = (float)Lhi;
-    d.Llo_f = (float)(L - Lhi);
+    // split precision: 32-bit fixed point of the periodic box
+    d.fix_scale = 4294967296.0 / L;
+    {  // 2^32/L as a 64-bit fixed-point integer with its top bit set
+        int e2 = 0;
+        std::frexp(d.fix_scale, &e2);  // fix_scale in [2^(e2-1), 2^e2)
+        d.fix_sh = 64 - e2;
+        d.fix_mul = (unsigned long long)std::ldexp(d.fix_scale, d.fix_sh - 11) << 11;  // 53 significant bits
+    }
+    d.fix_u = (float)(L / 4294967296.0);
+    d.fix_u2 = (float)((L / 4294967296.0) * (L / 4294967296.0));
+    d.zeta_lo = (float)(d.zeta - (double)(float)d.zeta);
     d.rv2f = (float)d.rv2;
-    // build candidates are relative to a grid point within h/2 of the home
-    // cell centre: a home particle and a stencil candidate differ by at most
-    // 2 cs + h per axis, which needs no minimum image below L/2
-    d.build_wrap = (nc >= 3 && 2.0 * d.cs + hg + 1e-3 < 0.5 * L) ? 0 : 1;
+    // build candidates are relative to the home cell centre: a home particle
+    // and a stencil candidate differ by at most 2 cs per axis, which needs
+    // no minimum image below L/2
+    d.build_wrap = (nc >= 3 && 2.0 * d.cs + 1e-3 < 0.5 * L) ? 0 : 1;
     return SIMMD_OK;
 }
 
@@ -1093,7 +1101,7 @@ static void destroy_ctx(simmd_ctx* c)
     cudaStreamSynchronize(c->stream);
     invalidate_graph(c);
     Slots& s = c->s;
-    void* ptrs[] = {s.posD, s.vx, s.vy, s.vz, s.fx, s.fy, s.fz, s.ux, s.uy, s.uz, s.rec, s.cellc, s.orig, s.nbr,
+    void* ptrs[] = {s.posD, s.vx, s.vy, s.vz, s.fx, s.fy, s.fz, s.ux, s.uy, s.uz, s.rec, s.cellc, s.orig, s.inv, s.nbr,
                     s.ncnt, s.bin_cell, s.bin_rank, s.src, s.t_posD, s.t_vx, s.t_vy, s.t_vz, s.t_fx, s.t_fy,
                     s.t_fz, s.t_orig, s.cell_count, s.cell_start, c->nbr_full, c->ncnt_full, c->epp, c->d_desc,
                     c->d_state, c->d_tile_rep, c->d_red_val, c->d_red_cnt, c->d_warp_part, c->d_tile_cnt, c->d_queue, c->d_stage, c->d_dump, c->d_noise,
@@ -1611,6 +1619,19 @@ int simmd_set_tuning(simmd_ctx* c, int32_t tpp, int32_t use_graphs, int32_t grap
     return SIMMD_OK;
 }
 
+int simmd_set_work_item(simmd_ctx* c, int32_t particles)
+{
+    if (!c) return set_err(SIMMD_ERR_BAD_ARG, "NULL context");
+    if (particles != 0 && particles != TILE && particles != TILE / 2 && particles != TILE / 4)
+        return set_err(SIMMD_ERR_BAD_ARG, "work item must be 0 (automatic), 128, 64 or 32 particles");
+    const int mp = particles == 0 ? 1 : TILE / particles;
+    if (mp != c->min_parts) {
+        c->min_parts = mp;
+        invalidate_graph(c);
+    }
+    return SIMMD_OK;
+}
+
 int simmd_sync(simmd_ctx* c)
 {
     if (!c) return set_err(SIMMD_ERR_BAD_ARG, "NULL context");
@@ -1809,6 +1830,86 @@ int simmd_relax(simmd_ctx* c, int64_t nsteps, double step_size, double max_disp)
         st.fmean_pending = 0;
         CK(cudaMemcpyAsync(c->d_state + r, &st, sizeof(RepState), cudaMemcpyHostToDevice, c->stream));
     }
+    CK(cudaStreamSynchronize(c->stream));
+    return SIMMD_OK;
+}
+
+int simmd_mc_sweeps(simmd_ctx* c, int64_t nsweeps, double max_displacement, double swap_probability)
+{
+    if (!c || nsweeps < 0 || !(max_displacement >= 0) || !(swap_probability >= 0))
+        return set_err(SIMMD_ERR_BAD_ARG, "bad argument");
+    CK(cudaSetDevice(c->device));
+    if (nsweeps == 0) return SIMMD_OK;
+    // find_energy runs over the full Verlet list, as in the reference
+    if (!c->keep_full) {
+        TRY(simmd_set_full_list(c, 1));
+        force_rebuild_all(c);
+    }
+    TRY(pending_rebuilds(c));
+    CK(cudaMemcpyAsync(c->h_state.data(), c->d_state, sizeof(RepState) * (size_t)c->R_cap, cudaMemcpyDeviceToHost,
+                       c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    for (int r = 0; r < c->R_cap; r++) {
+        RepState& st = c->h_state[(size_t)r];
+        st.mc_active = c->reps[r].active ? 1 : 0;
+        st.mc_target = st.mc_sweep + nsweeps;
+        st.mc_next = 0;
+    }
+    CK(cudaMemcpyAsync(c->d_state, c->h_state.data(), sizeof(RepState) * (size_t)c->R_cap, cudaMemcpyHostToDevice,
+                       c->stream));
+    Batch b = make_batch(c);
+    LaunchCfg lc = make_lc(c, FMODE_STEP);
+    int status = SIMMD_OK;
+    // the chains run until a replica needs a list rebuild (or finishes); the
+    // rebuild sequence serves those replicas, and the chains continue
+    for (long long round = 0;; round++) {
+        launch_mc_sweeps_impl(b, lc, c->nbr_full, c->ncnt_full, max_displacement, swap_probability);
+        rebuild_launch(c, b, lc);
+        CK(cudaGetLastError());
+        status = read_states(c);
+        bool done = true;
+        for (int r = 0; r < c->R_cap; r++) {
+            const RepState& st = c->h_state[(size_t)r];
+            if (st.mc_active && !st.nonfinite && st.mc_sweep < st.mc_target) done = false;
+        }
+        if (done || status != SIMMD_OK) break;
+    }
+    for (int r = 0; r < c->R_cap; r++) c->h_state[(size_t)r].mc_active = 0;
+    CK(cudaMemcpyAsync(c->d_state, c->h_state.data(), sizeof(RepState) * (size_t)c->R_cap, cudaMemcpyHostToDevice,
+                       c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    // the moves' displacements are not in the MD skin bookkeeping: fresh
+    // lists before the next force evaluation
+    force_rebuild_all(c);
+    return status;
+}
+
+int simmd_mc_stats(simmd_ctx* c, int32_t rep, int64_t* counts4, double* dE)
+{
+    if (!c) return set_err(SIMMD_ERR_BAD_ARG, "NULL context");
+    CK(cudaSetDevice(c->device));
+    if (rep < 0 || rep >= c->R_cap || !c->reps[rep].active) return set_err(SIMMD_ERR_NOT_FOUND, "no such replica");
+    RepState st;
+    CK(cudaMemcpyAsync(&st, c->d_state + rep, sizeof(RepState), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    if (counts4)
+        for (int k = 0; k < 4; k++) counts4[k] = st.mc_counts[k];
+    if (dE) *dE = st.mc_dE;
+    return SIMMD_OK;
+}
+
+int simmd_download_diameters(simmd_ctx* c, int32_t rep, double* D)
+{
+    if (!c || !D) return set_err(SIMMD_ERR_BAD_ARG, "NULL argument");
+    CK(cudaSetDevice(c->device));
+    if (rep < 0 || rep >= c->R_cap || !c->reps[rep].active) return set_err(SIMMD_ERR_NOT_FOUND, "no such replica");
+    HostRep& h = c->reps[rep];
+    TRY(ensure_stage(c, std::max<long long>(h.p.N * h.p.dims, (long long)h.p.N)));
+    Batch b = make_batch(c);
+    LaunchCfg lc = make_lc(c, FMODE_STEP);
+    launch_store_diameters_impl(b, lc, rep, h.d, c->d_stage);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(D, c->d_stage, sizeof(double) * h.p.N, cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
     return SIMMD_OK;
 }

@@ -1,12 +1,11 @@
 // k_diag.cu -- device self-check (not on the simulation path): the
-// bit-level conversions and grid index of the split-precision kernels
-// against the hardware converter and the FP64 forms.
+// bit-level float <-> double conversions of the split-precision kernels
+// against the hardware converter.
 #include "simmd_internal.cuh"
 
 namespace simmd {
 
-// self-check: f2d / d2f_rn against the converter, bit for bit, and the
-// integer grid index against its FP64 form
+// self-check: f2d / d2f_rn against the converter, bit for bit
 __device__ __forceinline__ unsigned long long mix64(unsigned long long x)
 {
     x ^= x >> 30;
@@ -37,20 +36,6 @@ __global__ void k_check_conversions(long long n, unsigned long long seed, unsign
         const double x = __longlong_as_double((long long)(kind == 4 ? h : b));  // kind 4: any pattern
         const float a = d2f_rn(x), c = (float)x;
         if (__float_as_uint(a) != __float_as_uint(c) && !(a != a && c != c)) nbad++;
-        // grid index: the FP64 form floor(x/h + 0.5) clamped to [0, 1023]
-        RepDesc dd = {};
-        const int hk = -(int)((h >> 20) & 7ull);  // h = 2^0 .. 2^-7
-        dd.h = __longlong_as_double((long long)(1023 + hk) << 52);
-        const double inv_h = __longlong_as_double((long long)(1023 - hk) << 52);
-        const int gk = (int)((h >> 24) & 7ull);
-        double xg;
-        if (gk == 0) xg = __longlong_as_double((long long)h);  // any pattern
-        else if (gk == 1) xg = ((double)(long long)((h >> 27) % 2300ull) * 0.5 - 50.0) * dd.h;  // ties
-        else if (gk == 2) xg = __longlong_as_double(0x3fdfffffffffffffll) * dd.h;  // 0.5 - 2^-54
-        else xg = ((double)(long long)(h >> 11) * 0x1.0p-53 * 1100.0 - 30.0) * dd.h;
-        const double q = floor(xg * inv_h + 0.5);
-        const int gref = (q == q) ? (int)fmax(fmin(q, 1023.0), 0.0) : 0;
-        if (grid_index(xg, dd) != gref) nbad++;
     }
     if (nbad) atomicAdd(bad, nbad);
 }

@@ -24,11 +24,11 @@
 // FP64 path: the reference's per-pair operation order with explicit
 // round-to-nearest intrinsics, so each pair force is bit-identical to the
 // reference expression; only the order of the per-particle sum differs.
-// FP32 split path: pair arithmetic in FP32 on FP32 offsets of the FP64
-// positions from a power-of-two grid, with the grid-point difference exact
-// (split_dx_g); one 32-byte record per neighbour gather; per-particle sums,
-// random force (four deviates per Philox call) and the mean-force partial
-// sums in FP32, integration in FP64.
+// FP32 split path: pair arithmetic in FP32 on exact integer differences of
+// the positions in 32-bit box-periodic fixed point (r^2 exact before one
+// rounding; compensated pair diameter); one 16-byte record per neighbour
+// gather; per-particle sums, random force (four deviates per Philox call)
+// and the mean-force partial sums in FP32, integration in FP64.
 #include "simmd_internal.cuh"
 #include "simmd_reduce.cuh"
 
@@ -126,30 +126,60 @@ __device__ __forceinline__ void pairs_f64(const Batch& b, const RepDesc& d, long
 // ---------------------------------------------------------------------------
 // FP32 split-precision pair
 // ---------------------------------------------------------------------------
-template <int DIM, int POT, bool EN>
-__device__ __forceinline__ void pair_f32(const RepDesc& d, const float4& oi, const float4& gi, const float4& oj,
-                                         const float4& gj, float& fx, float& fy, float& fz, float& e, float& w)
+// Positions are 32-bit box-periodic fixed point, so the minimum-image
+// difference of a pair is the exact int32 difference (the wraparound is the
+// periodic image) and r^2 is formed exactly in 64-bit integers and rounded
+// once.  The soft-sphere pair diameter s^2 = ((D_i + D_j)/2 (1 - zeta
+// |D_i - D_j|))^2 and the ratio x = r^2 / s^2 carry their rounding errors
+// along (error-free sum and FMA-based product residuals, first order): the
+// force's sensitivity to x (about 10 near contact, the r^-14 term) would
+// otherwise amplify the ~5 roundings of s^2 into most of the FP32 error.
+struct PairS2 {
+    float q, eq;  // s^2 = q + eq
+};
+
+__device__ __forceinline__ PairS2 pair_s2_comp(float Di, float Dj, const RepDesc& d)
 {
-    const float dx = split_dx_g(oi.x, oj.x, gi.x, gj.x, d);
-    const float dy = split_dx_g(oi.y, oj.y, gi.y, gj.y, d);
-    float dz = 0.0f, r2;
-    if (DIM == 3) {
-        dz = split_dx_g(oi.z, oj.z, gi.z, gj.z, d);
-        r2 = dx * dx + dy * dy + dz * dz;
-    } else {
-        r2 = dx * dx + dy * dy;
-    }
+    const float a = fmaxf(Di, Dj), b = fminf(Di, Dj);
+    const float S = a + b;
+    const float eS = b - (S - a);               // S + eS = Di + Dj exactly (|a| >= |b|)
+    const float dd = a - b;                     // |Di - Dj|, exact for D within a factor 2
+    const float p = d.zetaf * dd;
+    const float ep = fmaf(d.zetaf, dd, -p) + d.zeta_lo * dd;  // zeta |dD| = p + ep
+    const float T = 1.0f - p;
+    const float eT = ((1.0f - T) - p) - ep;     // T + eT = 1 - zeta |dD|
+    float m = S * T;
+    float em = fmaf(S, T, -m) + (S * eT + eS * T);
+    m *= 0.5f;
+    em *= 0.5f;
+    PairS2 r;
+    r.q = m * m;
+    r.eq = fmaf(m, m, -r.q) + 2.0f * m * em;
+    return r;
+}
+
+template <int DIM, int POT, bool EN>
+__device__ __forceinline__ void pair_f32(const RepDesc& d, const FixRec& pi, const FixRec& pj, float& fx, float& fy,
+                                         float& fz, float& e, float& w)
+{
+    const int ix = (int)(pi.x - pj.x), iy = (int)(pi.y - pj.y), iz = DIM == 3 ? (int)(pi.z - pj.z) : 0;
+    unsigned long long r2i = (unsigned long long)((long long)ix * ix) + (unsigned long long)((long long)iy * iy);
+    if (DIM == 3) r2i += (unsigned long long)((long long)iz * iz);
+    const float r2 = __ull2float_rn(r2i) * d.fix_u2;
+    const float dx = (float)ix * d.fix_u, dy = (float)iy * d.fix_u, dz = DIM == 3 ? (float)iz * d.fix_u : 0.0f;
     float Fr = 0.0f, V = 0.0f;
     if (POT == POT_BERTHIER) {
-        const float md = (oi.w + oj.w) * 0.5f * (1.0f - d.zetaf * fabsf(oi.w - oj.w));
-        const float mds = md * md;
-        const float inv = __fdividef(1.0f, mds);
-        const float ix2 = r2 * inv;
-        const float ix4 = ix2 * ix2;
-        const float xi14 = __fdividef(1.0f, ix4 * ix4 * ix4 * ix2);
-        const bool in = r2 <= d.rc2f * mds;
-        Fr = in ? -2.0f * inv * (d.c2f + 2.0f * d.c4f * ix2 - 6.0f * xi14) : 0.0f;
-        if (EN && in) V = xi14 * ix2 + d.c4f * ix4 + d.c2f * ix2 + d.c0f;
+        const PairS2 s2 = pair_s2_comp(pi.d, pj.d, d);
+        const float inv = __fdividef(1.0f, s2.q);
+        float x = r2 * inv;
+        x = fmaf(fmaf(-x, s2.q, r2) - x * s2.eq, inv, x);  // x = r^2 / (q + eq), first order
+        const float xsq = x * x;
+        const float xi14 = __fdividef(1.0f, xsq * xsq * xsq * x);
+        const bool in = r2 <= d.rc2f * s2.q;
+        const float B = fmaf(-6.0f, xi14, fmaf(2.0f * d.c4f, x, d.c2f));
+        const float F0 = -2.0f * inv * B;
+        Fr = in ? fmaf(-F0, s2.eq * inv, F0) : 0.0f;  // -2 B / (q + eq), first order
+        if (EN && in) V = xi14 * x + fmaf(d.c4f, xsq, fmaf(d.c2f, x, d.c0f));
     } else {
         const float inv = __fdividef(1.0f, r2);
         const float xi2 = (DIM == 3 ? d.sigma2f : d.sigma4f) * inv;
@@ -159,12 +189,12 @@ __device__ __forceinline__ void pair_f32(const RepDesc& d, const float4& oi, con
         Fr = in ? d.epsf * (48.0f * xi12 - 24.0f * xi6) * inv : 0.0f;
         if (EN && in) V = 4.0f * d.epsf * (xi12 - xi6) - d.Ucf;
     }
-    fx += Fr * dx;
-    fy += Fr * dy;
-    if (DIM == 3) fz += Fr * dz;
+    fx = fmaf(Fr, dx, fx);
+    fy = fmaf(Fr, dy, fy);
+    if (DIM == 3) fz = fmaf(Fr, dz, fz);
     if (EN) {
         e += V;
-        w += Fr * r2;
+        w = fmaf(Fr, r2, w);
     }
 }
 
@@ -188,27 +218,24 @@ constexpr int PAIR_UNROLL = SIMMD_PAIR_UNROLL;
 
 template <int DIM, int POT, bool EN, int T>
 __device__ __forceinline__ void pairs_f32(const Batch& b, const RepDesc& d, long long i, int sub,
-                                          const float4 oi, const float4 gi, int cnt, float& fx, float& fy,
-                                          float& fz, float& e, float& w, const unsigned* s_rows, int nrows, int pl,
-                                          int ppb)
+                                          const FixRec ri, int cnt, float& fx, float& fy, float& fz, float& e,
+                                          float& w, const unsigned* s_rows, int nrows, int pl, int ppb)
 {
-    const SplitRec* __restrict__ rec = b.s.rec;
+    const FixRec* __restrict__ rec = b.s.rec;
     int n = sub;
     for (; n + (PAIR_UNROLL - 1) * T < cnt; n += PAIR_UNROLL * T) {
         unsigned j[PAIR_UNROLL];
-        float4 o[PAIR_UNROLL], g[PAIR_UNROLL];
+        FixRec o[PAIR_UNROLL];
 #pragma unroll
         for (int u = 0; u < PAIR_UNROLL; u++) j[u] = list_entry<T>(b, s_rows, nrows, i, pl, ppb, n + u * T);
 #pragma unroll
-        for (int u = 0; u < PAIR_UNROLL; u++) rec_get(rec + j[u], o[u], g[u]);
+        for (int u = 0; u < PAIR_UNROLL; u++) o[u] = rec_get(rec + j[u]);
 #pragma unroll
-        for (int u = 0; u < PAIR_UNROLL; u++) pair_f32<DIM, POT, EN>(d, oi, gi, o[u], g[u], fx, fy, fz, e, w);
+        for (int u = 0; u < PAIR_UNROLL; u++) pair_f32<DIM, POT, EN>(d, ri, o[u], fx, fy, fz, e, w);
     }
     for (; n < cnt; n += T) {
         const unsigned j0 = list_entry<T>(b, s_rows, nrows, i, pl, ppb, n);
-        float4 o0, g0;
-        rec_get(rec + j0, o0, g0);
-        pair_f32<DIM, POT, EN>(d, oi, gi, o0, g0, fx, fy, fz, e, w);
+        pair_f32<DIM, POT, EN>(d, ri, rec_get(rec + j0), fx, fy, fz, e, w);
     }
 }
 
@@ -269,11 +296,10 @@ __device__ __forceinline__ void particle_pairs_f32(const Batch& b, const RepDesc
                                                    float& fx, float& fy, float& fz, float& e, float& w,
                                                    const unsigned* s_rows, int nrows, int pl, int ppb)
 {
-    const float4 oi = b.s.rec[i].o;
-    const float4 gi = b.s.rec[i].g;
+    const FixRec ri = rec_get(b.s.rec + i);
     if (d.pot == POT_BERTHIER)
-        pairs_f32<DIM, POT_BERTHIER, EN, T>(b, d, i, sub, oi, gi, cnt, fx, fy, fz, e, w, s_rows, nrows, pl, ppb);
-    else pairs_f32<DIM, POT_LJ, EN, T>(b, d, i, sub, oi, gi, cnt, fx, fy, fz, e, w, s_rows, nrows, pl, ppb);
+        pairs_f32<DIM, POT_BERTHIER, EN, T>(b, d, i, sub, ri, cnt, fx, fy, fz, e, w, s_rows, nrows, pl, ppb);
+    else pairs_f32<DIM, POT_LJ, EN, T>(b, d, i, sub, ri, cnt, fx, fy, fz, e, w, s_rows, nrows, pl, ppb);
 }
 
 // rows of the tile's list staged in shared memory (16-byte loads, all rows

@@ -31,20 +31,6 @@ __device__ __forceinline__ double wrap_coord(double x, const RepDesc& d)
     return dsub(x, dmul(floor(ddiv(x, d.L)), d.L));
 }
 
-// FP32 offset refresh: x - m*h in FP64 (one subtract; m*h exact), rounded to
-// FP32; the periodic unwrap (rare: a particle that crossed the box edge since
-// its rebuild) is decided in FP32 and redone in FP64 only then
-__device__ __forceinline__ float offset_refresh(double x, float g, const RepDesc& d)
-{
-    const double o = dsub(x, f2d(g));  // exact: g = m*h and |x - g| small
-    const float of = d2f_rn(o);
-    if (fabsf(of) < d.halfLf * 0.9f) return of;
-    double q = o;  // crossed the periodic boundary since the rebuild
-    q = (q > d.halfL) ? q - d.L : q;
-    q = (q < -d.halfL) ? q + d.L : q;
-    return (float)q;
-}
-
 // v + dt*F/(2m); one multiply when 2m is a power of two (exact scaling)
 __device__ __forceinline__ double half_kick(double v, double F, const RepDesc& d)
 {
@@ -53,7 +39,7 @@ __device__ __forceinline__ double half_kick(double v, double F, const RepDesc& d
 }
 
 // r += dr with the reference wrap rnew - floor(rnew/L)*L, displacement update,
-// FP32 offset refresh; returns |disp|^2
+// split record refresh; returns |disp|^2
 __device__ __forceinline__ double drift_slot(const Batch& b, const RepDesc& d, long long i, double drx,
                                              double dry, double drz)
 {
@@ -77,11 +63,12 @@ __device__ __forceinline__ double drift_slot(const Batch& b, const RepDesc& d, l
     const double y = wrap_coord(dadd(p.y, dry), d);
     const double z = (d.dims == 3) ? wrap_coord(dadd(p.z, drz), d) : p.z;
     S.posD[i] = make_double4_32a(x, y, z, p.w);
-    if (d.prec == PREC_FP32) {
-        const float4 g = S.rec[i].g;
-        const float w = S.rec[i].o.w;
-        S.rec[i].o = make_float4(offset_refresh(x, g.x, d), offset_refresh(y, g.y, d),
-                                 d.dims == 3 ? offset_refresh(z, g.z, d) : 0.0f, w);
+    if (d.prec == PREC_FP32) {  // the split record's fixed-point position (D kept)
+        FixRec q = S.rec[i];
+        q.x = fix32(x, d);
+        q.y = fix32(y, d);
+        if (d.dims == 3) q.z = fix32(z, d);
+        S.rec[i] = q;
     }
     return u2;
 }
@@ -443,6 +430,7 @@ __global__ void k_load_aos(Batch b, int rep, const double* r, const double* v, c
         S.uy[s] = disp ? disp[k * dm + 1] : 0.0;
         S.uz[s] = (disp && dm == 3) ? disp[k * dm + 2] : 0.0;
         S.orig[s] = (int)k;
+        S.inv[s] = (int)s;
     } else {
         S.posD[s] = make_double4_32a(0.0, 0.0, 0.0, 0.0);
         S.vx[s] = S.vy[s] = S.vz[s] = 0.0;
@@ -452,7 +440,7 @@ __global__ void k_load_aos(Batch b, int rep, const double* r, const double* v, c
     }
     S.ncnt[s] = 0;
     S.cellc[s] = 0;
-    rec_put(&S.rec[s], make_float4(0.f, 0.f, 0.f, 0.f), make_float4(0.f, 0.f, 0.f, 0.f));
+    S.rec[s] = FixRec{0u, 0u, 0u, 0.0f};
 }
 
 __global__ void k_store_aos(Batch b, int rep, double* r, double* v, double* F, double* disp,
@@ -513,11 +501,7 @@ __global__ void k_set_state(Batch b, int rep, const double* r, const double* v, 
         p.y = r[o * dm + 1];
         if (dm == 3) p.z = r[o * dm + 2];
         S.posD[s] = p;
-        if (d.prec == PREC_FP32) {
-            const float4 g = S.rec[s].g;
-            S.rec[s].o = make_float4(offset_refresh(p.x, g.x, d), offset_refresh(p.y, g.y, d),
-                                     dm == 3 ? offset_refresh(p.z, g.z, d) : 0.0f, (float)p.w);
-        }
+        if (d.prec == PREC_FP32) S.rec[s] = fix_rec(p.x, p.y, p.z, p.w, d);
     }
     if (v) {
         S.vx[s] = v[o * dm];
@@ -568,6 +552,7 @@ __global__ void k_load_all(Batch b, const double* r, const double* v, const doub
             S.uy[s] = uu ? uu[1] : 0.0;
             S.uz[s] = (uu && dm == 3) ? uu[2] : 0.0;
             S.orig[s] = (int)k;
+            S.inv[s] = (int)s;
         } else {
             S.posD[s] = make_double4_32a(0.0, 0.0, 0.0, 0.0);
             S.vx[s] = S.vy[s] = S.vz[s] = 0.0;
@@ -577,7 +562,7 @@ __global__ void k_load_all(Batch b, const double* r, const double* v, const doub
         }
         S.ncnt[s] = 0;
         S.cellc[s] = 0;
-        rec_put(&S.rec[s], make_float4(0.f, 0.f, 0.f, 0.f), make_float4(0.f, 0.f, 0.f, 0.f));
+        S.rec[s] = FixRec{0u, 0u, 0u, 0.0f};
     }
 }
 
@@ -634,6 +619,23 @@ void launch_load_all(const Batch& b, const LaunchCfg& lc, const double* r, const
 void launch_store_all(const Batch& b, const LaunchCfg& lc, double* r, double* v, double* F, double* disp)
 {
     k_store_all<<<lc.grid_stream, TILE, 0, lc.stream>>>(b, r, v, F, disp);
+    if (lc.launches) *lc.launches += 1;
+}
+
+// the replica's diameters in original order (swap moves exchange them)
+__global__ void k_store_diameters(Batch b, int rep, double* D)
+{
+    const RepDesc& d = b.desc[rep];
+    const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= d.n) return;
+    const long long s = d.slot0 + k;
+    D[b.s.orig[s]] = b.s.posD[s].w;
+}
+
+void launch_store_diameters_impl(const Batch& b, const LaunchCfg& lc, int rep, const RepDesc& hd, double* D)
+{
+    const int blocks = (hd.n + 127) / 128;
+    if (blocks > 0) k_store_diameters<<<blocks, 128, 0, lc.stream>>>(b, rep, D);
     if (lc.launches) *lc.launches += 1;
 }
 

@@ -221,23 +221,19 @@ __global__ void k_rb_gather(Batch b, int* ncnt_full)
             S.t_fy[nw] = S.fy[s];
             S.t_fz[nw] = S.fz[s];
             S.t_orig[nw] = S.orig[s];
+            S.inv[d.slot0 + S.orig[s]] = (int)nw;
             int lin = S.bin_cell[s];
             int nc = d.nc;
             int cx = lin % nc, cy = (lin / nc) % nc, cz = lin / (nc * nc);
             S.cellc[nw] = pack_cell(cx, cy, cz);
-            const int mx = grid_index(p.x, d), my = grid_index(p.y, d), mz = d.dims == 3 ? grid_index(p.z, d) : 0;
-            const float gx = (float)mx * d.hf, gy = (float)my * d.hf, gz = (float)mz * d.hf;
-            rec_put(&S.rec[nw],
-                    make_float4(grid_offset(p.x, gx, d), grid_offset(p.y, gy, d),
-                                d.dims == 3 ? grid_offset(p.z, gz, d) : 0.0f, d2f_rn(p.w)),
-                    make_float4(gx, gy, gz, 0.0f));
+            S.rec[nw] = fix_rec(p.x, p.y, p.z, p.w, d);
         } else {
             S.t_posD[nw] = make_double4_32a(0.0, 0.0, 0.0, 0.0);
             S.t_vx[nw] = S.t_vy[nw] = S.t_vz[nw] = 0.0;
             S.t_fx[nw] = S.t_fy[nw] = S.t_fz[nw] = 0.0;
             S.t_orig[nw] = -1;
             S.cellc[nw] = 0;
-            rec_put(&S.rec[nw], make_float4(0.f, 0.f, 0.f, 0.f), make_float4(0.f, 0.f, 0.f, 0.f));
+            S.rec[nw] = FixRec{0u, 0u, 0u, 0.0f};
         }
     }
 }
@@ -264,12 +260,12 @@ constexpr int BLD_THREADS = 128;
 constexpr int BLD_CHUNK = 512;
 
 struct BuildSmem {
-    float4 o[BLD_CHUNK];  // position relative to the home cell's grid reference (FP32), D
+    float4 o[BLD_CHUNK];  // position relative to the home cell's reference point (FP32), D
     int slot[BLD_CHUNK];
     int ca[27];
     int cn[27];
     int pre[28];
-    float rf[3];  // the home cell's grid reference point
+    unsigned rf[3];  // the home cell's centre in fixed point
     int nst;
     unsigned long long entries;
     int maxcnt;
@@ -297,13 +293,15 @@ __device__ void build_cell(const Batch& b, const RepDesc& d, RepState& st, int c
         sm.ca[tid] = a;
         sm.cn[tid] = S.cell_start[d.cell0 + lin + 1] - a;
     }
-    // grid reference point near the home cell centre: candidate coordinates
-    // relative to it are small, so a pair difference is one FP32 subtract
-    // (one thread: FP64 runs on a narrow pipe)
+    // reference point at the home cell centre (fixed point, (2c+1) 2^31 / nc):
+    // candidate coordinates relative to it are small, exact integer
+    // differences (minimum image by the int32 wraparound) turned into FP32,
+    // so a pair difference is one FP32 subtract
     if (tid == 32) {
-        sm.rf[0] = (float)grid_index(((double)cx + 0.5) * d.cs, d) * d.hf;
-        sm.rf[1] = (float)grid_index(((double)cy + 0.5) * d.cs, d) * d.hf;
-        sm.rf[2] = (DIM == 3) ? (float)grid_index(((double)cz + 0.5) * d.cs, d) * d.hf : 0.0f;
+        sm.rf[0] = (unsigned)(((2ull * (unsigned long long)cx + 1ull) << 31) / (unsigned long long)nc);
+        sm.rf[1] = (unsigned)(((2ull * (unsigned long long)cy + 1ull) << 31) / (unsigned long long)nc);
+        sm.rf[2] = (DIM == 3) ? (unsigned)(((2ull * (unsigned long long)cz + 1ull) << 31) / (unsigned long long)nc)
+                              : 0u;
     }
     __syncthreads();
     if (tid == 0) {
@@ -316,7 +314,8 @@ __device__ void build_cell(const Batch& b, const RepDesc& d, RepState& st, int c
     }
     __syncthreads();
     const int M = sm.pre[nst];
-    const float rfx = sm.rf[0], rfy = sm.rf[1], rfz = sm.rf[2];
+    const unsigned rfx = sm.rf[0], rfy = sm.rf[1], rfz = sm.rf[2];
+    const float u = d.fix_u;
     // lanes per home particle: as many as keep the block's 128 threads busy
     // (a power of two dividing 32, so a particle's lanes share one warp)
     const int Tb = P <= 4 ? 32 : (P <= 8 ? 16 : (P <= 16 ? 8 : (P <= 32 ? 4 : (P <= 64 ? 2 : 1))));
@@ -334,10 +333,9 @@ __device__ void build_cell(const Batch& b, const RepDesc& d, RepState& st, int c
         float4 oi = make_float4(0.f, 0.f, 0.f, 0.f);
         double4_32a pi = make_double4_32a(0.0, 0.0, 0.0, 0.0);
         if (active) {
-            const float4 o = S.rec[i].o;
-            const float4 g = S.rec[i].g;
-            oi = make_float4(split_dx_g(o.x, 0.0f, g.x, rfx, d), split_dx_g(o.y, 0.0f, g.y, rfy, d),
-                             DIM == 3 ? split_dx_g(o.z, 0.0f, g.z, rfz, d) : 0.0f, o.w);
+            const FixRec q = S.rec[i];
+            oi = make_float4((float)(int)(q.x - rfx) * u, (float)(int)(q.y - rfy) * u,
+                             DIM == 3 ? (float)(int)(q.z - rfz) * u : 0.0f, q.d);
             pi = S.t_posD[i];
         }
         int cnt = 0, cntf = 0;
@@ -349,14 +347,16 @@ __device__ void build_cell(const Batch& b, const RepDesc& d, RepState& st, int c
                 int k = 0;
                 while (k + 1 < nst && sm.pre[k + 1] <= idx) k++;
                 const int j = sm.ca[k] + (idx - sm.pre[k]);
-                const float4 o = S.rec[j].o;
-                const float4 g = S.rec[j].g;
-                sm.o[q] = make_float4(split_dx_g(o.x, 0.0f, g.x, rfx, d), split_dx_g(o.y, 0.0f, g.y, rfy, d),
-                                      DIM == 3 ? split_dx_g(o.z, 0.0f, g.z, rfz, d) : 0.0f, o.w);
+                const FixRec c = S.rec[j];
+                sm.o[q] = make_float4((float)(int)(c.x - rfx) * u, (float)(int)(c.y - rfy) * u,
+                                      DIM == 3 ? (float)(int)(c.z - rfz) * u : 0.0f, c.d);
                 sm.slot[q] = j;
             }
             __syncthreads();
-            for (int q0 = 0; q0 < len; q0 += Tb) {
+            // a warp with no home particle in this pass skips the candidates
+            // (warp-uniform: the ballots below stay within full warps)
+            const int qend = __any_sync(0xffffffffu, active) ? len : 0;
+            for (int q0 = 0; q0 < qend; q0 += Tb) {
                 const int q = q0 + sub;
                 bool pred = false, predf = false;
                 if (active && q < len) {

@@ -5,9 +5,9 @@
 //     multiple of TILE; slots hold particles in cell-sorted order after each
 //     rebuild, padding slots (orig < 0) never appear in a cell or a list;
 //   * per-slot SoA FP64 arrays v, F, displacement; an AoS double4_32a (x,y,z,D)
-//     gathered by neighbours; a 32-byte split-precision record (FP32 offsets
-//     from a power-of-two grid point, D, the grid point); packed rebuild-time
-//     cell coordinates; the original particle id;
+//     gathered by neighbours; a 16-byte split-precision record (the position
+//     as 32-bit box-periodic fixed point per axis, D in FP32); packed
+//     rebuild-time cell coordinates; the original particle id;
 //   * a padded ELL neighbour list, tile-major (see nbr_addr; T = threads per
 //     particle), each entry the slot of j (low 26 bits);
 //   * per-replica descriptors (read-only) and states (flags, counters,
@@ -54,9 +54,15 @@ struct RepDesc {
     double dt_over_two_m;      // dt/(2m) when 2m is a power of two (exact): one multiply per kick
     int two_m_pow2;
     int build_wrap;            // 0: stencil candidates never need the minimum image (2 cs + h < L/2)
-    // split precision: FP32 offsets from a power-of-two grid h (exact integer shifts)
-    double h, inv_h;
-    float hf, Lhi_f, Llo_f, rv2f;
+    // split precision: positions as 32-bit fixed point of the periodic box,
+    // X = round(x * 2^32 / L) mod 2^32, so x_i - x_j (minimum image) is the
+    // int32 difference X_i - X_j times u = L / 2^32
+    double fix_scale;          // 2^32 / L
+    unsigned long long fix_mul;  // round(2^(32 + fix_sh) / L) < 2^64
+    int fix_sh;
+    float fix_u, fix_u2;       // u and u^2 rounded to FP32
+    float zeta_lo;             // zeta - RN32(zeta)
+    float rv2f;
     float Lf, halfLf, csf, rc2f, rcutf, skinf, sigma2f, sigma4f, cut2f, epsf, Ucf, c0f, c2f, c4f, zetaf;
     float noisef, gammaf;      // noise_factor, gamma rounded to FP32
     unsigned long long seed;
@@ -93,13 +99,21 @@ struct RepState {
     long long min_iters;
     int min_done;                 // 1 converged, 2 iteration limit
     int min_active;               // replica takes part in the minimisation
+    // swap Monte Carlo
+    long long mc_sweep;           // sweeps done (counter of the MC random stream)
+    long long mc_target;          // sweep count to reach in this call
+    long long mc_counts[4];       // translations accepted, tried; swaps accepted, tried
+    double mc_dE;                 // sum of the accepted moves' energy changes
+    int mc_next;                  // next particle of the current sweep
+    int mc_active;                // replica takes part in the MC call
 };
 
-// split-precision gather record (one 32-byte sector): FP32 offsets of the
-// FP64 position from its grid point, FP32 diameter, packed grid index
-struct __align__(32) SplitRec {
-    float4 o;   // x, y, z offsets from the grid point, D
-    float4 g;   // grid point m*h per axis (exact in FP32), unused
+// split-precision gather record (16 bytes, one 128-bit load): the FP64
+// position quantised to 32-bit box-periodic fixed point per axis (z = 0 in
+// 2D) and the diameter in FP32
+struct __align__(16) FixRec {
+    unsigned x, y, z;
+    float d;
 };
 
 struct Slots {
@@ -107,9 +121,10 @@ struct Slots {
     double *vx, *vy, *vz;
     double *fx, *fy, *fz;
     double *ux, *uy, *uz;         // displacement since the last rebuild
-    SplitRec* rec;                // split precision: offsets + D + grid index
+    FixRec* rec;                  // split precision: fixed-point position + D
     int* cellc;                   // packed rebuild-time cell coords (10 bits each)
     int* orig;                    // original id, -1 for padding
+    int* inv;                     // slot of original id k of a replica at inv[slot0 + k]
     unsigned* nbr;                // ELL neighbour list
     int* ncnt;                    // neighbours per slot
     // rebuild scratch
@@ -209,95 +224,54 @@ __device__ __forceinline__ bool nonfinite_bits(double x)
     return (__double_as_longlong(x) & 0x7fffffffffffffffll) >= 0x7ff0000000000000ll;
 }
 
-// split precision: grid index of the FP32 offset origin (power-of-two grid
-// h), the FP64 form floor(x/h + 0.5) clamped to [0, 1023] (h a power of two, so
-// x/h is exact), computed on the integer pipes with the same result for every
-// x: with y = x/h in [2^j, 2^(j+1)), y + 0.5 is exact unless it crosses into
-// the next binade, and there no integer is within the rounding's reach --
-// except at j = -2, where y = 0.5 - 2^-54 rounds y + 0.5 up to 1
-__device__ __forceinline__ int grid_index(double x, const RepDesc& d)
+// split precision: the fixed-point coordinate X = round(x * 2^32 / L) mod
+// 2^32 of a position, on the integer pipes only (GB300's FP64 pipe is the
+// scarce unit of the position updates): the 53-bit mantissa of x times 2^32/L
+// held as a 64-bit fixed-point integer (fix_mul = 2^32/L * 2^fix_sh, top bit
+// set), the exact 117-bit product cut at the binary point and rounded half
+// up.  Any finite x with |x * 2^32 / L| < 2^84 (else 0); periodic by
+// construction (x and x + L give the same X).
+__device__ __forceinline__ unsigned fix32(double x, const RepDesc& d)
 {
     const long long b = __double_as_longlong(x);
-    if (b <= 0) return 0;  // +0, negatives, NaNs with the sign bit
-    const int ex = (int)(b >> 52);
-    const long long mant = b & 0xfffffffffffffll;
-    if (ex == 0x7ff) return mant ? 0 : 1023;  // NaN, +inf
-    if (ex == 0) return 0;                    // subnormal: y < 0.5
-    const int hk = (int)((__double_as_longlong(d.h) >> 52) & 0x7ff) - 1023;
-    const int j = ex - 1023 - hk;
-    if (j >= 10) return 1023;
-    if (j <= -3) return 0;
-    if (j == -2) return mant == 0xfffffffffffffll ? 1 : 0;
-    const long long M = mant | (1ll << 52);
-    const int sh = 52 - j;  // 43..53
-    const long long m = (M + (1ll << (sh - 1))) >> sh;
-    return m > 1023 ? 1023 : (int)m;
+    const long long a = b & 0x7fffffffffffffffll;
+    const int ex = (int)(a >> 52) - 1023;
+    // x * 2^32 / L = M * fix_mul * 2^(ex - 52 - fix_sh): the integer part
+    // starts at bit sh of the product
+    const int sh = 52 + d.fix_sh - ex;
+    if (ex < -1022 || ex > 1023 || sh >= 128 || sh < 33) return 0u;  // zero/subnormal, inf/nan, < 2^-11, huge
+    const unsigned long long M = (unsigned long long)(a & 0xfffffffffffffll) | (1ull << 52);
+    const unsigned long long hi = __umul64hi(M, d.fix_mul), lo = M * d.fix_mul;
+    unsigned long long v;
+    if (sh >= 64) {
+        const int s2 = sh - 64;  // 0 .. 63
+        v = s2 ? ((hi >> s2) + ((hi >> (s2 - 1)) & 1ull)) : (hi + (lo >> 63));
+    } else {
+        v = (hi << (64 - sh)) | (lo >> sh);
+        v += (lo >> (sh - 1)) & 1ull;
+    }
+    return (unsigned)((b < 0) ? (0ull - v) : v);
 }
 
-// FP32 offset of coordinate x from its grid point g = m*h (exact in FP32 and
-// FP64), continuous across the periodic wrap: one FP64 subtract; the wrap
-// correction (|x - g| > L/2, a particle just across the box edge) in FP64
-// only when the FP32 offset is not clearly inside
-__device__ __forceinline__ float grid_offset(double x, float g, const RepDesc& d)
+__device__ __forceinline__ FixRec fix_rec(double x, double y, double z, double D, const RepDesc& d)
 {
-    double o = dsub(x, f2d(g));
-    const float of = d2f_rn(o);
-    if (fabsf(of) < d.halfLf * 0.9f) return of;
-    o = (o > d.halfL) ? o - d.L : o;
-    o = (o < -d.halfL) ? o + d.L : o;
-    return (float)o;
+    FixRec r;
+    r.x = fix32(x, d);
+    r.y = fix32(y, d);
+    r.z = d.dims == 3 ? fix32(z, d) : 0u;
+    r.d = d2f_rn(D);
+    return r;
 }
 
-__device__ __forceinline__ int grid_axis(int g, int axis) { return (g >> (10 * axis)) & 1023; }
-
-// minimum-image difference x_i - x_j of two split-precision coordinates:
-// ((o_i - o_j) - s*L_lo) + ((m_i - m_j)*h - s*L_hi) with the integer grid
-// shift and L_hi = floor(L/h)*h exact in FP32, so only the small offset
-// terms and the final sum round
-__device__ __forceinline__ float split_dx(float oi, float oj, int mi, int mj, const RepDesc& d)
+__device__ __forceinline__ FixRec rec_get(const FixRec* __restrict__ r)
 {
-    const float a = oi - oj;
-    const float G0 = (float)(mi - mj) * d.hf;
-    const float dx0 = a + G0;
-    const float s = (dx0 > d.halfLf) ? 1.0f : ((dx0 < -d.halfLf) ? -1.0f : 0.0f);
-    return (a - s * d.Llo_f) + (G0 - s * d.Lhi_f);
-}
-
-// one 256-bit read-only load of a neighbour's record (sm_100 and later):
-// the record is one sector, so a warp's gather costs one request per lane
-// instead of two
-#ifndef SIMMD_REC_V8
-#define SIMMD_REC_V8 1
-#endif
-__device__ __forceinline__ void rec_get(const SplitRec* __restrict__ r, float4& o, float4& g)
-{
-#if SIMMD_REC_V8
-    asm("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
-        : "=f"(o.x), "=f"(o.y), "=f"(o.z), "=f"(o.w), "=f"(g.x), "=f"(g.y), "=f"(g.z), "=f"(g.w)
-        : "l"(r));
-#else
-    o = __ldg(&r->o);
-    g = __ldg(&r->g);
-#endif
-}
-
-__device__ __forceinline__ void rec_put(SplitRec* r, float4 o, float4 g)
-{
-    r->o = o;
-    r->g = g;
-}
-
-// minimum-image x_i - x_j from split records: (o_i - o_j) + (g_i - g_j) with
-// the grid difference exact; across the periodic boundary (rare) the box is
-// removed as L_hi (a grid multiple, exact) plus L_lo
-__device__ __forceinline__ float split_dx_g(float oi, float oj, float gi, float gj, const RepDesc& d)
-{
-    const float a = oi - oj;
-    const float G0 = gi - gj;
-    const float dx0 = a + G0;
-    if (fabsf(dx0) <= d.halfLf) return dx0;
-    const float s = dx0 > 0.0f ? 1.0f : -1.0f;
-    return (a - s * d.Llo_f) + (G0 - s * d.Lhi_f);
+    const uint4 q = __ldg(reinterpret_cast<const uint4*>(r));
+    FixRec o;
+    o.x = q.x;
+    o.y = q.y;
+    o.z = q.z;
+    o.d = __uint_as_float(q.w);
+    return o;
 }
 
 __device__ __forceinline__ bool need_rebuild(const RepState& st, const RepDesc& d)

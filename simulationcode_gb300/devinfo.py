@@ -1,9 +1,8 @@
 """Device self-check of libsimmd (not on the simulation path).
 
 ``check_conversions()`` runs, on the current GPU, the self-check of the
-split-precision kernels' bit-level float <-> double conversions and of the
-integer grid index against the hardware converter and the FP64 form
-(0 mismatches expected).  ``python -m simulationcode_gb300.devinfo`` prints
+split-precision kernels' bit-level float <-> double conversions against the
+hardware converter (0 mismatches expected).  ``python -m simulationcode_gb300.devinfo`` prints
 the count as one JSON line.
 """
 import ctypes as C

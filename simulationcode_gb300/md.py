@@ -38,6 +38,8 @@ Reference map (SimulationCode.jl):
   logdata                        src/AuxiliaryFunctions.jl:637-646
   create_when_to_save_array      src/Dump.jl:18-31
   save_data                      src/Dump.jl:60-88
+  do_MC_step!                    src/MC.jl:139-156 (translation :21-47, swap :67-110)
+  perform_swap_monte_carlo!      src/MC.jl:180-243
 """
 from __future__ import annotations
 
@@ -146,8 +148,10 @@ class NeighborListStruct:
         self._rebuilds_seen = 0
         self.keep_full_list = False
         self.pending = 0           # recorded steps not yet run on the device
-        self.device_calls = 0      # simmd_step calls made (batching evidence)
+        self.pending_mc = None     # recorded MC sweeps: [count, max_displacement, swap_probability]
+        self.device_calls = 0      # simmd_step / simmd_mc_sweeps calls made (batching evidence)
         self._output = None        # OutputStruct of the recorded steps
+        self._mc_seen = (np.zeros(4, np.int64), 0.0)
 
     # -- device context ---------------------------------------------------
     def _ensure(self, arrays: ArrayStruct, parameters: ParameterStruct):
@@ -189,11 +193,40 @@ class NeighborListStruct:
 
     def _begin(self, arrays, parameters, output):
         """before a device operation: create the context, run recorded
-        steps, push the host arrays"""
+        steps or sweeps, push the host arrays"""
         self._ensure(arrays, parameters)
         if self.pending:
             self._run(arrays, output, 0)
+        if self.pending_mc is not None:
+            self._run_mc(arrays, output, 0, *self.pending_mc[1:])
         self.push(arrays)
+
+    def _run_mc(self, arrays, output, extra, max_disp, swap_prob):
+        """run the recorded MC sweeps plus ``extra``, then copy back r, D and
+        the move counters"""
+        n = (self.pending_mc[0] if self.pending_mc is not None else 0) + extra
+        self.pending_mc = None
+        if n == 0:
+            return
+        self.push(arrays)
+        _lib.check(self._lib.simmd_mc_sweeps(self.ctx, int(n), float(max_disp), float(swap_prob)))
+        self.device_calls += 1
+        self.pull(arrays)
+        _lib.check(self._lib.simmd_download_diameters(self.ctx, 0, _lib.ptr(arrays.D_array)))
+        counts = np.zeros(4, np.int64)
+        de = C.c_double()
+        _lib.check(self._lib.simmd_mc_stats(self.ctx, 0, _lib.ptr(counts), C.byref(de)))
+        c0, d0 = self._mc_seen
+        out = output if output is not None else self._output
+        if out is not None:
+            dc = counts - c0
+            out.N_translations_accepted += int(dc[0])
+            out.N_translations_total += int(dc[1])
+            out.N_swaps_accepted += int(dc[2])
+            out.N_swaps_total += int(dc[3])
+            out.potential_energy += de.value - d0
+        self._mc_seen = (counts, de.value)
+        self._count_rebuilds(output)
 
     def _run(self, arrays, output, extra):
         """run the recorded steps plus ``extra`` from the host state of the
@@ -209,10 +242,36 @@ class NeighborListStruct:
         self._count_rebuilds(output)
 
     def flush(self, arrays, parameters, output):
-        """run the recorded steps now (the host arrays become current)"""
+        """run the recorded steps or sweeps now (the host arrays become current)"""
         if self.pending:
             self._ensure(arrays, parameters)
             self._run(arrays, output, 0)
+        if self.pending_mc is not None:
+            self._ensure(arrays, parameters)
+            self._run_mc(arrays, output, 0, *self.pending_mc[1:])
+
+    def do_MC_step_(self, arrays, parameters, output, swap_probability):
+        """do_MC_step! (src/MC.jl:139-156): one sweep of translation and swap
+        moves on the device; with the no-op callback, sweeps are recorded and
+        run together at the next sweep whose state the host sees"""
+        self._ensure(arrays, parameters)
+        if self.pending:
+            self._run(arrays, output, 0)
+        md_ = float(parameters.max_MC_displacement)
+        key = (md_, float(swap_probability))
+        if parameters.callback is None:
+            after = output.steps_done + 1  # steps_done advances after this call
+            self._output = output
+            if not (_dump_step(parameters, after) or logdata(after) or after > parameters.N_steps):
+                if self.pending_mc is not None and tuple(self.pending_mc[1:]) != key:
+                    self._run_mc(arrays, output, 0, *self.pending_mc[1:])
+                if self.pending_mc is None:
+                    self.pending_mc = [0, md_, float(swap_probability)]
+                self.pending_mc[0] += 1
+                return
+        if self.pending_mc is not None and tuple(self.pending_mc[1:]) != key:
+            self._run_mc(arrays, output, 0, *self.pending_mc[1:])
+        self._run_mc(arrays, output, 1, *key)
 
     # -- the reference's hot-path functions, device methods ----------------
     def update_neighbor_lists_(self, arrays, parameters, output):
@@ -390,6 +449,62 @@ def find_inherent_structure(arrays, parameters, neighborlist, tolerance=1e-6, ma
     Returns the iteration count; raises if max_iterations is reached (the
     reference's intent; its own error path raises a MethodError)."""
     return neighborlist.find_inherent_structure(arrays, parameters, tolerance, max_iterations, max_step_size, dt)
+
+
+def do_MC_step_(arrays, parameters, output, neighborlist, swap_probability):
+    """do_MC_step! (src/MC.jl:139-156): one sweep of Metropolis translation
+    and swap moves."""
+    neighborlist.do_MC_step_(arrays, parameters, output, swap_probability)
+
+
+def perform_swap_monte_carlo_(arrays, parameters, output, neighborlist, stepsdone=0, log=print):
+    """perform_swap_monte_carlo! (src/MC.jl:180-243), the reference's loop:
+    sweeps until steps_done passes N_steps, with the callback, save_data and
+    the log line (E_pot kept by adding each accepted move's dE, and
+    E_pot_test recomputed without the running lists).  Returns the logged
+    values (q4/q6/F2s are out of scope)."""
+    say = log if log is not None else (lambda m: None)
+    if getattr(neighborlist, "ctx", 0) is None:  # a device list not yet in use: keep the full list from the start
+        neighborlist.keep_full_list = True
+    update_neighbor_lists_(arrays, parameters, output, neighborlist)
+    output.kinetic_energy = calculate_full_energy(arrays, parameters, neighborlist)
+    output.steps_done = stepsdone
+    output.N_swaps_total = 0
+    output.N_swaps_accepted = 0
+    output.N_translations_total = 0
+    output.N_translations_accepted = 0
+    output.N_neighbor_list_rebuilds = 0
+    arrays.r_old_array[:] = arrays.r_array
+    if stepsdone == 0:
+        save_data(arrays, parameters, output, neighborlist, False)
+    cb = parameters.callback
+    if cb is not None:
+        cb(arrays, parameters, output, neighborlist)
+    output.potential_energy = calculate_full_energy_no_neigh(arrays, parameters, neighborlist)
+    logged = []
+    while output.steps_done <= parameters.N_steps:
+        do_MC_step_(arrays, parameters, output, neighborlist, parameters.swap_probability)
+        if cb is not None:
+            cb(arrays, parameters, output, neighborlist)
+        output.steps_done += 1
+        save_data(arrays, parameters, output, neighborlist, False)
+        if logdata(output.steps_done):
+            flush = getattr(neighborlist, "flush", None)
+            if flush is not None:
+                flush(arrays, parameters, output)
+            energy_no_neigh = calculate_full_energy_no_neigh(arrays, parameters, neighborlist)
+            say("%d/%d, E_pot = %.12f,  E_pot_test = %.12f" % (output.steps_done, parameters.N_steps,
+                                                                output.potential_energy, energy_no_neigh))
+            logged.append({"step": output.steps_done, "E_pot": output.potential_energy,
+                           "E_pot_test": energy_no_neigh})
+    flush = getattr(neighborlist, "flush", None)
+    if flush is not None:
+        flush(arrays, parameters, output)
+    say("Completed the MC procedure.")
+    say("Number of neighbor lists built = %d" % output.N_neighbor_list_rebuilds)
+    say("Swap moves accepted: %d/%d" % (output.N_swaps_accepted, output.N_swaps_total))
+    say("Translation moves accepted: %d/%d" % (output.N_translations_accepted, output.N_translations_total))
+    return logged
 
 
 def find_kinetic_energy(arrays, parameters, output):

@@ -80,3 +80,25 @@ def md_case(N=1000, dims=3, *, dt=0.002, N_steps=1000, N_eq=20, log_factor=1.5, 
     arrays.r_array[:] = lattice_positions(N, dims, L, 0.05, rng)
     arrays.D_array[:] = 1.0
     return arrays, params, OutputStruct(), dumps
+
+
+def mc_case(N=1000, *, N_steps=50, log_factor=2.0, N_starts=1, seed=7, kBT=0.3, swap=0.2, max_disp=0.05,
+            callback=None):
+    """(arrays, parameters, output, dumps) of a 3D polydisperse soft-sphere
+    system set up through the reference's structs for
+    perform_swap_monte_carlo!: random positions relaxed by the oracle's
+    initial-configuration MC, Berthier diameters, a dump schedule"""
+    from simulationcode_gb300 import md
+    from simulationcode_gb300.structs import ArrayStruct, Berthier, DumpInfo, Newtonian, OutputStruct, ParameterStruct
+    p, r, v, D, rc = make_case(O.POT_BERTHIER, 3, O.NEWTONIAN, N, seed=seed, skin=0.6)
+    U = Berthier()
+    dumps = {}
+    di = DumpInfo(True, "unused.h5", md.create_when_to_save_array(log_factor, N_starts, N_steps),
+                  save_r=True, save_v=False, save_F=False, save_D=True,
+                  writer=lambda step, d: dumps.__setitem__(step, d))
+    params = ParameterStruct(0, seed, 1.02, N, p.box_size, N_steps, swap, max_disp, U.rc ** 2, 0.0,
+                             Newtonian(kBT, 0.005, 1.0, False, 3), U, dump_info=di, callback=callback)
+    arrays = ArrayStruct(N, 3)
+    arrays.r_array[:] = r
+    arrays.D_array[:] = D
+    return arrays, params, OutputStruct(), dumps

@@ -42,6 +42,7 @@ class OracleNeighborList:
         self.seed = int(seed)
         self.sys = None
         self.noise_step = 0
+        self.mc_sweep = 0
         self._rebuilds_seen = 0
 
     def _ensure(self, arrays, parameters):
@@ -55,11 +56,13 @@ class OracleNeighborList:
         self.sys.r[:] = arrays.r_array
         self.sys.v[:] = arrays.v_array
         self.sys.F[:] = arrays.F_array
+        self.sys.D[:] = arrays.D_array
 
     def _out(self, arrays, output):
         arrays.r_array[:] = self.sys.r
         arrays.v_array[:] = self.sys.v
         arrays.F_array[:] = self.sys.F
+        arrays.D_array[:] = self.sys.D
         if output is not None:
             output.N_neighbor_list_rebuilds += self.sys.rebuilds - self._rebuilds_seen
         self._rebuilds_seen = self.sys.rebuilds
@@ -77,6 +80,18 @@ class OracleNeighborList:
             self.sys.run(nsteps, seed=self.seed, step0=self.noise_step)
             if not isinstance(system, Newtonian):
                 self.noise_step += nsteps
+        self._out(arrays, output)
+
+    def do_MC_step_(self, arrays, parameters, output, swap_probability):
+        self._in(arrays, parameters)
+        counts, de = self.sys.mc_sweeps(1, parameters.max_MC_displacement, swap_probability, self.seed,
+                                        sweep0=self.mc_sweep)
+        self.mc_sweep += 1
+        output.N_translations_accepted += int(counts[0])
+        output.N_translations_total += int(counts[1])
+        output.N_swaps_accepted += int(counts[2])
+        output.N_swaps_total += int(counts[3])
+        output.potential_energy += de
         self._out(arrays, output)
 
     def run_short_MD_equilibration_(self, arrays, parameters, output):

@@ -1,6 +1,7 @@
 """Autotuner selection logic against a fake batch (no device): it picks the
-fastest (tpp, skin), skips skins whose predicted lists overflow
-max_neighbors, and tunes each replica group's skin in a second pass."""
+fastest (tpp, skin) and tile shape (particles per work item), skips skins
+whose predicted lists overflow max_neighbors, and tunes each replica group's
+skin in a second pass."""
 import numpy as np
 
 from simulationcode_gb300.autotune import autotune
@@ -24,6 +25,8 @@ class FakeBatch:
         self.base_count = max_count
         self.t = 0.0
         self.calls = []
+        self.item = 0
+        self.best_item = 0
 
     def set_skin(self, skin, rid=-1):
         for r in self.specs:
@@ -34,11 +37,14 @@ class FakeBatch:
     def set_tuning(self, tpp, graphs=True, graph_steps=16):
         self.tpp = tpp
 
+    def set_work_item(self, particles):
+        self.item = particles
+
     def _ms(self):
         ms = 0.0
         for r, s in self.specs.items():
             ms += 1.0 + 5.0 * (self.skin[r] - self.best[s.dims]) ** 2
-        return ms * (1.0 + 0.1 * abs(np.log2(self.tpp) - 1))   # tpp 2 best
+        return ms * (1.0 + 0.1 * abs(np.log2(self.tpp) - 1)) * (1.0 if self.item == self.best_item else 1.05)
 
     def step(self, n):
         self.t += n * self._ms()
@@ -69,6 +75,15 @@ def test_picks_fastest_and_tunes_groups():
     assert res.skin == 0.6                       # best common skin for the mix
     assert res.group_skins == {"2D": 0.7, "3D": 0.5}
     assert [b.skin[r] for r in range(4)] == [0.7, 0.5, 0.7, 0.5]
+    assert res.work_item == 0 and b.item == 0    # whole tiles are the fastest here
+
+
+def test_picks_tile_shape():
+    b = FakeBatch([spec(2), spec(3)], best2d=0.5, best3d=0.5)
+    b.best_item = 64
+    res = autotune(b, tpps=(1, 2), skins=[0.5], warmup=1, steps=2)
+    assert res.work_item == 64 and b.item == 64
+    assert any(t.get("work_item") == 32 for t in res.trials)
 
 
 def test_overflowing_skins_are_skipped():
