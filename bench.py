@@ -175,16 +175,16 @@ def peaks():
 
 
 def force_bytes_per_launch(specs, stats):
-    """Algorithmic HBM bytes of one force-kernel launch: per particle its own
-    position record (FP64 x,y,z,D = 32 B, or the split record = FP32 offsets,
-    D and FP32 grid point = 32 B), the
-    list count, original id and 4 B per list entry, the force write (8 B per
-    component) and, when the second half-kick is fused (Newtonian/Langevin),
-    the velocity read and write (16 B per component).  Neighbour positions
-    are gathered from L2 (cell-sorted layout) and not counted."""
+    """Algorithmic HBM bytes of one force-kernel launch, independent of the
+    kernel's own representation: per particle its position (8 B per
+    component) and diameter (8 B), its list count (4 B) and 4 B per list
+    entry, the force write (8 B per component) and, when the second
+    half-kick is fused (Newtonian/Langevin), the velocity read and write
+    (16 B per component).  Neighbour positions are gathered from L2
+    (cell-sorted layout) and not counted."""
     total = 0
     for s, st in zip(specs, stats):
-        per = 32 + 4 + 4 + 8 * s.dims
+        per = 8 * s.dims + 8 + 4 + 8 * s.dims
         if s.dynamics != 2:
             per += 16 * s.dims
         total += s.N * per + 4 * int(st.list_entries)

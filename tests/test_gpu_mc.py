@@ -51,9 +51,10 @@ def test_mc_replica_alone_equals_in_a_batch(simlib):
     from simulationcode_gb300 import _lib, workloads as W
     from simulationcode_gb300.batch import ReplicaBatch
     rng = np.random.default_rng(2)
-    specs = [W.berthier_spec(900, 2, _lib.BROWNIAN, rng, seed=31, skin=0.6),
-             W.berthier_spec(1300, 3, _lib.NEWTONIAN, rng, seed=32, skin=0.6),
-             W.lj_spec(1000, 3, _lib.LANGEVIN, rng, seed=33, skin=0.6)]
+    # the full Verlet list at skin 0.6 holds up to ~130 entries a particle
+    specs = [W.berthier_spec(900, 2, _lib.BROWNIAN, rng, seed=31, skin=0.6, max_neighbors=200),
+             W.berthier_spec(1300, 3, _lib.NEWTONIAN, rng, seed=32, skin=0.6, max_neighbors=200),
+             W.lj_spec(1000, 3, _lib.LANGEVIN, rng, seed=33, skin=0.6, max_neighbors=200)]
     W.relax_on_device(specs, 0)
     mix = ReplicaBatch(0)
     ids = [mix.add(copy.copy(s)) for s in specs]
@@ -82,11 +83,11 @@ def test_mc_driver_device_vs_oracle(simlib, oracle):
     from oracle_nl import OracleNeighborList
     from simulationcode_gb300 import md
     a_o, params, out_o, dumps_o = mc_case(N=1000, N_steps=60)
-    a_g, _, out_g, dumps_g = mc_case(N=1000, N_steps=60)
+    a_g, params_g, out_g, dumps_g = mc_case(N=1000, N_steps=60)  # its own dump writer
     log_o = md.perform_swap_monte_carlo_(a_o, params, out_o, OracleNeighborList(0.6, 1.25, seed=params.random_seed),
                                          log=None)
     nl = md.initialize_neighbor_struct(0.6, params.box_size, 1.25, params.N, a_g.D_array, 3)
-    log_g = md.perform_swap_monte_carlo_(a_g, params, out_g, nl, log=None)
+    log_g = md.perform_swap_monte_carlo_(a_g, params_g, out_g, nl, log=None)
     for f in ("N_translations_accepted", "N_translations_total", "N_swaps_accepted", "N_swaps_total",
               "steps_done", "N_neighbor_list_rebuilds"):
         assert getattr(out_g, f) == getattr(out_o, f), f
