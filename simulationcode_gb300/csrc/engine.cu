@@ -28,6 +28,7 @@
 namespace simmd {
 void launch_rebuild_plan_impl(const Batch& b, const LaunchCfg& lc, cudaGraphConditionalHandle cond, int use_cond);
 void launch_rebuild_body_impl(const Batch& b, const LaunchCfg& lc, unsigned* nbr_full, int* ncnt_full, int Kfull);
+void launch_mark_rebuild_impl(const int* reps, int n, RepState* state, cudaStream_t s);
 void launch_export_impl(const Batch& b, const LaunchCfg& lc, int rep, const RepDesc& hd, const unsigned* lst,
                         const int* cnt, int T, long long* counts, long long* list, long long maxK, int half_only,
                         int* overflow);
@@ -124,6 +125,7 @@ struct simmd_ctx {
     int* d_plan_tiles = nullptr;
     int2* d_plan_cells = nullptr;
     int* d_plan_cnt = nullptr;
+    int* d_mark = nullptr;  // replica ids whose rebuild the host requests
     std::vector<int> h_tile_rep;
     std::vector<RepState> h_state;
     double* d_stage = nullptr;  // AoS staging, 5 arrays of stage_cap doubles
@@ -232,11 +234,12 @@ static int force_rebuild_all(simmd_ctx* c)
 constexpr long long SLOT_BYTES = 32 + 72 + 16 + 16 + 12 + 84 + 8;
 constexpr long long TILE_BYTES = RED_LEVELS * (RED_REC * 8 + 4) + NPART * 8 * WARP_SLOTS + 4 + 4 + 4;
 constexpr long long CELL_BYTES = 4 + 4 + 8;
+constexpr long long REP_BYTES = sizeof(RepDesc) + sizeof(RepState) + 4;
 
 static long long capacity_bytes(const simmd_ctx* c, long long S, long long C, int R, int K)
 {
     long long b = S * (SLOT_BYTES + 4LL * K) + (S / TILE) * TILE_BYTES + C * CELL_BYTES +
-                  (long long)R * (long long)(sizeof(RepDesc) + sizeof(RepState));
+                  (long long)R * REP_BYTES;
     if (c->keep_full) b += S * (4LL * std::max(K, c->Kfull) + 4);
     return b;
 }
@@ -349,6 +352,7 @@ static int ensure_capacity(simmd_ctx* c, long long S_need, long long C_need, int
     if (grow_r) {
         TRY(grow_keep(c, &c->d_desc, R_old, R_new));
         TRY(grow_keep(c, &c->d_state, R_old, R_new));
+        TRY(grow_fresh(c, &c->d_mark, R_old, R_new));
         c->reps.resize(R_new);
         c->h_state.resize(R_new);
         c->R_cap = R_new;
@@ -825,19 +829,22 @@ static void enqueue_step(simmd_ctx* c, const Batch& b, const LaunchCfg& lc, cons
     }
 }
 
+// the host's rebuild requests (a new or re-uploaded replica, a skin change,
+// simmd_rebuild): one copy of the replica ids and one marking kernel, then
+// the rebuild sequence, which works only on the marked replicas
 static int pending_rebuilds(simmd_ctx* c)
 {
-    bool any = false;
+    std::vector<int> ids;
     for (int r = 0; r < c->R_cap; r++) {
         HostRep& h = c->reps[r];
         if (h.active && h.pending_rebuild) {
-            int one = 1;
-            CK(cudaMemcpyAsync(&c->d_state[r].force_rebuild, &one, sizeof(int), cudaMemcpyHostToDevice, c->stream));
+            ids.push_back(r);
             h.pending_rebuild = false;
-            any = true;
         }
     }
-    if (any) {
+    if (!ids.empty()) {
+        CK(cudaMemcpyAsync(c->d_mark, ids.data(), sizeof(int) * ids.size(), cudaMemcpyHostToDevice, c->stream));
+        launch_mark_rebuild_impl(c->d_mark, (int)ids.size(), c->d_state, c->stream);
         Batch b = make_batch(c);
         LaunchCfg lc = make_lc(c, FMODE_STEP);
         rebuild_launch(c, b, lc);
@@ -1105,7 +1112,7 @@ static void destroy_ctx(simmd_ctx* c)
                     s.ncnt, s.bin_cell, s.bin_rank, s.src, s.t_posD, s.t_vx, s.t_vy, s.t_vz, s.t_fx, s.t_fy,
                     s.t_fz, s.t_orig, s.cell_count, s.cell_start, c->nbr_full, c->ncnt_full, c->epp, c->d_desc,
                     c->d_state, c->d_tile_rep, c->d_red_val, c->d_red_cnt, c->d_warp_part, c->d_tile_cnt, c->d_queue, c->d_stage, c->d_dump, c->d_noise,
-                    c->d_plan_tiles, c->d_plan_cells, c->d_plan_cnt};
+                    c->d_plan_tiles, c->d_plan_cells, c->d_plan_cnt, c->d_mark};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (c->dump_stream) cudaStreamSynchronize(c->dump_stream);

@@ -511,6 +511,18 @@ __global__ void k_rb_done(Batch b)
     st.rebuilds += 1;
 }
 
+// the host's rebuild requests: one thread per requested replica
+__global__ void k_mark_rebuild(const int* reps, int n, RepState* state)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < n) state[reps[k]].force_rebuild = 1;
+}
+
+void launch_mark_rebuild_impl(const int* reps, int n, RepState* state, cudaStream_t s)
+{
+    k_mark_rebuild<<<(n + 127) / 128, 128, 0, s>>>(reps, n, state);
+}
+
 void launch_rebuild_plan_impl(const Batch& b, const LaunchCfg& lc, cudaGraphConditionalHandle cond, int use_cond)
 {
     k_rb_plan<<<b.nreps, 128, 0, lc.stream>>>(b, cond, use_cond);
