@@ -283,6 +283,23 @@ int simmd_set_work_item(simmd_ctx* ctx, int32_t particles);
  * every replica: rep = -1); the lists are rebuilt before the next force
  * evaluation.  Results are unchanged up to the order of the force sums. */
 int simmd_set_skin(simmd_ctx* ctx, int32_t rep, double skin);
+/* inner (pruned) neighbour lists for the force pass: after every rebuild,
+ * and whenever a particle of the replica has moved more than inner_skin / 2
+ * since the last prune, the replica's list is filtered to the pairs within
+ * rc_ij + inner_skin (outer-list order kept); the force pass reads the
+ * filtered list.  The dropped pairs lie beyond the force cutoff until the
+ * next prune and add exactly zero, so with one thread per particle every
+ * force, energy and trajectory is bit-identical to the unfiltered list's
+ * (with more threads per particle the pairs regroup among the threads: the
+ * sums agree to rounding); the rebuild schedule (skin trigger) is
+ * unchanged.
+ * inner_skin > 0 for one replica (or every replica: rep = -1) turns the
+ * filtering on for the context (replicas without an inner skin keep every
+ * listed pair); 0 on every replica turns it off.  Costs 4K + 20 device
+ * bytes per slot (K list rows). */
+int simmd_set_prune(simmd_ctx* ctx, int32_t rep, double inner_skin);
+/* prunes done and inner-list entries at the last prune of one replica */
+int simmd_prune_stats(simmd_ctx* ctx, int32_t rep, int64_t* prunes, int64_t* inner_entries);
 int simmd_sync(simmd_ctx* ctx);
 void* simmd_stream(simmd_ctx* ctx);          /* the context's cudaStream_t */
 int simmd_timer_start(simmd_ctx* ctx);       /* CUDA event on the context stream */
@@ -304,6 +321,8 @@ int simmd_set_profile(simmd_ctx* ctx, int32_t enable);
 int simmd_host_register(void* ptr, int64_t bytes);
 int simmd_host_unregister(void* ptr);
 int simmd_profile_get(simmd_ctx* ctx, double* out6);
+/* the profile's time in list pruning (ms total; simmd_set_prune) */
+int simmd_profile_prune_ms(simmd_ctx* ctx, double* ms);
 /* self-check of the split-precision kernels' float <-> double conversions
  * (bit operations on the integer pipes) against the hardware converter on
  * the current device: n hashed float and double bit patterns (all classes,

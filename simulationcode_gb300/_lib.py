@@ -92,6 +92,8 @@ SIGNATURES = {
     "simmd_set_tuning": (C.c_int, [_vp, C.c_int32, C.c_int32, C.c_int32]),
     "simmd_set_work_item": (C.c_int, [_vp, C.c_int32]),
     "simmd_set_skin": (C.c_int, [_vp, C.c_int32, C.c_double]),
+    "simmd_set_prune": (C.c_int, [_vp, C.c_int32, C.c_double]),
+    "simmd_prune_stats": (C.c_int, [_vp, C.c_int32, _vp, _vp]),
     "simmd_sync": (C.c_int, [_vp]),
     "simmd_stream": (_vp, [_vp]),
     "simmd_timer_start": (C.c_int, [_vp]),
@@ -113,6 +115,7 @@ SIGNATURES = {
     "simmd_host_unregister": (C.c_int, [_vp]),
     "simmd_energy_virial_noalloc": (C.c_int, [_P(Params), _vp, _vp, _vp, _vp, C.c_int64, _vp, _vp]),
     "simmd_profile_get": (C.c_int, [_vp, _vp]),
+    "simmd_profile_prune_ms": (C.c_int, [_vp, _vp]),
     "simmd_check_conversions": (C.c_int, [C.c_int64, C.c_uint64, _P(C.c_int64)]),
 }
 

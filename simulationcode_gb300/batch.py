@@ -230,8 +230,24 @@ class ReplicaBatch:
     def profile_get(self):
         out = np.zeros(6)
         _lib.check(self.lib.simmd_profile_get(self.ctx, _lib.ptr(out)))
+        pr = C.c_double(0.0)
+        _lib.check(self.lib.simmd_profile_prune_ms(self.ctx, C.byref(pr)))
         return dict(force_ms=out[0], force_n=int(out[1]), kick_ms=out[2], rebuild_ms=out[3], update_ms=out[4],
-                    steps=int(out[5]))
+                    steps=int(out[5]), prune_ms=pr.value)
+
+    def set_prune(self, inner_skin: float, rid: int = -1):
+        """inner (pruned) lists for the force pass with this inner skin for
+        one replica (rid) or all (-1); 0 everywhere turns them off"""
+        _lib.check(self.lib.simmd_set_prune(self.ctx, rid, float(inner_skin)))
+        for k, s in self.specs.items():
+            if rid in (-1, k):
+                s.inner_skin = float(inner_skin)
+
+    def prune_stats(self, rid: int):
+        """(prunes done, inner-list entries at the last prune)"""
+        n, e = C.c_int64(0), C.c_int64(0)
+        _lib.check(self.lib.simmd_prune_stats(self.ctx, rid, C.byref(n), C.byref(e)))
+        return n.value, e.value
 
     def set_skin(self, skin: float, rid: int = -1):
         _lib.check(self.lib.simmd_set_skin(self.ctx, rid, skin))

@@ -29,6 +29,7 @@ namespace simmd {
 void launch_rebuild_plan_impl(const Batch& b, const LaunchCfg& lc, cudaGraphConditionalHandle cond, int use_cond);
 void launch_rebuild_body_impl(const Batch& b, const LaunchCfg& lc, unsigned* nbr_full, int* ncnt_full, int Kfull);
 void launch_mark_rebuild_impl(const int* reps, int n, RepState* state, cudaStream_t s);
+void launch_prune_impl(const Batch& b, const LaunchCfg& lc);
 void launch_export_impl(const Batch& b, const LaunchCfg& lc, int rep, const RepDesc& hd, const unsigned* lst,
                         const int* cnt, int T, long long* counts, long long* list, long long maxK, int half_only,
                         int* overflow);
@@ -83,10 +84,12 @@ struct HostRep {
     long long steps_done = 0;
     long long noise_draws = 0;
     bool pending_rebuild = false;
+    bool pending_prune = false;  // positions set without a rebuild: re-prune before the next force pass
+    double inner_skin = 0.0;     // inner-list skin (0: the outer skin, nothing pruned by distance)
 };
 
 struct ProfileAcc {
-    double force_ms = 0, kick_ms = 0, rebuild_ms = 0, update_ms = 0;
+    double force_ms = 0, kick_ms = 0, rebuild_ms = 0, update_ms = 0, prune_ms = 0;
     long long force_n = 0, steps = 0;
 };
 
@@ -94,7 +97,7 @@ struct simmd_ctx {
     int device = 0;
     cudaStream_t stream = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-    cudaEvent_t pev[8] = {};
+    cudaEvent_t pev[12] = {};
     int sm_count = 1;
     long long S_cap = 0;
     long long C_cap = 0;
@@ -126,6 +129,8 @@ struct simmd_ctx {
     int2* d_plan_cells = nullptr;
     int* d_plan_cnt = nullptr;
     int* d_mark = nullptr;  // replica ids whose rebuild the host requests
+    bool xfer_dirty = false;  // host descriptors hold transfer offsets the device copies lack
+    int prune_on = 0;         // the force pass reads inner (pruned) lists
     std::vector<int> h_tile_rep;
     std::vector<RepState> h_state;
     double* d_stage = nullptr;  // AoS staging, 5 arrays of stage_cap doubles
@@ -241,6 +246,7 @@ static long long capacity_bytes(const simmd_ctx* c, long long S, long long C, in
     long long b = S * (SLOT_BYTES + 4LL * K) + (S / TILE) * TILE_BYTES + C * CELL_BYTES +
                   (long long)R * REP_BYTES;
     if (c->keep_full) b += S * (4LL * std::max(K, c->Kfull) + 4);
+    if (c->prune_on) b += S * (4LL * K + 4 + 16);
     return b;
 }
 
@@ -325,10 +331,23 @@ static int ensure_capacity(simmd_ctx* c, long long S_need, long long C_need, int
         // tile-major lists: the old tiles keep their addresses, so resident
         // replicas keep their lists and their rebuild schedule
         TRY(grow_keep(c, &c->s.nbr, S_old * (long long)c->K, c->S_cap * (long long)c->K));
+        if (c->prune_on) {
+            TRY(grow_keep(c, &c->s.nbr_in, S_old * (long long)c->K, c->S_cap * (long long)c->K));
+            TRY(grow_keep(c, &c->s.ncnt_in, S_old, c->S_cap));
+            TRY(grow_keep(c, &c->s.recp, S_old, c->S_cap));
+        }
     }
     if (grow_k) {
         dfree(c, &c->s.nbr, (size_t)S_old * (size_t)c->K);
         TRY(dalloc(c, &c->s.nbr, (size_t)c->S_cap * (size_t)K_new));
+        if (c->prune_on) {  // rebuilt, then pruned, before the next force pass
+            dfree(c, &c->s.nbr_in, (size_t)S_old * (size_t)c->K);
+            TRY(dalloc(c, &c->s.nbr_in, (size_t)c->S_cap * (size_t)K_new));
+            if (grow_s) {
+                TRY(grow_fresh(c, &c->s.ncnt_in, S_old, c->S_cap));
+                TRY(grow_fresh(c, &c->s.recp, S_old, c->S_cap));
+            }
+        }
         c->K = K_new;
         force_rebuild_all(c);
     }
@@ -578,11 +597,32 @@ static int fill_desc_smax(const simmd_params* p, double smax, RepDesc& d)
     d.fix_u2 = (float)((L / 4294967296.0) * (L / 4294967296.0));
     d.zeta_lo = (float)(d.zeta - (double)(float)d.zeta);
     d.rv2f = (float)d.rv2;
+    d.dmaxf = (float)smax;
     // build candidates are relative to the home cell centre: a home particle
     // and a stencil candidate differ by at most 2 cs per axis, which needs
     // no minimum image below L/2
     d.build_wrap = (nc >= 3 && 2.0 * d.cs + 1e-3 < 0.5 * L) ? 0 : 1;
     return SIMMD_OK;
+}
+
+// the inner-list fields of a replica's descriptor (after every fill_desc):
+// the inner skin (the outer skin when none is set: the distance test then
+// keeps every listed pair), the cutoff of the inner test with 1e-4 slack, and
+// the displacement trigger in fixed-point units.  A fixed-point displacement
+// |dX| bounds the true one by (|dX| + sqrt(3)) u (each coordinate is rounded
+// to u/2 at both ends), so |dX| <= s_in/(2u) - sqrt(3) keeps it <= s_in/2;
+// one unit more of slack
+static void apply_prune_desc(const simmd_ctx* c, HostRep& h)
+{
+    RepDesc& d = h.d;
+    d.prune = c->prune_on;
+    const double s_in = (h.inner_skin > 0.0 && h.inner_skin < d.skin) ? h.inner_skin : d.skin;
+    d.prune_skin_f = (float)s_in;
+    const double rc = (d.pot == POT_BERTHIER) ? d.rcut : std::sqrt(std::max(d.rc2, d.lj_cut2));
+    d.prune_rcut_f = (float)(rc * (1.0 + 1e-4));
+    const double u = d.L / 4294967296.0;
+    const double A = s_in / (2.0 * u) - std::sqrt(3.0) - 1.0;
+    d.prune_thr = A > 0.0 ? (unsigned long long)std::floor(A * A) : 0ull;
 }
 
 static int push_desc(simmd_ctx* c, int r)
@@ -626,6 +666,7 @@ static int reset_state(simmd_ctx* c, int r, bool keep_counters)
     st.maxcount = mc;
     st.vscale = 1.0;
     st.force_rebuild = 1;
+    st.force_prune = 1;
     CK(cudaMemcpyAsync(c->d_state + r, &st, sizeof(RepState), cudaMemcpyHostToDevice, c->stream));
     CK(cudaStreamSynchronize(c->stream));
     c->h_state[r] = st;
@@ -693,6 +734,7 @@ static int add_replica(simmd_ctx* c, const simmd_params* p, const double* r, con
     h.p = *p;
     h.d = d;
     h.smax = max_diameter(D, p->N);
+    apply_prune_desc(c, h);
     TRY(push_desc(c, rid));
     TRY(reset_state(c, rid, false));
     TRY(upload_rep(c, rid, r, v, F, D, nullptr));
@@ -785,6 +827,27 @@ static void rebuild_launch(simmd_ctx* c, const Batch& b, const LaunchCfg& lc)
     fail(cudaStreamUpdateCaptureDependencies(c->stream, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
 }
 
+// the force pass's view of the batch: the inner (pruned) lists when the
+// context keeps them
+static Batch force_batch(const simmd_ctx* c, const Batch& b)
+{
+    Batch f = b;
+    if (c->prune_on) {
+        f.s.nbr = c->s.nbr_in;
+        f.s.ncnt = c->s.ncnt_in;
+    }
+    return f;
+}
+
+static void prune_launch(simmd_ctx* c, const Batch& b, const LaunchCfg& lc, int ev)
+{
+    if (!c->prune_on) return;
+    const bool prof = c->profile != 0;
+    if (prof) cudaEventRecord(c->pev[ev], c->stream);
+    launch_prune_impl(b, lc);
+    if (prof) cudaEventRecord(c->pev[ev + 1], c->stream);
+}
+
 static void enqueue_step(simmd_ctx* c, const Batch& b, const LaunchCfg& lc, const Mix& m, int fmode)
 {
     const bool prof = c->profile != 0;
@@ -794,9 +857,10 @@ static void enqueue_step(simmd_ctx* c, const Batch& b, const LaunchCfg& lc, cons
         if (prof) cudaEventRecord(c->pev[1], c->stream);
         rebuild_launch(c, b, lc);
         if (prof) cudaEventRecord(c->pev[2], c->stream);
+        prune_launch(c, b, lc, 8);
     }
     if (prof) cudaEventRecord(c->pev[3], c->stream);
-    launch_force_impl(b, lc, fmode, m.prec_mask, nullptr);
+    launch_force_impl(force_batch(c, b), lc, fmode, m.prec_mask, nullptr);
     c->n_force += __builtin_popcount(m.prec_mask);
     if (prof) cudaEventRecord(c->pev[4], c->stream);
     if (m.rescale) launch_rescale_impl(b, lc);
@@ -806,6 +870,7 @@ static void enqueue_step(simmd_ctx* c, const Batch& b, const LaunchCfg& lc, cons
         if (prof) cudaEventRecord(c->pev[6], c->stream);
         rebuild_launch(c, b, lc);
         if (prof) cudaEventRecord(c->pev[7], c->stream);
+        prune_launch(c, b, lc, 10);
     }
     if (prof) {
         cudaStreamSynchronize(c->stream);
@@ -815,6 +880,10 @@ static void enqueue_step(simmd_ctx* c, const Batch& b, const LaunchCfg& lc, cons
             c->prof.kick_ms += ms;
             cudaEventElapsedTime(&ms, c->pev[1], c->pev[2]);
             c->prof.rebuild_ms += ms;
+            if (c->prune_on) {
+                cudaEventElapsedTime(&ms, c->pev[8], c->pev[9]);
+                c->prof.prune_ms += ms;
+            }
         }
         cudaEventElapsedTime(&ms, c->pev[3], c->pev[4]);
         c->prof.force_ms += ms;
@@ -824,30 +893,44 @@ static void enqueue_step(simmd_ctx* c, const Batch& b, const LaunchCfg& lc, cons
             c->prof.update_ms += ms;
             cudaEventElapsedTime(&ms, c->pev[6], c->pev[7]);
             c->prof.rebuild_ms += ms;
+            if (c->prune_on) {
+                cudaEventElapsedTime(&ms, c->pev[10], c->pev[11]);
+                c->prof.prune_ms += ms;
+            }
         }
         c->prof.steps += 1;
     }
 }
 
-// the host's rebuild requests (a new or re-uploaded replica, a skin change,
-// simmd_rebuild): one copy of the replica ids and one marking kernel, then
-// the rebuild sequence, which works only on the marked replicas
+// the host's rebuild and prune requests (a new or re-uploaded replica, a
+// skin change, simmd_rebuild, positions set by the host): one copy of the
+// replica ids and one marking kernel, then the rebuild sequence, which works
+// only on the marked replicas, and the prune
 static int pending_rebuilds(simmd_ctx* c)
 {
     std::vector<int> ids;
+    bool any = false;
     for (int r = 0; r < c->R_cap; r++) {
         HostRep& h = c->reps[r];
-        if (h.active && h.pending_rebuild) {
-            ids.push_back(r);
+        if (h.active && (h.pending_rebuild || h.pending_prune)) {
+            ids.push_back(r * 4 + (h.pending_rebuild ? 1 : 0) + (h.pending_prune ? 2 : 0));
+            any = any || h.pending_rebuild;
             h.pending_rebuild = false;
+            h.pending_prune = false;
         }
     }
     if (!ids.empty()) {
         CK(cudaMemcpyAsync(c->d_mark, ids.data(), sizeof(int) * ids.size(), cudaMemcpyHostToDevice, c->stream));
         launch_mark_rebuild_impl(c->d_mark, (int)ids.size(), c->d_state, c->stream);
+    }
+    if (any || c->prune_on) {
         Batch b = make_batch(c);
         LaunchCfg lc = make_lc(c, FMODE_STEP);
-        rebuild_launch(c, b, lc);
+        if (any) rebuild_launch(c, b, lc);
+        // inner lists before the next force pass: requested prunes (a
+        // rebuild, positions set by the host) and displacements since the
+        // last prune by other movers (minimiser)
+        if (c->prune_on) launch_prune_impl(b, lc);
         CK(cudaGetLastError());
     }
     return SIMMD_OK;
@@ -974,7 +1057,7 @@ static bool xfer_layout(simmd_ctx* c, long long* nvec, long long* nsc)
     for (int r = 0; r < c->R_cap; r++) {
         HostRep& h = c->reps[r];
         if (!h.active) continue;
-        if (h.d.xfer_off != off || h.d.xfer_soff != soff) changed = true;
+        if (h.d.xfer_off != off || h.d.xfer_soff != soff) changed = c->xfer_dirty = true;
         h.d.xfer_off = off;
         h.d.xfer_soff = soff;
         off += h.p.N * h.p.dims;
@@ -993,6 +1076,7 @@ static int push_all_desc(simmd_ctx* c, std::vector<RepDesc>& staging)
     for (int r = 0; r < c->R_cap; r++) staging[(size_t)r] = c->reps[r].d;
     CK(cudaMemcpyAsync(c->d_desc, staging.data(), sizeof(RepDesc) * (size_t)c->R_cap, cudaMemcpyHostToDevice,
                        c->stream));
+    c->xfer_dirty = false;
     return SIMMD_OK;
 }
 
@@ -1020,6 +1104,7 @@ static int refresh_desc(simmd_ctx* c, int rep, const double* D)
     d.xfer_off = h.d.xfer_off;
     d.xfer_soff = h.d.xfer_soff;
     h.d = d;
+    apply_prune_desc(c, h);
     return SIMMD_OK;
 }
 
@@ -1112,7 +1197,7 @@ static void destroy_ctx(simmd_ctx* c)
                     s.ncnt, s.bin_cell, s.bin_rank, s.src, s.t_posD, s.t_vx, s.t_vy, s.t_vz, s.t_fx, s.t_fy,
                     s.t_fz, s.t_orig, s.cell_count, s.cell_start, c->nbr_full, c->ncnt_full, c->epp, c->d_desc,
                     c->d_state, c->d_tile_rep, c->d_red_val, c->d_red_cnt, c->d_warp_part, c->d_tile_cnt, c->d_queue, c->d_stage, c->d_dump, c->d_noise,
-                    c->d_plan_tiles, c->d_plan_cells, c->d_plan_cnt, c->d_mark};
+                    c->d_plan_tiles, c->d_plan_cells, c->d_plan_cnt, c->d_mark, s.nbr_in, s.ncnt_in, s.recp};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (c->dump_stream) cudaStreamSynchronize(c->dump_stream);
@@ -1277,6 +1362,7 @@ int simmd_set_state_r(simmd_ctx* c, int32_t rep, const double* r, const double* 
     launch_set_state_impl(b, lc, rep, h.d, r ? dr : nullptr, v ? dv : nullptr, F ? dF : nullptr, disp ? du : nullptr);
     CK(cudaGetLastError());
     CK(cudaStreamSynchronize(c->stream));
+    if (r) h.pending_prune = true;  // the lists are kept; the inner list is re-pruned
     return SIMMD_OK;
 }
 
@@ -1332,6 +1418,7 @@ int simmd_upload_all(simmd_ctx* c, const double* r, const double* v, const doubl
         st.maxcount = mc;
         st.vscale = 1.0;
         st.force_rebuild = 1;
+        st.force_prune = 1;
     }
     CK(cudaMemcpyAsync(c->d_state, c->h_state.data(), sizeof(RepState) * (size_t)c->R_cap, cudaMemcpyHostToDevice,
                        c->stream));
@@ -1358,7 +1445,9 @@ int simmd_download_all(simmd_ctx* c, double* r, double* v, double* F, double* di
     CK(cudaSetDevice(c->device));
     long long nv = 0, ns = 0;
     std::vector<RepDesc> dstage;
-    if (xfer_layout(c, &nv, &ns)) TRY(push_all_desc(c, dstage));
+    xfer_layout(c, &nv, &ns);
+    // the offsets may have been laid out by an earlier call (simmd_transfer_layout)
+    if (c->xfer_dirty) TRY(push_all_desc(c, dstage));
     if (nv == 0) return set_err(SIMMD_ERR_NOT_FOUND, "no replica");
     TRY(ensure_stage(c, nv));
     double* stg = c->d_stage;
@@ -1613,6 +1702,10 @@ int simmd_set_tuning(simmd_ctx* c, int32_t tpp, int32_t use_graphs, int32_t grap
         if (K != c->K) {
             dfree(c, &c->s.nbr, (size_t)c->S_cap * (size_t)c->K);
             TRY(dalloc(c, &c->s.nbr, (size_t)c->S_cap * (size_t)K));
+            if (c->prune_on) {
+                dfree(c, &c->s.nbr_in, (size_t)c->S_cap * (size_t)c->K);
+                TRY(dalloc(c, &c->s.nbr_in, (size_t)c->S_cap * (size_t)K));
+            }
             c->K = K;
         }
         force_rebuild_all(c);
@@ -1948,12 +2041,74 @@ int simmd_set_skin(simmd_ctx* c, int32_t rep, double skin)
         d.host_noise = h.d.host_noise;
         d.noise_step0 = h.d.noise_step0;
         d.noise_nsteps = h.d.noise_nsteps;
+        d.xfer_off = h.d.xfer_off;
+        d.xfer_soff = h.d.xfer_soff;
         h.p = p;
         h.d = d;
+        apply_prune_desc(c, h);
         TRY(push_desc(c, r));
         h.pending_rebuild = true;
     }
     CK(cudaStreamSynchronize(c->stream));
+    return SIMMD_OK;
+}
+
+int simmd_set_prune(simmd_ctx* c, int32_t rep, double inner_skin)
+{
+    if (!c || !(inner_skin >= 0.0)) return set_err(SIMMD_ERR_BAD_ARG, "bad argument");
+    CK(cudaSetDevice(c->device));
+    if (rep >= 0 && (rep >= c->R_cap || !c->reps[rep].active)) return set_err(SIMMD_ERR_NOT_FOUND, "no such replica");
+    for (int r = 0; r < c->R_cap; r++) {
+        HostRep& h = c->reps[r];
+        if (h.active && (rep < 0 || r == rep)) h.inner_skin = inner_skin;
+    }
+    int on = 0;
+    for (const auto& h : c->reps)
+        if (h.active && h.inner_skin > 0.0) on = 1;
+    if (on && !c->prune_on) {
+        // the inner list, its counts and the prune-time records; every
+        // replica rebuilt (its record refreshed) and pruned before the next
+        // force pass
+        if (c->budget > 0 && c->bytes + c->S_cap * (4LL * c->K + 4 + 16) > c->budget)
+            return set_err(SIMMD_ERR_BUDGET, "device memory budget exceeded");
+        CK(cudaStreamSynchronize(c->stream));
+        TRY(dalloc(c, &c->s.nbr_in, (size_t)c->S_cap * (size_t)c->K));
+        TRY(dalloc(c, &c->s.ncnt_in, (size_t)c->S_cap));
+        TRY(dalloc(c, &c->s.recp, (size_t)c->S_cap));
+        CK(cudaMemsetAsync(c->s.ncnt_in, 0, sizeof(int) * (size_t)c->S_cap, c->stream));
+        c->prune_on = 1;
+        force_rebuild_all(c);
+        invalidate_graph(c);
+    } else if (!on && c->prune_on) {
+        CK(cudaStreamSynchronize(c->stream));
+        dfree(c, &c->s.nbr_in, (size_t)c->S_cap * (size_t)c->K);
+        dfree(c, &c->s.ncnt_in, (size_t)c->S_cap);
+        dfree(c, &c->s.recp, (size_t)c->S_cap);
+        c->prune_on = 0;
+        invalidate_graph(c);
+    }
+    for (int r = 0; r < c->R_cap; r++) {
+        HostRep& h = c->reps[r];
+        if (!h.active) continue;
+        apply_prune_desc(c, h);
+        h.pending_prune = c->prune_on != 0;
+    }
+    std::vector<RepDesc> dstage;
+    TRY(push_all_desc(c, dstage));
+    CK(cudaStreamSynchronize(c->stream));
+    return SIMMD_OK;
+}
+
+int simmd_prune_stats(simmd_ctx* c, int32_t rep, int64_t* prunes, int64_t* inner_entries)
+{
+    if (!c) return set_err(SIMMD_ERR_BAD_ARG, "NULL context");
+    CK(cudaSetDevice(c->device));
+    if (rep < 0 || rep >= c->R_cap || !c->reps[rep].active) return set_err(SIMMD_ERR_NOT_FOUND, "no such replica");
+    RepState st;
+    CK(cudaMemcpyAsync(&st, c->d_state + rep, sizeof(RepState), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    if (prunes) *prunes = st.prunes;
+    if (inner_entries) *inner_entries = st.list_entries_in;
     return SIMMD_OK;
 }
 
@@ -1988,6 +2143,13 @@ int simmd_profile_get(simmd_ctx* c, double* out6)
     out6[3] = c->prof.rebuild_ms;
     out6[4] = c->prof.update_ms;
     out6[5] = (double)c->prof.steps;
+    return SIMMD_OK;
+}
+
+int simmd_profile_prune_ms(simmd_ctx* c, double* ms)
+{
+    if (!c || !ms) return set_err(SIMMD_ERR_BAD_ARG, "NULL argument");
+    *ms = c->prof.prune_ms;
     return SIMMD_OK;
 }
 

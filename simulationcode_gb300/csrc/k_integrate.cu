@@ -39,9 +39,10 @@ __device__ __forceinline__ double half_kick(double v, double F, const RepDesc& d
 }
 
 // r += dr with the reference wrap rnew - floor(rnew/L)*L, displacement update,
-// split record refresh; returns |disp|^2
+// fixed-point record refresh; returns |disp|^2, and in d2in the fixed-point
+// |X - X_prune|^2 when the context keeps inner lists
 __device__ __forceinline__ double drift_slot(const Batch& b, const RepDesc& d, long long i, double drx,
-                                             double dry, double drz)
+                                             double dry, double drz, unsigned long long& d2in)
 {
     const Slots& S = b.s;
     double ux = dadd(S.ux[i], drx), uy = dadd(S.uy[i], dry), uz = 0.0;
@@ -63,19 +64,22 @@ __device__ __forceinline__ double drift_slot(const Batch& b, const RepDesc& d, l
     const double y = wrap_coord(dadd(p.y, dry), d);
     const double z = (d.dims == 3) ? wrap_coord(dadd(p.z, drz), d) : p.z;
     S.posD[i] = make_double4_32a(x, y, z, p.w);
-    if (d.prec == PREC_FP32) {  // the split record's fixed-point position (D kept)
+    if (d.prec == PREC_FP32 || d.prune) {  // the record's fixed-point position (D kept)
         FixRec q = S.rec[i];
         q.x = fix32(x, d);
         q.y = fix32(y, d);
         if (d.dims == 3) q.z = fix32(z, d);
         S.rec[i] = q;
+        if (d.prune) d2in = fix_dist2(q, S.recp[i]);
     }
     return u2;
 }
 
 // block-level max of |disp|^2 (bit pattern; non-negative doubles order as
-// integers), one atomic per tile and only when it raises the replica's max
-__device__ __forceinline__ void block_max_to_state(double u2, RepState& st, unsigned long long* s_max)
+// integers) and of the fixed-point displacement since the last prune, one
+// atomic per tile and only when it raises the replica's max
+__device__ __forceinline__ void block_max_to_state(double u2, unsigned long long d2in, const RepDesc& d,
+                                                   RepState& st, unsigned long long* s_max)
 {
     unsigned long long bits = (unsigned long long)__double_as_longlong(u2);
     if (nonfinite_bits(u2)) {
@@ -86,14 +90,26 @@ __device__ __forceinline__ void block_max_to_state(double u2, RepState& st, unsi
     for (int o = 16; o > 0; o >>= 1) {
         unsigned long long y = __shfl_xor_sync(0xffffffffu, bits, o);
         bits = y > bits ? y : bits;
+        if (d.prune) {
+            y = __shfl_xor_sync(0xffffffffu, d2in, o);
+            d2in = y > d2in ? y : d2in;
+        }
     }
     const int w = threadIdx.x >> 5;
-    if ((threadIdx.x & 31) == 0) s_max[w] = bits;
+    constexpr int NW = TILE / 32;
+    if ((threadIdx.x & 31) == 0) {
+        s_max[w] = bits;
+        s_max[NW + w] = d2in;
+    }
     __syncthreads();
     if (threadIdx.x == 0) {
-        unsigned long long m = s_max[0];
-        for (int k = 1; k < (int)(blockDim.x >> 5); k++) m = s_max[k] > m ? s_max[k] : m;
+        unsigned long long m = s_max[0], mi = s_max[NW];
+        for (int k = 1; k < (int)(blockDim.x >> 5); k++) {
+            m = s_max[k] > m ? s_max[k] : m;
+            mi = s_max[NW + k] > mi ? s_max[NW + k] : mi;
+        }
         if (m > *(volatile unsigned long long*)&st.maxdisp2) atomicMax(&st.maxdisp2, m);
+        if (d.prune && mi > *(volatile unsigned long long*)&st.maxdisp_in) atomicMax(&st.maxdisp_in, mi);
     }
     __syncthreads();
 }
@@ -107,7 +123,7 @@ __device__ __forceinline__ void block_max_to_state(double u2, RepState& st, unsi
 // kick1 + drift for Newtonian / Langevin replicas (src/MD.jl:510-522)
 __global__ void __launch_bounds__(TILE, SIMMD_UPD_MINB) k_kick_drift(Batch b)
 {
-    __shared__ unsigned long long s_max[TILE / 32];
+    __shared__ unsigned long long s_max[2 * (TILE / 32)];
     for (int t = blockIdx.x; t < b.ntiles; t += gridDim.x) {
         int r = b.tile_rep[t];
         if (r < 0) continue;
@@ -116,6 +132,7 @@ __global__ void __launch_bounds__(TILE, SIMMD_UPD_MINB) k_kick_drift(Batch b)
         RepState& st = b.state[r];
         long long i = (long long)t * TILE + threadIdx.x;
         double u2 = 0.0;
+        unsigned long long d2in = 0ull;
         if (i < d.slot0 + d.n) {
             const Slots& S = b.s;
             const double vs = st.vscale;
@@ -138,9 +155,9 @@ __global__ void __launch_bounds__(TILE, SIMMD_UPD_MINB) k_kick_drift(Batch b)
                 vz = half_kick(vz, S.fz[i], d);
                 S.vz[i] = vz;
             }
-            u2 = drift_slot(b, d, i, dmul(d.dt, vx), dmul(d.dt, vy), dmul(d.dt, vz));
+            u2 = drift_slot(b, d, i, dmul(d.dt, vx), dmul(d.dt, vy), dmul(d.dt, vz), d2in);
         }
-        block_max_to_state(u2, st, s_max);
+        block_max_to_state(u2, d2in, d, st, s_max);
     }
 }
 
@@ -151,7 +168,7 @@ __global__ void __launch_bounds__(TILE, SIMMD_UPD_MINB) k_kick_drift(Batch b)
 // precision: one fused multiply-add (the force is FP32-accurate anyway).
 __global__ void __launch_bounds__(TILE, SIMMD_UPD_MINB) k_brownian_update(Batch b)
 {
-    __shared__ unsigned long long s_max[TILE / 32];
+    __shared__ unsigned long long s_max[2 * (TILE / 32)];
     for (int t = blockIdx.x; t < b.ntiles; t += gridDim.x) {
         int r = b.tile_rep[t];
         if (r < 0) continue;
@@ -160,6 +177,7 @@ __global__ void __launch_bounds__(TILE, SIMMD_UPD_MINB) k_brownian_update(Batch 
         RepState& st = b.state[r];
         long long i = (long long)t * TILE + threadIdx.x;
         double u2 = 0.0;
+        unsigned long long d2in = 0ull;
         if (i < d.slot0 + d.n) {
             const Slots& S = b.s;
             const double c = d.dt_over_gamma;
@@ -191,9 +209,9 @@ __global__ void __launch_bounds__(TILE, SIMMD_UPD_MINB) k_brownian_update(Batch 
                     }
                 }
             }
-            u2 = drift_slot(b, d, i, drx, dry, drz);
+            u2 = drift_slot(b, d, i, drx, dry, drz, d2in);
         }
-        block_max_to_state(u2, st, s_max);
+        block_max_to_state(u2, d2in, d, st, s_max);
     }
 }
 
@@ -258,7 +276,7 @@ __global__ void k_min_max(Batch b, double dt)
 // max_step, wrap, displacement, skin max
 __global__ void k_min_drift(Batch b, double dt, double max_step)
 {
-    __shared__ unsigned long long s_max[TILE / 32];
+    __shared__ unsigned long long s_max[2 * (TILE / 32)];
     for (int t = blockIdx.x; t < b.ntiles; t += gridDim.x) {
         const int r = b.tile_rep[t];
         if (r < 0) continue;
@@ -268,6 +286,7 @@ __global__ void k_min_drift(Batch b, double dt, double max_step)
         const double stepsize = __longlong_as_double((long long)st.min_step);
         const long long i = (long long)t * TILE + threadIdx.x;
         double u2 = 0.0;
+        unsigned long long d2in = 0ull;
         if (i < d.slot0 + d.n) {
             const Slots& S = b.s;
             double vx = dmul(S.fx[i], dt), vy = dmul(S.fy[i], dt), vz = d.dims == 3 ? dmul(S.fz[i], dt) : 0.0;
@@ -277,9 +296,9 @@ __global__ void k_min_drift(Batch b, double dt, double max_step)
                 vy = dmul(vy, sc);
                 vz = dmul(vz, sc);
             }
-            u2 = drift_slot(b, d, i, vx, vy, vz);
+            u2 = drift_slot(b, d, i, vx, vy, vz, d2in);
         }
-        block_max_to_state(u2, st, s_max);
+        block_max_to_state(u2, d2in, d, st, s_max);
     }
 }
 
@@ -501,7 +520,7 @@ __global__ void k_set_state(Batch b, int rep, const double* r, const double* v, 
         p.y = r[o * dm + 1];
         if (dm == 3) p.z = r[o * dm + 2];
         S.posD[s] = p;
-        if (d.prec == PREC_FP32) S.rec[s] = fix_rec(p.x, p.y, p.z, p.w, d);
+        if (d.prec == PREC_FP32 || d.prune) S.rec[s] = fix_rec(p.x, p.y, p.z, p.w, d);
     }
     if (v) {
         S.vx[s] = v[o * dm];

@@ -159,7 +159,7 @@ __device__ void mc_chain(const Batch& b, const RepDesc& d, RepState& st, const u
                             S.uz[si] = uz;
                             u2 = dadd(u2, dmul(uz, uz));
                         }
-                        if (d.prec == PREC_FP32) S.rec[si] = fix_rec(rn[0], rn[1], rn[2], pi.w, d);
+                        if (d.prec == PREC_FP32 || d.prune) S.rec[si] = fix_rec(rn[0], rn[1], rn[2], pi.w, d);
                         rebuild = u2 > d.skin_half2;
                     }
                     if (rebuild) {  // src/MC.jl:147-149: rebuild before the next move
@@ -190,7 +190,7 @@ __device__ void mc_chain(const Batch& b, const RepDesc& d, RepState& st, const u
                         st.mc_dE = dadd(st.mc_dE, dE);
                         S.posD[si] = make_double4_32a(pi.x, pi.y, pi.z, Dj);
                         S.posD[sj] = make_double4_32a(pj.x, pj.y, pj.z, Di);
-                        if (d.prec == PREC_FP32) {
+                        if (d.prec == PREC_FP32 || d.prune) {
                             S.rec[si].d = d2f_rn(Dj);
                             S.rec[sj].d = d2f_rn(Di);
                         }

@@ -249,19 +249,28 @@ __device__ __forceinline__ double mean_d_f64(const RepDesc& d, double Di, double
 // Verlet build, one home cell at a time: the block stages the candidates of
 // the home cell's stencil (27 cells in 3D, 9 in 2D; one cell along an axis
 // with fewer than three cells) in shared memory, then Tb lanes per home
-// particle test them in candidate order.  A lane's candidate passes an FP32
-// prefilter on the split-precision offsets, then the exact FP64 test of the
-// reference: d2 <= verlet^2 (the pair enumeration radius) and
+// particle test them, lane `sub` the candidates sub, sub + Tb, ...  Each
+// candidate gets an FP32 test against the reference thresholds with a
+// margin, and the exact FP64 test of the reference in the band around a
+// threshold: d2 <= verlet^2 (the pair enumeration radius) and
 // d2 < (sqrt(rc2)*mean_d + skin)^2 (add_pair!, src/NeighborLists.jl:82-104).
-// Accepted entries are appended in candidate order (warp ballot + popc), so
-// the list order is a pure function of the replica's own state.
+// 2D (few candidates per lane): one pass in candidate order, accepted
+// entries appended through a warp ballot.  3D (hundreds of candidates, ~1 in
+// 8 near enough): per window of 32 candidates per lane, first a radius
+// filter alone -- FP32 d2 against a bound of every threshold the home
+// particle can meet (its largest pair diameter; the Verlet radius as cap) --
+// kept as a bit mask in a register, then the full test on the survivors, one
+// per lane and round, appended in lane order per round.  A candidate the
+// filter drops lies above every threshold's band, so the full test would
+// have rejected it.  Either way the list order is a pure function of the
+// replica's own state.
 // ---------------------------------------------------------------------------
 constexpr int BLD_THREADS = 128;
 constexpr int BLD_CHUNK = 512;
 
 struct BuildSmem {
     float4 o[BLD_CHUNK];  // position relative to the home cell's reference point (FP32), D
-    int slot[BLD_CHUNK];
+    int slot[BLD_CHUNK];  // slot of the candidate (-1: padding of the last round)
     int ca[27];
     int cn[27];
     int pre[28];
@@ -270,6 +279,63 @@ struct BuildSmem {
     unsigned long long entries;
     int maxcnt;
 };
+
+template <int DIM, bool WRAP>
+__device__ __forceinline__ float build_d2(const float4& oi, const float4& oj, const RepDesc& d)
+{
+    const float dxf = WRAP ? min_image_f32(oi.x - oj.x, d.halfLf, d.Lf) : oi.x - oj.x;
+    const float dyf = WRAP ? min_image_f32(oi.y - oj.y, d.halfLf, d.Lf) : oi.y - oj.y;
+    float d2f = dxf * dxf + dyf * dyf;
+    if (DIM == 3) {
+        const float dzf = WRAP ? min_image_f32(oi.z - oj.z, d.halfLf, d.Lf) : oi.z - oj.z;
+        d2f += dzf * dzf;
+    }
+    return d2f;
+}
+
+// the full test of candidate q for home particle i: pred (half list),
+// predf (the Verlet list)
+template <int DIM, bool FULL, bool WRAP>
+__device__ __forceinline__ void build_classify(const Slots& S, const RepDesc& d, const BuildSmem& sm, int q,
+                                               long long i, const float4& oi, const double4_32a& pi,
+                                               long long halfLb, float flo, float fhi, int& j, bool& pred,
+                                               bool& predf)
+{
+    j = sm.slot[q];
+    if (j < 0 || j == (int)i) return;
+    const float4 oj = sm.o[q];
+    const float d2f = build_d2<DIM, WRAP>(oi, oj, d);
+    // FP32 classification against the reference thresholds with a relative
+    // margin (1e-5) far above the FP32 error of d2 and of the thresholds
+    // (~1e-6): clear accepts and rejects are the reference's decisions; the
+    // exact FP64 test runs only in the narrow band around a threshold, so the
+    // pair set stays bit-identical while the FP64 pipe stays idle
+    float tf = (d.pot == POT_LJ) ? d.rcutf * d.sigma2f
+                                 : d.rcutf * ((oi.w + oj.w) * 0.5f * (1.0f - d.zetaf * fabsf(oi.w - oj.w)));
+    tf += d.skinf;
+    const float thr = fminf(tf * tf, d.rv2f);
+    const float lo = thr * (1.0f - 1e-5f), hi = thr * (1.0f + 1e-5f);
+    const bool band = (d2f >= lo && d2f <= hi) || (FULL && d2f >= flo && d2f <= fhi);
+    if (!band) {
+        pred = d2f < lo;
+        predf = d2f < flo;
+        return;
+    }
+    // exact FP64 test in the reference's operation order
+    const double4_32a pj = S.t_posD[j];
+    const double ddx = min_image_f64(dsub(pi.x, pj.x), halfLb, d.L);
+    const double ddy = min_image_f64(dsub(pi.y, pj.y), halfLb, d.L);
+    double d2 = dadd(dmul(ddx, ddx), dmul(ddy, ddy));
+    if (DIM == 3) {
+        const double ddz = min_image_f64(dsub(pi.z, pj.z), halfLb, d.L);
+        d2 = dadd(d2, dmul(ddz, ddz));
+    }
+    if (d2 <= d.rv2) {
+        predf = true;
+        const double tt = dadd(dmul(d.rcut, mean_d_f64(d, pi.w, pj.w)), d.skin);
+        pred = d2 < dmul(tt, tt);
+    }
+}
 
 template <int DIM, bool FULL, bool WRAP>
 __device__ void build_cell(const Batch& b, const RepDesc& d, RepState& st, int c, BuildSmem& sm,
@@ -323,9 +389,11 @@ __device__ void build_cell(const Batch& b, const RepDesc& d, RepState& st, int c
     const int lane = tid & 31;
     const int gbase = (lane / Tb) * Tb;
     const unsigned gmask = (Tb == 32) ? 0xffffffffu : ((1u << Tb) - 1u);
+    const unsigned below = (1u << sub) - 1u;
     const int K = b.K, tsh = 31 - __clz(b.tpp);  // threads per particle: a power of two
     const long long SS = b.S;
     const long long halfLb = __double_as_longlong(d.halfL);
+    const float flo = d.rv2f * (1.0f - 1e-5f), fhi = d.rv2f * (1.0f + 1e-5f);
     for (int base = 0; base < P; base += BLD_THREADS / Tb) {
         const int p = base + tid / Tb;
         const bool active = p < P;
@@ -338,88 +406,94 @@ __device__ void build_cell(const Batch& b, const RepDesc& d, RepState& st, int c
                              DIM == 3 ? (float)(int)(q.z - rfz) * u : 0.0f, q.d);
             pi = S.t_posD[i];
         }
+        // the filter radius: every pair threshold of this home particle
+        // (pair diameter <= (D_i + max D) / 2) and its band lie below it, with
+        // 1e-4 relative slack for the FP32 roundings of both forms; nothing
+        // passes for a lane without a home particle
+        float r1 = -1.0f;
+        if (active) {
+            float tm = (d.pot == POT_LJ) ? d.rcutf * d.sigma2f : d.rcutf * ((oi.w + d.dmaxf) * 0.5f);
+            tm += d.skinf;
+            r1 = (FULL ? d.rv2f : fminf(tm * tm, d.rv2f)) * (1.0f + 1e-4f);
+        }
         int cnt = 0, cntf = 0;
+        // one accepted-or-not decision per lane -> appended in lane order
+        auto append = [&](bool pred, bool predf, int j) {
+            const unsigned gb = (__ballot_sync(0xffffffffu, pred) >> gbase) & gmask;
+            if (pred) {
+                const int pos = cnt + __popc(gb & below);
+                if (pos < K) S.nbr[nbr_addr_sh(pos, i, tsh, K)] = (unsigned)j;
+            }
+            cnt += __popc(gb);
+            if (FULL) {
+                const unsigned gf = (__ballot_sync(0xffffffffu, predf) >> gbase) & gmask;
+                if (predf) {
+                    const int pos = cntf + __popc(gf & below);
+                    if (pos < Kfull) nbr_full[(size_t)pos * SS + i] = (unsigned)j;
+                }
+                cntf += __popc(gf);
+            }
+        };
         for (int c0 = 0; c0 < M; c0 += BLD_CHUNK) {
             const int len = min(BLD_CHUNK, M - c0);
+            // candidates of this chunk, then padding up to the last round's end
+            const int lenr = min(BLD_CHUNK, (len + Tb - 1) / Tb * Tb);
             __syncthreads();
-            for (int q = tid; q < len; q += BLD_THREADS) {
+            for (int q = tid; q < lenr; q += BLD_THREADS) {
+                if (q >= len) {
+                    sm.o[q] = make_float4(1e30f, 1e30f, 1e30f, 0.0f);
+                    sm.slot[q] = -1;
+                    continue;
+                }
                 const int idx = c0 + q;
+                // the stencil cell holding candidate idx: the last k with pre[k] <= idx
                 int k = 0;
-                while (k + 1 < nst && sm.pre[k + 1] <= idx) k++;
+#pragma unroll
+                for (int step = 16; step >= 1; step >>= 1)
+                    if (k + step < nst && sm.pre[k + step] <= idx) k += step;
                 const int j = sm.ca[k] + (idx - sm.pre[k]);
-                const FixRec c = S.rec[j];
-                sm.o[q] = make_float4((float)(int)(c.x - rfx) * u, (float)(int)(c.y - rfy) * u,
-                                      DIM == 3 ? (float)(int)(c.z - rfz) * u : 0.0f, c.d);
+                const FixRec cr = S.rec[j];
+                sm.o[q] = make_float4((float)(int)(cr.x - rfx) * u, (float)(int)(cr.y - rfy) * u,
+                                      DIM == 3 ? (float)(int)(cr.z - rfz) * u : 0.0f, cr.d);
                 sm.slot[q] = j;
             }
             __syncthreads();
             // a warp with no home particle in this pass skips the candidates
-            // (warp-uniform: the ballots below stay within full warps)
-            const int qend = __any_sync(0xffffffffu, active) ? len : 0;
-            for (int q0 = 0; q0 < qend; q0 += Tb) {
-                const int q = q0 + sub;
-                bool pred = false, predf = false;
-                if (active && q < len) {
-                    const int j = sm.slot[q];
-                    if (j != (int)i) {
-                        const float4 oj = sm.o[q];
-                        const float dxf = WRAP ? min_image_f32(oi.x - oj.x, d.halfLf, d.Lf) : oi.x - oj.x;
-                        const float dyf = WRAP ? min_image_f32(oi.y - oj.y, d.halfLf, d.Lf) : oi.y - oj.y;
-                        float d2f = dxf * dxf + dyf * dyf;
-                        if (DIM == 3) {
-                            const float dzf = WRAP ? min_image_f32(oi.z - oj.z, d.halfLf, d.Lf) : oi.z - oj.z;
-                            d2f += dzf * dzf;
-                        }
-                        // FP32 classification against the reference thresholds with a
-                        // relative margin (1e-5) far above the FP32 error of d2 and of
-                        // the thresholds (~1e-6): clear accepts and rejects are the
-                        // reference's decisions; the exact FP64 test runs only in the
-                        // narrow band around a threshold, so the pair set stays
-                        // bit-identical while the FP64 pipe stays idle
-                        float tf = (d.pot == POT_LJ) ? d.rcutf * d.sigma2f
-                                                     : d.rcutf * ((oi.w + oj.w) * 0.5f *
-                                                                  (1.0f - d.zetaf * fabsf(oi.w - oj.w)));
-                        tf += d.skinf;
-                        const float thr = fminf(tf * tf, d.rv2f);
-                        const float lo = thr * (1.0f - 1e-5f), hi = thr * (1.0f + 1e-5f);
-                        const float flo = d.rv2f * (1.0f - 1e-5f), fhi = d.rv2f * (1.0f + 1e-5f);
-                        const bool band = (d2f >= lo && d2f <= hi) || (FULL && d2f >= flo && d2f <= fhi);
-                        if (!band) {
-                            pred = d2f < lo;
-                            predf = d2f < flo;
-                        } else {
-                            // exact FP64 test in the reference's operation order
-                            const double4_32a pj = S.t_posD[j];
-                            const double ddx = min_image_f64(dsub(pi.x, pj.x), halfLb, d.L);
-                            const double ddy = min_image_f64(dsub(pi.y, pj.y), halfLb, d.L);
-                            double d2 = dadd(dmul(ddx, ddx), dmul(ddy, ddy));
-                            if (DIM == 3) {
-                                const double ddz = min_image_f64(dsub(pi.z, pj.z), halfLb, d.L);
-                                d2 = dadd(d2, dmul(ddz, ddz));
-                            }
-                            if (d2 <= d.rv2) {
-                                predf = true;
-                                const double tt = dadd(dmul(d.rcut, mean_d_f64(d, pi.w, pj.w)), d.skin);
-                                pred = d2 < dmul(tt, tt);
-                            }
-                        }
-                    }
+            // (warp-uniform: the ballots stay within full warps)
+            const int qend = __any_sync(0xffffffffu, active) ? lenr : 0;
+            if (DIM == 2) {
+                for (int q0 = 0; q0 < qend; q0 += Tb) {
+                    bool pred = false, predf = false;
+                    int j = -1;
+                    if (active) build_classify<DIM, FULL, WRAP>(S, d, sm, q0 + sub, i, oi, pi, halfLb, flo, fhi, j,
+                                                                pred, predf);
+                    append(pred, predf, j);
                 }
-                const unsigned bal = __ballot_sync(0xffffffffu, pred);
-                const unsigned gb = (bal >> gbase) & gmask;
-                if (pred) {
-                    const int pos = cnt + __popc(gb & ((1u << sub) - 1u));
-                    if (pos < K) S.nbr[nbr_addr_sh(pos, i, tsh, K)] = (unsigned)sm.slot[q];
-                }
-                cnt += __popc(gb);
-                if (FULL) {
-                    const unsigned balf = __ballot_sync(0xffffffffu, predf);
-                    const unsigned gf = (balf >> gbase) & gmask;
-                    if (predf) {
-                        const int pos = cntf + __popc(gf & ((1u << sub) - 1u));
-                        if (pos < Kfull) nbr_full[(size_t)pos * SS + i] = (unsigned)sm.slot[q];
+            } else {
+                const int win = Tb * 32;
+                for (int w0 = 0; w0 < qend; w0 += win) {
+                    // radius filter: bit k of mask = candidate w0 + k*Tb + sub
+                    const int nr = min(32, (qend - w0) / Tb);
+                    unsigned mask = 0u;
+                    {
+                        int q = w0 + sub;
+#pragma unroll 8
+                        for (int k = 0; k < nr; k++, q += Tb)
+                            mask |= (build_d2<DIM, WRAP>(oi, sm.o[q], d) <= r1) ? (1u << k) : 0u;
                     }
-                    cntf += __popc(gf);
+                    // the survivors: one per lane and round
+                    const int rounds = __reduce_max_sync(0xffffffffu, __popc(mask));
+                    for (int rr = 0; rr < rounds; rr++) {
+                        bool pred = false, predf = false;
+                        int j = -1;
+                        if (mask) {
+                            const int k = __ffs(mask) - 1;
+                            mask &= mask - 1u;
+                            build_classify<DIM, FULL, WRAP>(S, d, sm, w0 + k * Tb + sub, i, oi, pi, halfLb, flo,
+                                                            fhi, j, pred, predf);
+                        }
+                        append(pred, predf, j);
+                    }
                 }
             }
         }
@@ -439,9 +513,11 @@ __device__ void build_cell(const Batch& b, const RepDesc& d, RepState& st, int c
 
 // one block per cell task of the plan; FULL: the full (Verlet) list as well
 // (parity tests), kept in its own kernel so the production kernel's register
-// budget is that of the half list alone
+// budget is that of the half list alone.  8 blocks per SM (64 registers):
+// the latency of the staging loads and barriers is hidden by more cells in
+// flight
 template <bool FULL>
-__global__ void __launch_bounds__(BLD_THREADS) k_rb_build(Batch b, unsigned* nbr_full, int* ncnt_full, int Kfull)
+__global__ void __launch_bounds__(BLD_THREADS, 8) k_rb_build(Batch b, unsigned* nbr_full, int* ncnt_full, int Kfull)
 {
     __shared__ BuildSmem sm;
     const int ntask = plan_count(b, 1);
@@ -509,13 +585,110 @@ __global__ void k_rb_done(Batch b)
     st.maxdisp2 = 0ull;
     st.force_rebuild = 0;
     st.rebuilds += 1;
+    st.force_prune = 1;  // the slots were re-ordered: the inner list follows
 }
 
-// the host's rebuild requests: one thread per requested replica
+// ---------------------------------------------------------------------------
+// Inner (pruned) list of the force pass, per replica whose trigger fired
+// (a particle moved more than prune_skin/2 since the last prune) or that was
+// rebuilt: the outer-list entries j of i with
+//     |r_ij| <= sqrt(rc2) * s_ij * (1 + 1e-4) + prune_skin
+// on the fixed-point records (s_ij the pair diameter of the potential, FP32),
+// (LJ: |r_ij| <= r_cut * (1 + 1e-4) + prune_skin, r_cut the larger of the
+// force and energy cutoffs) in the outer list's order.  A pair within the
+// force cutoff at a later
+// step was within sqrt(rc2)*s_ij + prune_skin at the prune (each particle
+// moved at most prune_skin/2), and the 1e-4 slack covers the FP32 roundings
+// of the test, so the inner list holds every pair the force pass finds in
+// range; the pairs it drops were out of range and add exactly zero.
+// One thread per particle, whole tiles of the pruning replicas.
+// ---------------------------------------------------------------------------
+constexpr int PRUNE_UNROLL = 4;
+
+__global__ void __launch_bounds__(TILE) k_prune(Batch b)
+{
+    for (int t = blockIdx.x; t < b.ntiles; t += gridDim.x) {
+        const int r = b.tile_rep[t];
+        if (r < 0) continue;
+        const RepDesc& d = b.desc[r];
+        if (!d.active || !need_prune(b.state[r], d)) continue;
+        const long long i = (long long)t * TILE + threadIdx.x;
+        const Slots& S = b.s;
+        int m = 0;
+        if (i < d.slot0 + d.n) {
+            const FixRec ri = S.rec[i];
+            S.recp[i] = ri;
+            const int cnt = S.ncnt[i], K = b.K, T = b.tpp;
+            const float u2 = d.fix_u2, sk = d.prune_skin_f, rcf = d.prune_rcut_f;
+            const bool ber = d.pot == POT_BERTHIER;
+            auto keep = [&](const FixRec& rj) {
+                const float r2 = __ull2float_rn(fix_dist2(ri, rj)) * u2;
+                float tt = rcf + sk;  // LJ: one cutoff radius
+                if (ber) {
+                    const float sij = (ri.d + rj.d) * 0.5f * (1.0f - d.zetaf * fabsf(ri.d - rj.d));
+                    tt = fmaf(rcf, sij, sk);
+                }
+                return r2 <= tt * tt;
+            };
+            // PRUNE_UNROLL entries and their records loaded before the tests
+            int n = 0;
+            for (; n + PRUNE_UNROLL <= cnt; n += PRUNE_UNROLL) {
+                unsigned e[PRUNE_UNROLL];
+                FixRec q[PRUNE_UNROLL];
+#pragma unroll
+                for (int u = 0; u < PRUNE_UNROLL; u++) e[u] = __ldg(S.nbr + nbr_addr(n + u, i, T, K));
+#pragma unroll
+                for (int u = 0; u < PRUNE_UNROLL; u++) q[u] = rec_get(S.rec + (e[u] & IDX_MASK));
+#pragma unroll
+                for (int u = 0; u < PRUNE_UNROLL; u++)
+                    if (keep(q[u])) S.nbr_in[nbr_addr(m++, i, T, K)] = e[u];
+            }
+            for (; n < cnt; n++) {
+                const unsigned e = __ldg(S.nbr + nbr_addr(n, i, T, K));
+                if (keep(rec_get(S.rec + (e & IDX_MASK)))) S.nbr_in[nbr_addr(m++, i, T, K)] = e;
+            }
+        }
+        S.ncnt_in[i] = m;
+        // the replica's inner-list size: one atomic per warp (the whole
+        // block takes this branch: one replica per tile)
+        unsigned long long sum = (unsigned long long)m;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+        if ((threadIdx.x & 31) == 0 && sum) atomicAdd(&b.state[r].entries_in_acc, sum);
+    }
+}
+
+// after the prune: the pruned replicas' triggers reset, inner-list sizes
+__global__ void k_prune_done(Batch b)
+{
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= b.nreps) return;
+    const RepDesc& d = b.desc[r];
+    RepState& st = b.state[r];
+    if (!d.active || !need_prune(st, d)) return;
+    st.maxdisp_in = 0ull;
+    st.force_prune = 0;
+    st.prunes += 1;
+    st.list_entries_in = (long long)st.entries_in_acc;
+    st.entries_in_acc = 0ull;
+}
+
+void launch_prune_impl(const Batch& b, const LaunchCfg& lc)
+{
+    k_prune<<<lc.grid_stream, TILE, 0, lc.stream>>>(b);
+    k_prune_done<<<(b.nreps + 127) / 128, 128, 0, lc.stream>>>(b);
+    if (lc.launches) *lc.launches += 2;
+}
+
+// the host's requests: one thread per entry rep * 4 + flags (1 rebuild,
+// 2 prune)
 __global__ void k_mark_rebuild(const int* reps, int n, RepState* state)
 {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k < n) state[reps[k]].force_rebuild = 1;
+    if (k >= n) return;
+    const int e = reps[k];
+    if (e & 1) state[e >> 2].force_rebuild = 1;
+    if (e & 2) state[e >> 2].force_prune = 1;
 }
 
 void launch_mark_rebuild_impl(const int* reps, int n, RepState* state, cudaStream_t s)

@@ -71,7 +71,15 @@ struct RepDesc {
     const double* host_noise;  // [noise_nsteps][n][dims], original order
     long long noise_step0;
     int noise_nsteps;
-    int pad_;
+    float dmaxf;               // max(D) rounded to FP32: bounds every pair threshold of the build
+    // pruned (inner) list of the force pass: the outer-list pairs within
+    // rc_ij + prune_skin at the last prune, valid while no particle has moved
+    // prune_skin / 2 since (the pairs it drops add exactly zero to the sums)
+    int prune;                 // the context keeps inner lists (every replica)
+    float prune_rcut_f;        // (1 + 1e-4) sqrt(rc2) (Berthier: times s_ij; LJ: the larger of the force and
+                               // energy cutoff radii) in FP32: the inner test's cutoff, with slack
+    float prune_skin_f;        // inner skin (FP32)
+    unsigned long long prune_thr;  // prune when max |dX|^2 since the last prune exceeds this (fixed-point units^2)
 };
 
 struct RepState {
@@ -106,6 +114,13 @@ struct RepState {
     double mc_dE;                 // sum of the accepted moves' energy changes
     int mc_next;                  // next particle of the current sweep
     int mc_active;                // replica takes part in the MC call
+    // inner list
+    unsigned long long maxdisp_in;  // max |X - X_prune|^2 (fixed-point units^2) since the last prune
+    int force_prune;              // prune before the next force pass (rebuild, host request)
+    int pad_prune;
+    long long prunes;             // prunes done
+    long long list_entries_in;    // inner-list entries at the last prune
+    unsigned long long entries_in_acc;  // ... summed by the prune in progress
 };
 
 // split-precision gather record (16 bytes, one 128-bit load): the FP64
@@ -127,6 +142,9 @@ struct Slots {
     int* inv;                     // slot of original id k of a replica at inv[slot0 + k]
     unsigned* nbr;                // ELL neighbour list
     int* ncnt;                    // neighbours per slot
+    unsigned* nbr_in;             // inner (pruned) list, the same layout; null when not kept
+    int* ncnt_in;
+    FixRec* recp;                 // the record at the last prune (displacement since)
     // rebuild scratch
     int* bin_cell;
     int* bin_rank;
@@ -277,6 +295,19 @@ __device__ __forceinline__ FixRec rec_get(const FixRec* __restrict__ r)
 __device__ __forceinline__ bool need_rebuild(const RepState& st, const RepDesc& d)
 {
     return st.force_rebuild || (__longlong_as_double((long long)st.maxdisp2) > d.skin_half2);
+}
+
+__device__ __forceinline__ bool need_prune(const RepState& st, const RepDesc& d)
+{
+    return d.prune && (st.force_prune || st.maxdisp_in > d.prune_thr);
+}
+
+// |X - X0|^2 of two fixed-point records in fixed-point units^2 (exact; the
+// int32 wraparound is the minimum image)
+__device__ __forceinline__ unsigned long long fix_dist2(const FixRec& a, const FixRec& b)
+{
+    const long long ex = (int)(a.x - b.x), ey = (int)(a.y - b.y), ez = (int)(a.z - b.z);
+    return (unsigned long long)(ex * ex) + (unsigned long long)(ey * ey) + (unsigned long long)(ez * ez);
 }
 
 // List layout, tile-major: the TILE slots of a tile own TILE*K consecutive

@@ -165,3 +165,29 @@ def test_batched_host_transfers_equal_per_replica_calls(simlib):
         assert a.stats(ia[k]).rebuilds == b.stats(ib[k]).rebuilds
     a.close()
     b.close()
+
+
+def test_download_all_after_layout_query_and_skin_change(simlib):
+    """simmd_download_all right after simmd_transfer_layout (no upload in
+    between) and after a skin change: every replica's block equals its
+    simmd_download_r copy (the device descriptors get the offsets that the
+    layout query set on the host)."""
+    specs = _relaxed(_mixed_specs(seed=5))
+    b = ReplicaBatch(0)
+    ids = [b.add(s) for s in specs]
+    b.rebuild()
+    b.step(4)
+
+    def check():
+        total, offs = b.transfer_layout()
+        r = np.full(total, np.nan)
+        b.download_all(r)
+        for rid, s in zip(ids, specs):
+            o, n = offs[rid], s.N * s.dims
+            assert np.array_equal(b.state(rid)[0].reshape(-1), r[o:o + n]), rid
+
+    check()
+    b.set_skin(0.45, ids[2])
+    b.step(3)
+    check()
+    b.close()
