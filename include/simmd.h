@@ -287,12 +287,12 @@ int simmd_set_skin(simmd_ctx* ctx, int32_t rep, double skin);
  * and whenever a particle of the replica has moved more than inner_skin / 2
  * since the last prune, the replica's list is filtered to the pairs within
  * rc_ij + inner_skin (outer-list order kept); the force pass reads the
- * filtered list.  The dropped pairs lie beyond the force cutoff until the
- * next prune and add exactly zero, so with one thread per particle every
- * force, energy and trajectory is bit-identical to the unfiltered list's
- * (with more threads per particle the pairs regroup among the threads: the
- * sums agree to rounding); the rebuild schedule (skin trigger) is
- * unchanged.
+ * filtered list, and a force pass that finds a replica's filter due reads
+ * the full list and writes the filtered one while it sums.  The dropped
+ * pairs lie beyond the force cutoff until the next filter and add exactly
+ * zero, so every force, energy and trajectory is bit-identical to the
+ * unfiltered list's; the rebuild schedule (skin trigger) is unchanged.
+ * Needs one thread per particle (simmd_set_tuning tpp = 1).
  * inner_skin > 0 for one replica (or every replica: rep = -1) turns the
  * filtering on for the context (replicas without an inner skin keep every
  * listed pair); 0 on every replica turns it off.  Costs 4K + 20 device
@@ -321,8 +321,6 @@ int simmd_set_profile(simmd_ctx* ctx, int32_t enable);
 int simmd_host_register(void* ptr, int64_t bytes);
 int simmd_host_unregister(void* ptr);
 int simmd_profile_get(simmd_ctx* ctx, double* out6);
-/* the profile's time in list pruning (ms total; simmd_set_prune) */
-int simmd_profile_prune_ms(simmd_ctx* ctx, double* ms);
 /* self-check of the split-precision kernels' float <-> double conversions
  * (bit operations on the integer pipes) against the hardware converter on
  * the current device: n hashed float and double bit patterns (all classes,

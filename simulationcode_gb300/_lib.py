@@ -115,7 +115,6 @@ SIGNATURES = {
     "simmd_host_unregister": (C.c_int, [_vp]),
     "simmd_energy_virial_noalloc": (C.c_int, [_P(Params), _vp, _vp, _vp, _vp, C.c_int64, _vp, _vp]),
     "simmd_profile_get": (C.c_int, [_vp, _vp]),
-    "simmd_profile_prune_ms": (C.c_int, [_vp, _vp]),
     "simmd_check_conversions": (C.c_int, [C.c_int64, C.c_uint64, _P(C.c_int64)]),
 }
 

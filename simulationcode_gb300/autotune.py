@@ -1,7 +1,8 @@
 """Autotuner for a loaded ReplicaBatch: the force pass's tile shape (particles
 per work item x threads per particle), the skin (the rebuild cadence: a
-larger skin means longer lists but fewer rebuilds, per replica group) and
-the number of steps per captured CUDA graph.
+larger skin means longer lists but fewer rebuilds, per replica group), the
+inner skin of the force pass's filtered lists (0: no filtering) and the
+number of steps per captured CUDA graph.
 
 Each candidate is timed on the live batch with CUDA events over a short run
 after a short warm-up; the trial steps are ordinary MD steps of the batch
@@ -30,6 +31,7 @@ class TuneResult:
     trials: list
     group_skins: dict = dataclasses.field(default_factory=dict)
     work_item: int = 0
+    inner_skin: float = 0.0
 
 
 def _may_overflow(batch: ReplicaBatch, skin: float, skin_seen: float, margin: float = 1.15) -> bool:
@@ -47,13 +49,15 @@ def _may_overflow(batch: ReplicaBatch, skin: float, skin_seen: float, margin: fl
 
 def autotune(batch: ReplicaBatch, *, tpps: Iterable[int] = (1, 2, 4, 8), skins: Optional[Iterable[float]] = None,
              graph_steps: Iterable[int] = (16,), warmup: int = 32, steps: int = 96, log=None,
-             group_by=None, work_items: Iterable[int] = (0, 64, 32)) -> TuneResult:
+             group_by=None, work_items: Iterable[int] = (0, 64, 32),
+             inner_skins: Iterable[float] = (0.2, 0.3, 0.4)) -> TuneResult:
     """Grid search over (skin, tpp, graph steps); ``skins`` None keeps the
     replicas' configured skin.  A skin whose predicted longest list could
     overflow max_neighbors is skipped (skins are tried in increasing order).
     ``group_by(spec)``: a second pass tunes the skin of each group of
     replicas separately (the rebuild cadence that suits 2D replicas differs
-    from 3D)."""
+    from 3D).  Last, with one thread per particle, the inner skin of the
+    force pass's filtered lists (kept only when it beats no filtering)."""
     base_skin = next(iter(batch.specs.values())).skin if batch.specs else 0.3
     skins = [base_skin] if skins is None else sorted(skins)
     skin_seen = base_skin
@@ -128,8 +132,25 @@ def autotune(batch: ReplicaBatch, *, tpps: Iterable[int] = (1, 2, 4, 8), skins: 
                     batch.set_skin(gbest[0], rid)
                 group_skins[str(key)] = gbest[0]
                 ms = min(ms, gbest[1])
+    # inner skin of the force pass's filtered lists (one thread per particle)
+    inner = 0.0
+    if tpp == 1:
+        inner_ms = ms
+        for si in inner_skins:
+            batch.set_prune(si)
+            batch.step(warmup)
+            batch.timer_start()
+            batch.step(steps)
+            t = batch.timer_stop() / steps
+            trials.append({"tpp": tpp, "skin": skin, "inner_skin": si, "graph_steps": gs, "ms_per_step": t})
+            if log:
+                log("autotune: inner skin %.2f -> %.4f ms/step" % (si, t))
+            if t < inner_ms:
+                inner, inner_ms = si, t
+        batch.set_prune(inner)
+        ms = inner_ms
     return TuneResult(tpp=tpp, skin=skin, graph_steps=gs, ms_per_step=ms, trials=trials, group_skins=group_skins,
-                      work_item=item)
+                      work_item=item, inner_skin=inner)
 
 
 class _Subset:
@@ -175,8 +196,13 @@ def apply_tuned(batch: ReplicaBatch, tuned: dict, graphs: bool = True):
         sk = skin_for(tuned, spec)
         if sk != spec.skin:
             batch.set_skin(sk, rid)
-    batch.set_tuning(int(tuned.get("tpp", 1)), graphs, int(tuned.get("graph_steps", 16)))
+    tpp, inner = int(tuned.get("tpp", 1)), float(tuned.get("inner_skin", 0.0))
+    if batch.inner_skin > 0 and (tpp != 1 or inner == 0):
+        batch.set_prune(0.0)
+    batch.set_tuning(tpp, graphs, int(tuned.get("graph_steps", 16)))
     batch.set_work_item(int(tuned.get("work_item", 0)))
+    if inner > 0:
+        batch.set_prune(inner)
 
 
 def as_tuned(result: TuneResult, batch: ReplicaBatch) -> dict:
@@ -184,5 +210,6 @@ def as_tuned(result: TuneResult, batch: ReplicaBatch) -> dict:
     skins = {}
     for spec in batch.specs.values():
         skins[group_key(spec)] = float(spec.skin)
-    return {"tpp": result.tpp, "graph_steps": result.graph_steps, "skins": skins, "work_item": result.work_item}
+    return {"tpp": result.tpp, "graph_steps": result.graph_steps, "skins": skins, "work_item": result.work_item,
+            "inner_skin": result.inner_skin}
 

@@ -73,6 +73,7 @@ class ReplicaBatch:
         _lib.check(self.lib.simmd_engine_create(device, C.byref(self.ctx)))
         _lib.check(self.lib.simmd_set_tuning(self.ctx, tpp, int(graphs), graph_steps))
         self.specs = {}
+        self.inner_skin = 0.0  # inner skin of the filtered force-pass lists (0: none)
 
     def reserve(self, slots: int, cells: int, replicas: int, max_neighbors: int = 200):
         _lib.check(self.lib.simmd_reserve(self.ctx, slots, cells, replicas, max_neighbors))
@@ -230,18 +231,17 @@ class ReplicaBatch:
     def profile_get(self):
         out = np.zeros(6)
         _lib.check(self.lib.simmd_profile_get(self.ctx, _lib.ptr(out)))
-        pr = C.c_double(0.0)
-        _lib.check(self.lib.simmd_profile_prune_ms(self.ctx, C.byref(pr)))
         return dict(force_ms=out[0], force_n=int(out[1]), kick_ms=out[2], rebuild_ms=out[3], update_ms=out[4],
-                    steps=int(out[5]), prune_ms=pr.value)
+                    steps=int(out[5]))
 
     def set_prune(self, inner_skin: float, rid: int = -1):
         """inner (pruned) lists for the force pass with this inner skin for
         one replica (rid) or all (-1); 0 everywhere turns them off"""
         _lib.check(self.lib.simmd_set_prune(self.ctx, rid, float(inner_skin)))
-        for k, s in self.specs.items():
-            if rid in (-1, k):
-                s.inner_skin = float(inner_skin)
+        if rid == -1:
+            self.inner_skin = float(inner_skin)
+        else:
+            self.inner_skin = max(self.inner_skin, float(inner_skin))
 
     def prune_stats(self, rid: int):
         """(prunes done, inner-list entries at the last prune)"""

@@ -29,7 +29,7 @@ namespace simmd {
 void launch_rebuild_plan_impl(const Batch& b, const LaunchCfg& lc, cudaGraphConditionalHandle cond, int use_cond);
 void launch_rebuild_body_impl(const Batch& b, const LaunchCfg& lc, unsigned* nbr_full, int* ncnt_full, int Kfull);
 void launch_mark_rebuild_impl(const int* reps, int n, RepState* state, cudaStream_t s);
-void launch_prune_impl(const Batch& b, const LaunchCfg& lc);
+void launch_rep_dmax_impl(const Batch& b, const LaunchCfg& lc, const double* D, double* out);
 void launch_export_impl(const Batch& b, const LaunchCfg& lc, int rep, const RepDesc& hd, const unsigned* lst,
                         const int* cnt, int T, long long* counts, long long* list, long long maxK, int half_only,
                         int* overflow);
@@ -89,7 +89,7 @@ struct HostRep {
 };
 
 struct ProfileAcc {
-    double force_ms = 0, kick_ms = 0, rebuild_ms = 0, update_ms = 0, prune_ms = 0;
+    double force_ms = 0, kick_ms = 0, rebuild_ms = 0, update_ms = 0;
     long long force_n = 0, steps = 0;
 };
 
@@ -97,7 +97,7 @@ struct simmd_ctx {
     int device = 0;
     cudaStream_t stream = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-    cudaEvent_t pev[12] = {};
+    cudaEvent_t pev[8] = {};
     int sm_count = 1;
     long long S_cap = 0;
     long long C_cap = 0;
@@ -129,6 +129,7 @@ struct simmd_ctx {
     int2* d_plan_cells = nullptr;
     int* d_plan_cnt = nullptr;
     int* d_mark = nullptr;  // replica ids whose rebuild the host requests
+    double* d_dmax = nullptr;  // per replica max(D) of a batched upload
     bool xfer_dirty = false;  // host descriptors hold transfer offsets the device copies lack
     int prune_on = 0;         // the force pass reads inner (pruned) lists
     std::vector<int> h_tile_rep;
@@ -232,14 +233,14 @@ static int force_rebuild_all(simmd_ctx* c)
 }
 
 // device bytes of the capacity-sized arrays: per slot the state (posD 32,
-// v/F/u 72), the split record 16, cellc/orig/inv/ncnt 16, rebuild scratch
+// v/F/u 72), the fixed-point record and its rebuild-time copy 16 + 16, cellc/orig/inv/ncnt 16, rebuild scratch
 // (bin/rank/src 12, staged posD/v/F/orig 84), per-particle energy 8 and the
 // list 4K; per tile the partial sums, plan and owner; per cell count, start
 // and plan entry; per replica its descriptor and state
-constexpr long long SLOT_BYTES = 32 + 72 + 16 + 16 + 12 + 84 + 8;
+constexpr long long SLOT_BYTES = 32 + 72 + 16 + 16 + 16 + 12 + 84 + 8;
 constexpr long long TILE_BYTES = RED_LEVELS * (RED_REC * 8 + 4) + NPART * 8 * WARP_SLOTS + 4 + 4 + 4;
 constexpr long long CELL_BYTES = 4 + 4 + 8;
-constexpr long long REP_BYTES = sizeof(RepDesc) + sizeof(RepState) + 4;
+constexpr long long REP_BYTES = sizeof(RepDesc) + sizeof(RepState) + 4 + 8;
 
 static long long capacity_bytes(const simmd_ctx* c, long long S, long long C, int R, int K)
 {
@@ -296,6 +297,7 @@ static int ensure_capacity(simmd_ctx* c, long long S_need, long long C_need, int
         TRY(grow_keep(c, &s.uy, S_old, S_new));
         TRY(grow_keep(c, &s.uz, S_old, S_new));
         TRY(grow_keep(c, &s.rec, S_old, S_new));
+        TRY(grow_keep(c, &s.recb, S_old, S_new));
         TRY(grow_keep(c, &s.cellc, S_old, S_new));
         TRY(grow_keep(c, &s.orig, S_old, S_new));
         TRY(grow_keep(c, &s.inv, S_old, S_new));
@@ -372,6 +374,7 @@ static int ensure_capacity(simmd_ctx* c, long long S_need, long long C_need, int
         TRY(grow_keep(c, &c->d_desc, R_old, R_new));
         TRY(grow_keep(c, &c->d_state, R_old, R_new));
         TRY(grow_fresh(c, &c->d_mark, R_old, R_new));
+        TRY(grow_fresh(c, &c->d_dmax, R_old, R_new));
         c->reps.resize(R_new);
         c->h_state.resize(R_new);
         c->R_cap = R_new;
@@ -594,6 +597,14 @@ static int fill_desc_smax(const simmd_params* p, double smax, RepDesc& d)
         d.fix_mul = (unsigned long long)std::ldexp(d.fix_scale, d.fix_sh - 11) << 11;  // 53 significant bits
     }
     d.fix_u = (float)(L / 4294967296.0);
+    d.fix_ud = L / 4294967296.0;
+    {  // split precision's skin trigger in fixed-point units: a fixed-point
+       // displacement |dX| bounds the true one by (|dX| + sqrt(3)) u (each
+       // coordinate rounded to u/2 at both ends), so |dX| <= skin/(2u) -
+       // sqrt(3) keeps it <= skin/2; one unit more of slack
+        const double A = p->skin / (2.0 * d.fix_ud) - std::sqrt(3.0) - 1.0;
+        d.skin_thr = A > 0.0 ? (unsigned long long)std::floor(A * A) : 0ull;
+    }
     d.fix_u2 = (float)((L / 4294967296.0) * (L / 4294967296.0));
     d.zeta_lo = (float)(d.zeta - (double)(float)d.zeta);
     d.rv2f = (float)d.rv2;
@@ -827,27 +838,6 @@ static void rebuild_launch(simmd_ctx* c, const Batch& b, const LaunchCfg& lc)
     fail(cudaStreamUpdateCaptureDependencies(c->stream, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
 }
 
-// the force pass's view of the batch: the inner (pruned) lists when the
-// context keeps them
-static Batch force_batch(const simmd_ctx* c, const Batch& b)
-{
-    Batch f = b;
-    if (c->prune_on) {
-        f.s.nbr = c->s.nbr_in;
-        f.s.ncnt = c->s.ncnt_in;
-    }
-    return f;
-}
-
-static void prune_launch(simmd_ctx* c, const Batch& b, const LaunchCfg& lc, int ev)
-{
-    if (!c->prune_on) return;
-    const bool prof = c->profile != 0;
-    if (prof) cudaEventRecord(c->pev[ev], c->stream);
-    launch_prune_impl(b, lc);
-    if (prof) cudaEventRecord(c->pev[ev + 1], c->stream);
-}
-
 static void enqueue_step(simmd_ctx* c, const Batch& b, const LaunchCfg& lc, const Mix& m, int fmode)
 {
     const bool prof = c->profile != 0;
@@ -857,10 +847,9 @@ static void enqueue_step(simmd_ctx* c, const Batch& b, const LaunchCfg& lc, cons
         if (prof) cudaEventRecord(c->pev[1], c->stream);
         rebuild_launch(c, b, lc);
         if (prof) cudaEventRecord(c->pev[2], c->stream);
-        prune_launch(c, b, lc, 8);
     }
     if (prof) cudaEventRecord(c->pev[3], c->stream);
-    launch_force_impl(force_batch(c, b), lc, fmode, m.prec_mask, nullptr);
+    launch_force_impl(b, lc, fmode, m.prec_mask, nullptr);
     c->n_force += __builtin_popcount(m.prec_mask);
     if (prof) cudaEventRecord(c->pev[4], c->stream);
     if (m.rescale) launch_rescale_impl(b, lc);
@@ -870,7 +859,6 @@ static void enqueue_step(simmd_ctx* c, const Batch& b, const LaunchCfg& lc, cons
         if (prof) cudaEventRecord(c->pev[6], c->stream);
         rebuild_launch(c, b, lc);
         if (prof) cudaEventRecord(c->pev[7], c->stream);
-        prune_launch(c, b, lc, 10);
     }
     if (prof) {
         cudaStreamSynchronize(c->stream);
@@ -880,10 +868,6 @@ static void enqueue_step(simmd_ctx* c, const Batch& b, const LaunchCfg& lc, cons
             c->prof.kick_ms += ms;
             cudaEventElapsedTime(&ms, c->pev[1], c->pev[2]);
             c->prof.rebuild_ms += ms;
-            if (c->prune_on) {
-                cudaEventElapsedTime(&ms, c->pev[8], c->pev[9]);
-                c->prof.prune_ms += ms;
-            }
         }
         cudaEventElapsedTime(&ms, c->pev[3], c->pev[4]);
         c->prof.force_ms += ms;
@@ -893,10 +877,6 @@ static void enqueue_step(simmd_ctx* c, const Batch& b, const LaunchCfg& lc, cons
             c->prof.update_ms += ms;
             cudaEventElapsedTime(&ms, c->pev[6], c->pev[7]);
             c->prof.rebuild_ms += ms;
-            if (c->prune_on) {
-                cudaEventElapsedTime(&ms, c->pev[10], c->pev[11]);
-                c->prof.prune_ms += ms;
-            }
         }
         c->prof.steps += 1;
     }
@@ -905,7 +885,8 @@ static void enqueue_step(simmd_ctx* c, const Batch& b, const LaunchCfg& lc, cons
 // the host's rebuild and prune requests (a new or re-uploaded replica, a
 // skin change, simmd_rebuild, positions set by the host): one copy of the
 // replica ids and one marking kernel, then the rebuild sequence, which works
-// only on the marked replicas, and the prune
+// only on the marked replicas (a requested prune is done by the next force
+// pass)
 static int pending_rebuilds(simmd_ctx* c)
 {
     std::vector<int> ids;
@@ -923,14 +904,10 @@ static int pending_rebuilds(simmd_ctx* c)
         CK(cudaMemcpyAsync(c->d_mark, ids.data(), sizeof(int) * ids.size(), cudaMemcpyHostToDevice, c->stream));
         launch_mark_rebuild_impl(c->d_mark, (int)ids.size(), c->d_state, c->stream);
     }
-    if (any || c->prune_on) {
+    if (any) {
         Batch b = make_batch(c);
         LaunchCfg lc = make_lc(c, FMODE_STEP);
-        if (any) rebuild_launch(c, b, lc);
-        // inner lists before the next force pass: requested prunes (a
-        // rebuild, positions set by the host) and displacements since the
-        // last prune by other movers (minimiser)
-        if (c->prune_on) launch_prune_impl(b, lc);
+        rebuild_launch(c, b, lc);
         CK(cudaGetLastError());
     }
     return SIMMD_OK;
@@ -1082,12 +1059,12 @@ static int push_all_desc(simmd_ctx* c, std::vector<RepDesc>& staging)
 
 // a replica's descriptor from its (new) diameters: the Verlet radius and
 // the cell grid follow max(D); slots, tiles and transfer offsets stay
-static int refresh_desc(simmd_ctx* c, int rep, const double* D)
+static int refresh_desc_smax(simmd_ctx* c, int rep, double smax)
 {
     HostRep& h = c->reps[rep];
     RepDesc d;
-    TRY(fill_desc(&h.p, D, d));
-    h.smax = max_diameter(D, h.p.N);
+    TRY(fill_desc_smax(&h.p, smax, d));
+    h.smax = smax;
     if (d.ncell != h.d.ncell) {
         give_range(c->free_cells, h.d.cell0, h.d.ncell + 1);
         long long cstart;
@@ -1106,6 +1083,11 @@ static int refresh_desc(simmd_ctx* c, int rep, const double* D)
     h.d = d;
     apply_prune_desc(c, h);
     return SIMMD_OK;
+}
+
+static int refresh_desc(simmd_ctx* c, int rep, const double* D)
+{
+    return refresh_desc_smax(c, rep, max_diameter(D, c->reps[rep].p.N));
 }
 
 // ---------------------------------------------------------------------------
@@ -1197,7 +1179,7 @@ static void destroy_ctx(simmd_ctx* c)
                     s.ncnt, s.bin_cell, s.bin_rank, s.src, s.t_posD, s.t_vx, s.t_vy, s.t_vz, s.t_fx, s.t_fy,
                     s.t_fz, s.t_orig, s.cell_count, s.cell_start, c->nbr_full, c->ncnt_full, c->epp, c->d_desc,
                     c->d_state, c->d_tile_rep, c->d_red_val, c->d_red_cnt, c->d_warp_part, c->d_tile_cnt, c->d_queue, c->d_stage, c->d_dump, c->d_noise,
-                    c->d_plan_tiles, c->d_plan_cells, c->d_plan_cnt, c->d_mark, s.nbr_in, s.ncnt_in, s.recp};
+                    c->d_plan_tiles, c->d_plan_cells, c->d_plan_cnt, c->d_mark, c->d_dmax, s.nbr_in, s.ncnt_in, s.recp, s.recb};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (c->dump_stream) cudaStreamSynchronize(c->dump_stream);
@@ -1395,20 +1377,38 @@ int simmd_upload_all(simmd_ctx* c, const double* r, const double* v, const doubl
     long long nv = 0, ns = 0;
     xfer_layout(c, &nv, &ns);
     if (nv == 0) return set_err(SIMMD_ERR_NOT_FOUND, "no replica");
-    for (int rep = 0; rep < c->R_cap; rep++) {
-        if (!c->reps[rep].active) continue;
-        TRY(refresh_desc(c, rep, D + c->reps[rep].d.xfer_soff));
-        c->reps[rep].pending_rebuild = true;
-    }
     std::vector<RepDesc> dstage;
-    TRY(push_all_desc(c, dstage));
-    // every replica's state as reset_state(keep_counters) leaves it, in one
-    // round trip
+    if (c->xfer_dirty) TRY(push_all_desc(c, dstage));  // the transfer offsets, read by the kernels below
+    TRY(ensure_stage(c, nv));
+    double* stg = c->d_stage;
+    double *dr = stg, *dv = stg + c->stage_cap, *dF = stg + 2 * c->stage_cap, *dD = stg + 3 * c->stage_cap,
+           *du = stg + 4 * c->stage_cap;
+    CK(cudaMemcpyAsync(dr, r, sizeof(double) * nv, cudaMemcpyHostToDevice, c->stream));
+    if (v) CK(cudaMemcpyAsync(dv, v, sizeof(double) * nv, cudaMemcpyHostToDevice, c->stream));
+    if (F) CK(cudaMemcpyAsync(dF, F, sizeof(double) * nv, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(dD, D, sizeof(double) * ns, cudaMemcpyHostToDevice, c->stream));
+    if (disp) CK(cudaMemcpyAsync(du, disp, sizeof(double) * nv, cudaMemcpyHostToDevice, c->stream));
+    // max(D) per replica on the device (it sets the Verlet radius and the
+    // cell grid), with every replica's state, in one round trip
+    {
+        Batch b = make_batch(c);
+        LaunchCfg lc = make_lc(c, FMODE_STEP);
+        launch_rep_dmax_impl(b, lc, dD, c->d_dmax);
+        CK(cudaGetLastError());
+    }
+    std::vector<double> smax((size_t)c->R_cap, 0.0);
+    CK(cudaMemcpyAsync(smax.data(), c->d_dmax, sizeof(double) * (size_t)c->R_cap, cudaMemcpyDeviceToHost,
+                       c->stream));
     CK(cudaMemcpyAsync(c->h_state.data(), c->d_state, sizeof(RepState) * (size_t)c->R_cap, cudaMemcpyDeviceToHost,
                        c->stream));
     CK(cudaStreamSynchronize(c->stream));
     for (int rep = 0; rep < c->R_cap; rep++) {
         if (!c->reps[rep].active) continue;
+        // a new descriptor only when max(D) changed (a re-upload of the same
+        // diameters keeps it)
+        if (smax[(size_t)rep] != c->reps[rep].smax) TRY(refresh_desc_smax(c, rep, smax[(size_t)rep]));
+        c->reps[rep].pending_rebuild = true;  // the rebuild runs before the next force pass
+        // the state as reset_state(keep_counters) leaves it
         RepState& st = c->h_state[(size_t)rep];
         const long long step = st.step, rb = st.rebuilds;
         const int mc = st.maxcount;
@@ -1420,17 +1420,9 @@ int simmd_upload_all(simmd_ctx* c, const double* r, const double* v, const doubl
         st.force_rebuild = 1;
         st.force_prune = 1;
     }
+    TRY(push_all_desc(c, dstage));
     CK(cudaMemcpyAsync(c->d_state, c->h_state.data(), sizeof(RepState) * (size_t)c->R_cap, cudaMemcpyHostToDevice,
                        c->stream));
-    TRY(ensure_stage(c, nv));
-    double* stg = c->d_stage;
-    double *dr = stg, *dv = stg + c->stage_cap, *dF = stg + 2 * c->stage_cap, *dD = stg + 3 * c->stage_cap,
-           *du = stg + 4 * c->stage_cap;
-    CK(cudaMemcpyAsync(dr, r, sizeof(double) * nv, cudaMemcpyHostToDevice, c->stream));
-    if (v) CK(cudaMemcpyAsync(dv, v, sizeof(double) * nv, cudaMemcpyHostToDevice, c->stream));
-    if (F) CK(cudaMemcpyAsync(dF, F, sizeof(double) * nv, cudaMemcpyHostToDevice, c->stream));
-    CK(cudaMemcpyAsync(dD, D, sizeof(double) * ns, cudaMemcpyHostToDevice, c->stream));
-    if (disp) CK(cudaMemcpyAsync(du, disp, sizeof(double) * nv, cudaMemcpyHostToDevice, c->stream));
     Batch b = make_batch(c);
     LaunchCfg lc = make_lc(c, FMODE_STEP);
     launch_load_all(b, lc, dr, v ? dv : nullptr, F ? dF : nullptr, dD, disp ? du : nullptr);
@@ -1694,6 +1686,8 @@ int simmd_set_tuning(simmd_ctx* c, int32_t tpp, int32_t use_graphs, int32_t grap
 {
     if (!c) return set_err(SIMMD_ERR_BAD_ARG, "NULL context");
     if (tpp != 1 && tpp != 2 && tpp != 4 && tpp != 8) return set_err(SIMMD_ERR_BAD_ARG, "tpp must be 1, 2, 4 or 8");
+    if (tpp != 1 && c->prune_on)
+        return set_err(SIMMD_ERR_BAD_ARG, "inner lists need one thread per particle (tpp = 1): simmd_set_prune 0 first");
     CK(cudaSetDevice(c->device));
     if (tpp != c->T) {
         CK(cudaStreamSynchronize(c->stream));
@@ -1892,6 +1886,10 @@ int simmd_relax(simmd_ctx* c, int64_t nsteps, double step_size, double max_disp)
 {
     if (!c || nsteps < 0 || !(max_disp > 0) || !(step_size > 0)) return set_err(SIMMD_ERR_BAD_ARG, "bad argument");
     CK(cudaSetDevice(c->device));
+    // split replicas keep no FP64 displacement: rebuilt first, so the FP64
+    // relaxation starts from a zero displacement
+    for (int r = 0; r < c->R_cap; r++)
+        if (c->reps[r].active && c->reps[r].d.prec == PREC_FP32) c->reps[r].pending_rebuild = true;
     TRY(pending_rebuilds(c));
     std::vector<RepDesc> saved;
     for (int r = 0; r < c->R_cap; r++) {
@@ -2065,6 +2063,7 @@ int simmd_set_prune(simmd_ctx* c, int32_t rep, double inner_skin)
     int on = 0;
     for (const auto& h : c->reps)
         if (h.active && h.inner_skin > 0.0) on = 1;
+    if (on && c->T != 1) return set_err(SIMMD_ERR_BAD_ARG, "inner lists need one thread per particle (tpp = 1)");
     if (on && !c->prune_on) {
         // the inner list, its counts and the prune-time records; every
         // replica rebuilt (its record refreshed) and pruned before the next
@@ -2143,13 +2142,6 @@ int simmd_profile_get(simmd_ctx* c, double* out6)
     out6[3] = c->prof.rebuild_ms;
     out6[4] = c->prof.update_ms;
     out6[5] = (double)c->prof.steps;
-    return SIMMD_OK;
-}
-
-int simmd_profile_prune_ms(simmd_ctx* c, double* ms)
-{
-    if (!c || !ms) return set_err(SIMMD_ERR_BAD_ARG, "NULL argument");
-    *ms = c->prof.prune_ms;
     return SIMMD_OK;
 }
 

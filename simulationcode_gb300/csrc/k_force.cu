@@ -37,10 +37,18 @@ namespace simmd {
 // ---------------------------------------------------------------------------
 // FP64 pair (reference arithmetic)
 // ---------------------------------------------------------------------------
+// the inner-list test of a pair (the force pass prunes while it sums):
+// |r| <= r_cut (1 + 1e-4) s + inner skin, s the pair diameter (LJ: 1)
+__device__ __forceinline__ bool prune_keep(const RepDesc& d, float r2, float s)
+{
+    const float tt = fmaf(d.prune_rcut_f, s, d.prune_skin_f);
+    return r2 <= tt * tt;
+}
+
 template <int DIM, int POT, bool EN>
 __device__ __forceinline__ void pair_f64(const RepDesc& d, long long halfLb, const double4_32a& pi,
                                          const double4_32a& pj, double& fx, double& fy, double& fz, double& e,
-                                         double& w)
+                                         double& w, double& r2o, double& so)
 {
     const double L = d.L, rc2 = d.rc2;
     const double dx = min_image_f64(dsub(pi.x, pj.x), halfLb, L);
@@ -53,8 +61,11 @@ __device__ __forceinline__ void pair_f64(const RepDesc& d, long long halfLb, con
         r2 = dadd(dmul(dx, dx), dmul(dy, dy));
     }
     double Fr = 0.0, V = 0.0;
+    r2o = r2;
+    so = 1.0;
     if (POT == POT_BERTHIER) {
         const double md = dmul(dmul(dadd(pi.w, pj.w), 0.5), dsub(1.0, dmul(d.zeta, fabs(dsub(pi.w, pj.w)))));
+        so = md;
         const double mds = dmul(md, md);
         const bool out = dmul(rc2, mds) < r2;
         const double inv = drcp(mds);
@@ -100,26 +111,34 @@ __device__ __forceinline__ void pair_f64(const RepDesc& d, long long halfLb, con
     }
 }
 
-template <int DIM, int POT, bool EN, int T>
+// PR: the pass also writes the inner list of the pairs prune_keep accepts
+// (in list order; one thread per particle)
+template <int DIM, int POT, bool EN, int T, bool PR>
 __device__ __forceinline__ void pairs_f64(const Batch& b, const RepDesc& d, long long i, int sub,
-                                          const double4_32a pi, int cnt, double& fx, double& fy, double& fz,
-                                          double& e, double& w)
+                                          const double4_32a pi, const unsigned* __restrict__ nbr, int cnt,
+                                          double& fx, double& fy, double& fz, double& e, double& w, int& m)
 {
     const long long halfLb = __double_as_longlong(d.halfL);
-    const unsigned* __restrict__ nbr = b.s.nbr;
     const double4_32a* __restrict__ posD = b.s.posD;
+    double r2, sd;
+    auto keep = [&](unsigned j) {
+        if (PR && prune_keep(d, (float)r2, (float)sd)) b.s.nbr_in[nbr_addr(m++, i, 1, b.K)] = j;
+    };
     int n = sub;
     for (; n + T < cnt; n += 2 * T) {
         const unsigned j0 = __ldg(nbr + nbr_addr(n, i, T, b.K)) & IDX_MASK;
         const unsigned j1 = __ldg(nbr + nbr_addr(n + T, i, T, b.K)) & IDX_MASK;
         const double4_32a p0 = posD[j0];
         const double4_32a p1 = posD[j1];
-        pair_f64<DIM, POT, EN>(d, halfLb, pi, p0, fx, fy, fz, e, w);
-        pair_f64<DIM, POT, EN>(d, halfLb, pi, p1, fx, fy, fz, e, w);
+        pair_f64<DIM, POT, EN>(d, halfLb, pi, p0, fx, fy, fz, e, w, r2, sd);
+        keep(j0);
+        pair_f64<DIM, POT, EN>(d, halfLb, pi, p1, fx, fy, fz, e, w, r2, sd);
+        keep(j1);
     }
     if (n < cnt) {
         const unsigned j0 = __ldg(nbr + nbr_addr(n, i, T, b.K)) & IDX_MASK;
-        pair_f64<DIM, POT, EN>(d, halfLb, pi, posD[j0], fx, fy, fz, e, w);
+        pair_f64<DIM, POT, EN>(d, halfLb, pi, posD[j0], fx, fy, fz, e, w, r2, sd);
+        keep(j0);
     }
 }
 
@@ -136,6 +155,7 @@ __device__ __forceinline__ void pairs_f64(const Batch& b, const RepDesc& d, long
 // otherwise amplify the ~5 roundings of s^2 into most of the FP32 error.
 struct PairS2 {
     float q, eq;  // s^2 = q + eq
+    float s;      // s (rounded): the inner-list test
 };
 
 __device__ __forceinline__ PairS2 pair_s2_comp(float Di, float Dj, const RepDesc& d)
@@ -153,6 +173,7 @@ __device__ __forceinline__ PairS2 pair_s2_comp(float Di, float Dj, const RepDesc
     m *= 0.5f;
     em *= 0.5f;
     PairS2 r;
+    r.s = m;
     r.q = m * m;
     r.eq = fmaf(m, m, -r.q) + 2.0f * m * em;
     return r;
@@ -160,16 +181,19 @@ __device__ __forceinline__ PairS2 pair_s2_comp(float Di, float Dj, const RepDesc
 
 template <int DIM, int POT, bool EN>
 __device__ __forceinline__ void pair_f32(const RepDesc& d, const FixRec& pi, const FixRec& pj, float& fx, float& fy,
-                                         float& fz, float& e, float& w)
+                                         float& fz, float& e, float& w, float& r2o, float& so)
 {
     const int ix = (int)(pi.x - pj.x), iy = (int)(pi.y - pj.y), iz = DIM == 3 ? (int)(pi.z - pj.z) : 0;
     unsigned long long r2i = (unsigned long long)((long long)ix * ix) + (unsigned long long)((long long)iy * iy);
     if (DIM == 3) r2i += (unsigned long long)((long long)iz * iz);
     const float r2 = __ull2float_rn(r2i) * d.fix_u2;
+    r2o = r2;
+    so = 1.0f;
     const float dx = (float)ix * d.fix_u, dy = (float)iy * d.fix_u, dz = DIM == 3 ? (float)iz * d.fix_u : 0.0f;
     float Fr = 0.0f, V = 0.0f;
     if (POT == POT_BERTHIER) {
         const PairS2 s2 = pair_s2_comp(pi.d, pj.d, d);
+        so = s2.s;
         const float inv = __fdividef(1.0f, s2.q);
         float x = r2 * inv;
         x = fmaf(fmaf(-x, s2.q, r2) - x * s2.eq, inv, x);  // x = r^2 / (q + eq), first order
@@ -201,12 +225,12 @@ __device__ __forceinline__ void pair_f32(const RepDesc& d, const FixRec& pi, con
 // list entry n of the particle: from the tile's rows staged in shared memory
 // (rows < nrows), else from global memory
 template <int T>
-__device__ __forceinline__ unsigned list_entry(const Batch& b, const unsigned* s_rows, int nrows, long long i, int pl,
-                                               int ppb, int n)
+__device__ __forceinline__ unsigned list_entry(const Batch& b, const unsigned* __restrict__ lst,
+                                               const unsigned* s_rows, int nrows, long long i, int pl, int ppb, int n)
 {
     const int row = n / T;
     if (row < nrows) return s_rows[row * (ppb * T) + pl * T + (n % T)] & IDX_MASK;
-    return __ldg(b.s.nbr + nbr_addr(n, i, T, b.K)) & IDX_MASK;
+    return __ldg(lst + nbr_addr(n, i, T, b.K)) & IDX_MASK;
 }
 
 // neighbour records gathered PAIR_UNROLL at a time (all loads issued before
@@ -216,26 +240,34 @@ __device__ __forceinline__ unsigned list_entry(const Batch& b, const unsigned* s
 #endif
 constexpr int PAIR_UNROLL = SIMMD_PAIR_UNROLL;
 
-template <int DIM, int POT, bool EN, int T>
+// PR: the pass also writes the inner list of the pairs prune_keep accepts
+// (in list order; one thread per particle)
+template <int DIM, int POT, bool EN, int T, bool PR>
 __device__ __forceinline__ void pairs_f32(const Batch& b, const RepDesc& d, long long i, int sub,
-                                          const FixRec ri, int cnt, float& fx, float& fy, float& fz, float& e,
-                                          float& w, const unsigned* s_rows, int nrows, int pl, int ppb)
+                                          const FixRec ri, const unsigned* __restrict__ lst, int cnt, float& fx,
+                                          float& fy, float& fz, float& e, float& w, const unsigned* s_rows,
+                                          int nrows, int pl, int ppb, int& m)
 {
     const FixRec* __restrict__ rec = b.s.rec;
+    float r2, sd;
     int n = sub;
     for (; n + (PAIR_UNROLL - 1) * T < cnt; n += PAIR_UNROLL * T) {
         unsigned j[PAIR_UNROLL];
         FixRec o[PAIR_UNROLL];
 #pragma unroll
-        for (int u = 0; u < PAIR_UNROLL; u++) j[u] = list_entry<T>(b, s_rows, nrows, i, pl, ppb, n + u * T);
+        for (int u = 0; u < PAIR_UNROLL; u++) j[u] = list_entry<T>(b, lst, s_rows, nrows, i, pl, ppb, n + u * T);
 #pragma unroll
         for (int u = 0; u < PAIR_UNROLL; u++) o[u] = rec_get(rec + j[u]);
 #pragma unroll
-        for (int u = 0; u < PAIR_UNROLL; u++) pair_f32<DIM, POT, EN>(d, ri, o[u], fx, fy, fz, e, w);
+        for (int u = 0; u < PAIR_UNROLL; u++) {
+            pair_f32<DIM, POT, EN>(d, ri, o[u], fx, fy, fz, e, w, r2, sd);
+            if (PR && prune_keep(d, r2, sd)) b.s.nbr_in[nbr_addr(m++, i, 1, b.K)] = j[u];
+        }
     }
     for (; n < cnt; n += T) {
-        const unsigned j0 = list_entry<T>(b, s_rows, nrows, i, pl, ppb, n);
-        pair_f32<DIM, POT, EN>(d, ri, rec_get(rec + j0), fx, fy, fz, e, w);
+        const unsigned j0 = list_entry<T>(b, lst, s_rows, nrows, i, pl, ppb, n);
+        pair_f32<DIM, POT, EN>(d, ri, rec_get(rec + j0), fx, fy, fz, e, w, r2, sd);
+        if (PR && prune_keep(d, r2, sd)) b.s.nbr_in[nbr_addr(m++, i, 1, b.K)] = j0;
     }
 }
 
@@ -281,25 +313,26 @@ __device__ __forceinline__ void particle_noise(const RepDesc& d, RepState& st, i
     }
 }
 
-template <int DIM, bool EN, int T>
-__device__ __forceinline__ void particle_pairs_f64(const Batch& b, const RepDesc& d, long long i, int sub, double& fx,
-                                                   double& fy, double& fz, double& e, double& w)
+template <int DIM, bool EN, int T, bool PR>
+__device__ __forceinline__ void particle_pairs_f64(const Batch& b, const RepDesc& d, long long i, int sub,
+                                                   const unsigned* lst, int cnt, double& fx, double& fy, double& fz,
+                                                   double& e, double& w, int& m)
 {
-    const int cnt = b.s.ncnt[i];
     const double4_32a pi = b.s.posD[i];
-    if (d.pot == POT_BERTHIER) pairs_f64<DIM, POT_BERTHIER, EN, T>(b, d, i, sub, pi, cnt, fx, fy, fz, e, w);
-    else pairs_f64<DIM, POT_LJ, EN, T>(b, d, i, sub, pi, cnt, fx, fy, fz, e, w);
+    if (d.pot == POT_BERTHIER) pairs_f64<DIM, POT_BERTHIER, EN, T, PR>(b, d, i, sub, pi, lst, cnt, fx, fy, fz, e, w, m);
+    else pairs_f64<DIM, POT_LJ, EN, T, PR>(b, d, i, sub, pi, lst, cnt, fx, fy, fz, e, w, m);
 }
 
-template <int DIM, bool EN, int T>
-__device__ __forceinline__ void particle_pairs_f32(const Batch& b, const RepDesc& d, long long i, int sub, int cnt,
-                                                   float& fx, float& fy, float& fz, float& e, float& w,
-                                                   const unsigned* s_rows, int nrows, int pl, int ppb)
+template <int DIM, bool EN, int T, bool PR>
+__device__ __forceinline__ void particle_pairs_f32(const Batch& b, const RepDesc& d, long long i, int sub,
+                                                   const FixRec ri, const unsigned* lst, int cnt, float& fx,
+                                                   float& fy, float& fz, float& e, float& w, const unsigned* s_rows,
+                                                   int nrows, int pl, int ppb, int& m)
 {
-    const FixRec ri = rec_get(b.s.rec + i);
     if (d.pot == POT_BERTHIER)
-        pairs_f32<DIM, POT_BERTHIER, EN, T>(b, d, i, sub, ri, cnt, fx, fy, fz, e, w, s_rows, nrows, pl, ppb);
-    else pairs_f32<DIM, POT_LJ, EN, T>(b, d, i, sub, ri, cnt, fx, fy, fz, e, w, s_rows, nrows, pl, ppb);
+        pairs_f32<DIM, POT_BERTHIER, EN, T, PR>(b, d, i, sub, ri, lst, cnt, fx, fy, fz, e, w, s_rows, nrows, pl, ppb,
+                                                m);
+    else pairs_f32<DIM, POT_LJ, EN, T, PR>(b, d, i, sub, ri, lst, cnt, fx, fy, fz, e, w, s_rows, nrows, pl, ppb, m);
 }
 
 // rows of the tile's list staged in shared memory (16-byte loads, all rows
@@ -312,12 +345,13 @@ constexpr int STAGE_WORDS = SIMMD_STAGE_WORDS;  // list entries staged per block
 // A block covers the ppb particles of one part of a tile; each staged row
 // holds their ppb*T entries (one contiguous run of the tile-major row).
 template <int T>
-__device__ __forceinline__ int stage_rows(const Batch& b, int t, int part, int ppb, int maxcnt, unsigned* s_rows)
+__device__ __forceinline__ int stage_rows(const Batch& b, const unsigned* lst, int t, int part, int ppb, int maxcnt,
+                                          unsigned* s_rows)
 {
     const int row_words = ppb * T, vpr = row_words / 4;
     const int vsh = 31 - __clz(vpr);  // ppb and T are powers of two
     const int nrows = min((maxcnt + T - 1) / T, STAGE_WORDS / row_words);
-    const uint4* src = reinterpret_cast<const uint4*>(b.s.nbr + (size_t)t * ((size_t)TILE * (size_t)b.K) +
+    const uint4* src = reinterpret_cast<const uint4*>(lst + (size_t)t * ((size_t)TILE * (size_t)b.K) +
                                                       (size_t)part * row_words);
     uint4* dst = reinterpret_cast<uint4*>(s_rows);
     for (int v = threadIdx.x; v < nrows * vpr; v += blockDim.x) {
@@ -344,9 +378,30 @@ __device__ __forceinline__ void combine_lanes(R& fx, R& fy, R& fz, R& e, R& w)
 
 // last tile of a replica: the replica totals -> COM velocity / mean force,
 // energy and virial, noise counter
-template <int MODE, int NV>
-__device__ __forceinline__ void finish_replica(const RepDesc& d, RepState& st, const double (&out)[NV], bool noise)
+// the replica's inner-list size, one atomic per warp; before the tile
+// reduction, whose fence orders it before the replica's last tile reads it
+__device__ __forceinline__ void count_inner(RepState& st, int m)
 {
+    unsigned long long sum = (unsigned long long)m;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+    if ((threadIdx.x & 31) == 0 && sum) {
+        atomicAdd(&st.entries_in_acc, sum);
+        __threadfence();
+    }
+}
+
+template <int MODE, int NV>
+__device__ __forceinline__ void finish_replica(const RepDesc& d, RepState& st, const double (&out)[NV], bool noise,
+                                               bool pruned)
+{
+    if (pruned) {  // every tile of the replica wrote its inner list in this pass
+        st.maxdisp_in = 0ull;
+        st.force_prune = 0;
+        st.prunes += 1;
+        st.list_entries_in = (long long)st.entries_in_acc;
+        st.entries_in_acc = 0ull;
+    }
     constexpr bool EN = (MODE == FMODE_ENERGY || MODE == FMODE_STEP_ENERGY);
     constexpr bool STEP = (MODE == FMODE_STEP || MODE == FMODE_STEP_ENERGY);
     const double nd = (double)d.n;
@@ -417,6 +472,13 @@ __global__ void __launch_bounds__(TILE * T, force_min_blocks<PREC, T>()) k_force
         const bool real = i < d.slot0 + d.n;
         const bool noise = d.dyn != DYN_NEWTONIAN && MODE != FMODE_ENERGY && d.relax_cap == 0.0;
         const bool nl = d.dyn != DYN_BROWNIAN;
+        // the list of this pass: the inner list when the context keeps one
+        // and it is valid; the outer list when a prune is due, the pass then
+        // writing the inner list (one thread per particle)
+        const bool prn = T == 1 && need_prune(st, d);
+        const bool inner = d.prune && !prn;
+        const unsigned* lst = inner ? b.s.nbr_in : b.s.nbr;
+        int m = 0;
         double pv[NV];
 #pragma unroll
         for (int k = 0; k < NV; k++) pv[k] = 0.0;
@@ -426,17 +488,31 @@ __global__ void __launch_bounds__(TILE * T, force_min_blocks<PREC, T>()) k_force
             // ---- split precision: everything per particle in FP32 except the
             // FP64 state updates (force store, velocity kick)
             float fx = 0.f, fy = 0.f, fz = 0.f, e = 0.f, w = 0.f;
-            const int cnt = real ? b.s.ncnt[i] : 0;
+            const int cnt = real ? (inner ? b.s.ncnt_in[i] : b.s.ncnt[i]) : 0;
             if (tid == 0) s_maxcnt = 0;
             __syncthreads();
             if (sub == 0 && cnt > 0) atomicMax(&s_maxcnt, cnt);
             __syncthreads();
-            const int nrows = stage_rows<T>(b, t, part, ppb, s_maxcnt, s_rows);
+            const int nrows = stage_rows<T>(b, lst, t, part, ppb, s_maxcnt, s_rows);
             __syncthreads();
             if (real) {
-                if (d.dims == 3)
-                    particle_pairs_f32<3, EN, T>(b, d, i, sub, cnt, fx, fy, fz, e, w, s_rows, nrows, pl, ppb);
-                else particle_pairs_f32<2, EN, T>(b, d, i, sub, cnt, fx, fy, fz, e, w, s_rows, nrows, pl, ppb);
+                const FixRec ri = rec_get(b.s.rec + i);
+                if (prn) {
+                    if (d.dims == 3)
+                        particle_pairs_f32<3, EN, T, true>(b, d, i, sub, ri, lst, cnt, fx, fy, fz, e, w, s_rows, nrows,
+                                                           pl, ppb, m);
+                    else
+                        particle_pairs_f32<2, EN, T, true>(b, d, i, sub, ri, lst, cnt, fx, fy, fz, e, w, s_rows, nrows,
+                                                           pl, ppb, m);
+                    b.s.ncnt_in[i] = m;
+                    b.s.recp[i] = ri;
+                } else if (d.dims == 3) {
+                    particle_pairs_f32<3, EN, T, false>(b, d, i, sub, ri, lst, cnt, fx, fy, fz, e, w, s_rows, nrows,
+                                                        pl, ppb, m);
+                } else {
+                    particle_pairs_f32<2, EN, T, false>(b, d, i, sub, ri, lst, cnt, fx, fy, fz, e, w, s_rows, nrows,
+                                                        pl, ppb, m);
+                }
             }
             if (T > 1) combine_lanes<float, T, EN>(fx, fy, fz, e, w);
             float q0 = 0.f, q1 = 0.f, q2 = 0.f;  // per-particle contribution to the replica sums
@@ -521,13 +597,23 @@ __global__ void __launch_bounds__(TILE * T, force_min_blocks<PREC, T>()) k_force
                 pv[NV - 2] = de;
                 pv[NV - 1] = dw;
             }
+            if (prn) count_inner(st, m);
             last = tile_reduce<NV, true>(b, item, d, st, pv, out, s_part, &s_flag, parts);
         } else {
             // ---- FP64: the reference's arithmetic
             double fx = 0.0, fy = 0.0, fz = 0.0, e = 0.0, w = 0.0;
             if (real) {
-                if (d.dims == 3) particle_pairs_f64<3, EN, T>(b, d, i, sub, fx, fy, fz, e, w);
-                else particle_pairs_f64<2, EN, T>(b, d, i, sub, fx, fy, fz, e, w);
+                const int cnt = inner ? b.s.ncnt_in[i] : b.s.ncnt[i];
+                if (prn) {
+                    if (d.dims == 3) particle_pairs_f64<3, EN, T, true>(b, d, i, sub, lst, cnt, fx, fy, fz, e, w, m);
+                    else particle_pairs_f64<2, EN, T, true>(b, d, i, sub, lst, cnt, fx, fy, fz, e, w, m);
+                    b.s.ncnt_in[i] = m;
+                    b.s.recp[i] = b.s.rec[i];
+                } else if (d.dims == 3) {
+                    particle_pairs_f64<3, EN, T, false>(b, d, i, sub, lst, cnt, fx, fy, fz, e, w, m);
+                } else {
+                    particle_pairs_f64<2, EN, T, false>(b, d, i, sub, lst, cnt, fx, fy, fz, e, w, m);
+                }
             }
             if (T > 1) combine_lanes<double, T, EN>(fx, fy, fz, e, w);
             if (sub == 0 && real) {
@@ -578,9 +664,10 @@ __global__ void __launch_bounds__(TILE * T, force_min_blocks<PREC, T>()) k_force
                     }
                 }
             }
+            if (prn) count_inner(st, m);
             last = tile_reduce<NV>(b, item, d, st, pv, out, s_part, &s_flag, parts);
         }
-        if (last && tid == 0) finish_replica<MODE, NV>(d, st, out, noise);
+        if (last && tid == 0) finish_replica<MODE, NV>(d, st, out, noise, prn);
     }
     if (tid == 0) {
         __threadfence();

@@ -38,26 +38,31 @@ __device__ __forceinline__ double half_kick(double v, double F, const RepDesc& d
     return dadd(v, ddiv(dmul(d.dt, F), d.two_m));
 }
 
-// r += dr with the reference wrap rnew - floor(rnew/L)*L, displacement update,
-// fixed-point record refresh; returns |disp|^2, and in d2in the fixed-point
-// |X - X_prune|^2 when the context keeps inner lists
-__device__ __forceinline__ double drift_slot(const Batch& b, const RepDesc& d, long long i, double drx,
-                                             double dry, double drz, unsigned long long& d2in)
+// r += dr with the reference wrap rnew - floor(rnew/L)*L, displacement,
+// fixed-point record refresh.  Returns the skin-trigger key: FP64 replicas
+// the bits of |disp|^2 (the reference's accumulated displacement, its
+// rounding); split-precision replicas the fixed-point |X - X_rebuild|^2,
+// exact, with no FP64 displacement arithmetic.  d2in: the fixed-point
+// |X - X_prune|^2 when the context keeps inner lists; bad: a non-finite
+// position or displacement
+__device__ __forceinline__ unsigned long long drift_slot(const Batch& b, const RepDesc& d, long long i, double drx,
+                                                         double dry, double drz, unsigned long long& d2in,
+                                                         bool& bad)
 {
     const Slots& S = b.s;
-    double ux = dadd(S.ux[i], drx), uy = dadd(S.uy[i], dry), uz = 0.0;
-    S.ux[i] = ux;
-    S.uy[i] = uy;
-    if (d.dims == 3) {
-        uz = dadd(S.uz[i], drz);
-        S.uz[i] = uz;
-    }
-    double u2;
+    unsigned long long key = 0ull;
     if (d.prec == PREC_FP64) {  // the reference's rounding of sum(abs2, disp)
-        u2 = dadd(dmul(ux, ux), dmul(uy, uy));
-        if (d.dims == 3) u2 = dadd(u2, dmul(uz, uz));
-    } else {  // split precision: fused (FP64 throughout, two fewer FP64 operations)
-        u2 = (d.dims == 3) ? __fma_rn(ux, ux, __fma_rn(uy, uy, dmul(uz, uz))) : __fma_rn(ux, ux, dmul(uy, uy));
+        double ux = dadd(S.ux[i], drx), uy = dadd(S.uy[i], dry), uz = 0.0;
+        S.ux[i] = ux;
+        S.uy[i] = uy;
+        double u2 = dadd(dmul(ux, ux), dmul(uy, uy));
+        if (d.dims == 3) {
+            uz = dadd(S.uz[i], drz);
+            S.uz[i] = uz;
+            u2 = dadd(u2, dmul(uz, uz));
+        }
+        key = (unsigned long long)__double_as_longlong(u2);
+        bad = nonfinite_bits(u2);
     }
     double4_32a p = S.posD[i];
     const double x = wrap_coord(dadd(p.x, drx), d);
@@ -70,21 +75,24 @@ __device__ __forceinline__ double drift_slot(const Batch& b, const RepDesc& d, l
         q.y = fix32(y, d);
         if (d.dims == 3) q.z = fix32(z, d);
         S.rec[i] = q;
+        if (d.prec == PREC_FP32) {
+            key = fix_dist2(q, S.recb[i]);
+            bad = nonfinite_bits(x) || nonfinite_bits(y) || nonfinite_bits(z);
+        }
         if (d.prune) d2in = fix_dist2(q, S.recp[i]);
     }
-    return u2;
+    return key;
 }
 
-// block-level max of |disp|^2 (bit pattern; non-negative doubles order as
-// integers) and of the fixed-point displacement since the last prune, one
-// atomic per tile and only when it raises the replica's max
-__device__ __forceinline__ void block_max_to_state(double u2, unsigned long long d2in, const RepDesc& d,
-                                                   RepState& st, unsigned long long* s_max)
+// block-level max of the skin-trigger key (FP64: non-negative doubles order
+// as integers) and of the fixed-point displacement since the last prune,
+// one atomic per tile and only when it raises the replica's max
+__device__ __forceinline__ void block_max_to_state(unsigned long long bits, bool bad, unsigned long long d2in,
+                                                   const RepDesc& d, RepState& st, unsigned long long* s_max)
 {
-    unsigned long long bits = (unsigned long long)__double_as_longlong(u2);
-    if (nonfinite_bits(u2)) {
+    if (bad) {
         st.nonfinite = 1;
-        bits = 0x7ff0000000000000ull;
+        bits = 0x7ff0000000000000ull;  // above every threshold of either kind
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
@@ -114,6 +122,17 @@ __device__ __forceinline__ void block_max_to_state(double u2, unsigned long long
     __syncthreads();
 }
 
+// the displacement since the last rebuild of slot s, component k: FP64
+// replicas the accumulated one, split replicas the fixed-point difference
+// X - X_rebuild times u
+__device__ __forceinline__ double slot_disp(const Slots& S, const RepDesc& d, long long s, int k)
+{
+    if (d.prec == PREC_FP64) return k == 0 ? S.ux[s] : (k == 1 ? S.uy[s] : S.uz[s]);
+    const FixRec q = S.rec[s], q0 = S.recb[s];
+    const unsigned a = k == 0 ? q.x : (k == 1 ? q.y : q.z), a0 = k == 0 ? q0.x : (k == 1 ? q0.y : q0.z);
+    return dmul((double)(int)(a - a0), d.fix_ud);
+}
+
 // blocks per SM the position updates are compiled for (registers): more
 // warps in flight hide the FP64 and memory latency of these streaming passes
 #ifndef SIMMD_UPD_MINB
@@ -131,8 +150,8 @@ __global__ void __launch_bounds__(TILE, SIMMD_UPD_MINB) k_kick_drift(Batch b)
         if (d.dyn == DYN_BROWNIAN) continue;
         RepState& st = b.state[r];
         long long i = (long long)t * TILE + threadIdx.x;
-        double u2 = 0.0;
-        unsigned long long d2in = 0ull;
+        unsigned long long u2 = 0ull, d2in = 0ull;
+        bool bad = false;
         if (i < d.slot0 + d.n) {
             const Slots& S = b.s;
             const double vs = st.vscale;
@@ -155,9 +174,9 @@ __global__ void __launch_bounds__(TILE, SIMMD_UPD_MINB) k_kick_drift(Batch b)
                 vz = half_kick(vz, S.fz[i], d);
                 S.vz[i] = vz;
             }
-            u2 = drift_slot(b, d, i, dmul(d.dt, vx), dmul(d.dt, vy), dmul(d.dt, vz), d2in);
+            u2 = drift_slot(b, d, i, dmul(d.dt, vx), dmul(d.dt, vy), dmul(d.dt, vz), d2in, bad);
         }
-        block_max_to_state(u2, d2in, d, st, s_max);
+        block_max_to_state(u2, bad, d2in, d, st, s_max);
     }
 }
 
@@ -176,8 +195,8 @@ __global__ void __launch_bounds__(TILE, SIMMD_UPD_MINB) k_brownian_update(Batch 
         if (d.dyn != DYN_BROWNIAN) continue;
         RepState& st = b.state[r];
         long long i = (long long)t * TILE + threadIdx.x;
-        double u2 = 0.0;
-        unsigned long long d2in = 0ull;
+        unsigned long long u2 = 0ull, d2in = 0ull;
+        bool bad = false;
         if (i < d.slot0 + d.n) {
             const Slots& S = b.s;
             const double c = d.dt_over_gamma;
@@ -209,9 +228,9 @@ __global__ void __launch_bounds__(TILE, SIMMD_UPD_MINB) k_brownian_update(Batch 
                     }
                 }
             }
-            u2 = drift_slot(b, d, i, drx, dry, drz, d2in);
+            u2 = drift_slot(b, d, i, drx, dry, drz, d2in, bad);
         }
-        block_max_to_state(u2, d2in, d, st, s_max);
+        block_max_to_state(u2, bad, d2in, d, st, s_max);
     }
 }
 
@@ -285,8 +304,8 @@ __global__ void k_min_drift(Batch b, double dt, double max_step)
         if (!st.min_active || st.min_done) continue;
         const double stepsize = __longlong_as_double((long long)st.min_step);
         const long long i = (long long)t * TILE + threadIdx.x;
-        double u2 = 0.0;
-        unsigned long long d2in = 0ull;
+        unsigned long long u2 = 0ull, d2in = 0ull;
+        bool bad = false;
         if (i < d.slot0 + d.n) {
             const Slots& S = b.s;
             double vx = dmul(S.fx[i], dt), vy = dmul(S.fy[i], dt), vz = d.dims == 3 ? dmul(S.fz[i], dt) : 0.0;
@@ -296,9 +315,9 @@ __global__ void k_min_drift(Batch b, double dt, double max_step)
                 vy = dmul(vy, sc);
                 vz = dmul(vz, sc);
             }
-            u2 = drift_slot(b, d, i, vx, vy, vz, d2in);
+            u2 = drift_slot(b, d, i, vx, vy, vz, d2in, bad);
         }
-        block_max_to_state(u2, d2in, d, st, s_max);
+        block_max_to_state(u2, bad, d2in, d, st, s_max);
     }
 }
 
@@ -496,9 +515,9 @@ __global__ void k_store_aos(Batch b, int rep, double* r, double* v, double* F, d
         }
     }
     if (disp) {
-        disp[o * dm] = S.ux[s];
-        disp[o * dm + 1] = S.uy[s];
-        if (dm == 3) disp[o * dm + 2] = S.uz[s];
+        disp[o * dm] = slot_disp(S, d, s, 0);
+        disp[o * dm + 1] = slot_disp(S, d, s, 1);
+        if (dm == 3) disp[o * dm + 2] = slot_disp(S, d, s, 2);
     }
     if (epp && epp_src) epp[o] = epp_src[s];
 }
@@ -520,7 +539,17 @@ __global__ void k_set_state(Batch b, int rep, const double* r, const double* v, 
         p.y = r[o * dm + 1];
         if (dm == 3) p.z = r[o * dm + 2];
         S.posD[s] = p;
-        if (d.prec == PREC_FP32 || d.prune) S.rec[s] = fix_rec(p.x, p.y, p.z, p.w, d);
+        if (d.prec == PREC_FP32 || d.prune) {
+            const FixRec q0 = S.rec[s], q = fix_rec(p.x, p.y, p.z, p.w, d);
+            S.rec[s] = q;
+            if (d.prec == PREC_FP32 && !disp) {  // the displacement since the rebuild is kept
+                FixRec qb = S.recb[s];
+                qb.x += q.x - q0.x;
+                qb.y += q.y - q0.y;
+                qb.z += q.z - q0.z;
+                S.recb[s] = qb;
+            }
+        }
     }
     if (v) {
         S.vx[s] = v[o * dm];
@@ -537,6 +566,11 @@ __global__ void k_set_state(Batch b, int rep, const double* r, const double* v, 
         S.ux[s] = disp[o * dm];
         S.uy[s] = disp[o * dm + 1];
         if (dm == 3) S.uz[s] = disp[o * dm + 2];
+        if (d.prec == PREC_FP32) {  // the rebuild-time record: the position minus the displacement
+            const double4_32a p = S.posD[s];
+            S.recb[s] = fix_rec(dsub(p.x, disp[o * dm]), dsub(p.y, disp[o * dm + 1]),
+                                dm == 3 ? dsub(p.z, disp[o * dm + 2]) : 0.0, p.w, d);
+        }
     }
 }
 
@@ -621,11 +655,38 @@ __global__ void k_store_all(Batch b, double* r, double* v, double* F, double* di
             }
         }
         if (disp) {
-            disp[o] = S.ux[s];
-            disp[o + 1] = S.uy[s];
-            if (dm == 3) disp[o + 2] = S.uz[s];
+            disp[o] = slot_disp(S, d, s, 0);
+            disp[o + 1] = slot_disp(S, d, s, 1);
+            if (dm == 3) disp[o + 2] = slot_disp(S, d, s, 2);
         }
     }
+}
+
+// max(D) of each replica's block of a batched upload (one block per
+// replica; max is order-independent, so the result is exact)
+__global__ void k_rep_dmax(Batch b, const double* D, double* out)
+{
+    const int r = blockIdx.x;
+    if (r >= b.nreps) return;
+    const RepDesc& d = b.desc[r];
+    if (!d.active) return;
+    double m = 0.0;
+    for (long long k = threadIdx.x; k < d.n; k += blockDim.x) m = fmax(m, D[d.xfer_soff + k]);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+    __shared__ double s_m[32];
+    if ((threadIdx.x & 31) == 0) s_m[threadIdx.x >> 5] = m;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int w = 1; w < (int)(blockDim.x >> 5); w++) m = fmax(m, s_m[w]);
+        out[r] = m;
+    }
+}
+
+void launch_rep_dmax_impl(const Batch& b, const LaunchCfg& lc, const double* D, double* out)
+{
+    k_rep_dmax<<<b.nreps, 256, 0, lc.stream>>>(b, D, out);
+    if (lc.launches) *lc.launches += 1;
 }
 
 void launch_load_all(const Batch& b, const LaunchCfg& lc, const double* r, const double* v, const double* F,

@@ -150,17 +150,21 @@ __device__ void mc_chain(const Batch& b, const RepDesc& d, RepState& st, const u
                         st.mc_counts[0] += 1;
                         st.mc_dE = dadd(st.mc_dE, dE);
                         S.posD[si] = make_double4_32a(rn[0], rn[1], rn[2], pi.w);
-                        const double ux = dadd(S.ux[si], dr[0]), uy = dadd(S.uy[si], dr[1]);
-                        S.ux[si] = ux;
-                        S.uy[si] = uy;
-                        double u2 = dadd(dmul(ux, ux), dmul(uy, uy));
-                        if (DIM == 3) {
-                            const double uz = dadd(S.uz[si], dr[2]);
-                            S.uz[si] = uz;
-                            u2 = dadd(u2, dmul(uz, uz));
-                        }
                         if (d.prec == PREC_FP32 || d.prune) S.rec[si] = fix_rec(rn[0], rn[1], rn[2], pi.w, d);
-                        rebuild = u2 > d.skin_half2;
+                        if (d.prec == PREC_FP64) {
+                            const double ux = dadd(S.ux[si], dr[0]), uy = dadd(S.uy[si], dr[1]);
+                            S.ux[si] = ux;
+                            S.uy[si] = uy;
+                            double u2 = dadd(dmul(ux, ux), dmul(uy, uy));
+                            if (DIM == 3) {
+                                const double uz = dadd(S.uz[si], dr[2]);
+                                S.uz[si] = uz;
+                                u2 = dadd(u2, dmul(uz, uz));
+                            }
+                            rebuild = u2 > d.skin_half2;
+                        } else {  // split precision: the fixed-point displacement since the rebuild
+                            rebuild = fix_dist2(S.rec[si], S.recb[si]) > d.skin_thr;
+                        }
                     }
                     if (rebuild) {  // src/MC.jl:147-149: rebuild before the next move
                         st.mc_next = i + 1;

@@ -226,7 +226,9 @@ __global__ void k_rb_gather(Batch b, int* ncnt_full)
             int nc = d.nc;
             int cx = lin % nc, cy = (lin / nc) % nc, cz = lin / (nc * nc);
             S.cellc[nw] = pack_cell(cx, cy, cz);
-            S.rec[nw] = fix_rec(p.x, p.y, p.z, p.w, d);
+            const FixRec q = fix_rec(p.x, p.y, p.z, p.w, d);
+            S.rec[nw] = q;
+            S.recb[nw] = q;  // displacement since this rebuild: 0
         } else {
             S.t_posD[nw] = make_double4_32a(0.0, 0.0, 0.0, 0.0);
             S.t_vx[nw] = S.t_vy[nw] = S.t_vz[nw] = 0.0;
@@ -234,6 +236,7 @@ __global__ void k_rb_gather(Batch b, int* ncnt_full)
             S.t_orig[nw] = -1;
             S.cellc[nw] = 0;
             S.rec[nw] = FixRec{0u, 0u, 0u, 0.0f};
+            S.recb[nw] = FixRec{0u, 0u, 0u, 0.0f};
         }
     }
 }
@@ -586,98 +589,6 @@ __global__ void k_rb_done(Batch b)
     st.force_rebuild = 0;
     st.rebuilds += 1;
     st.force_prune = 1;  // the slots were re-ordered: the inner list follows
-}
-
-// ---------------------------------------------------------------------------
-// Inner (pruned) list of the force pass, per replica whose trigger fired
-// (a particle moved more than prune_skin/2 since the last prune) or that was
-// rebuilt: the outer-list entries j of i with
-//     |r_ij| <= sqrt(rc2) * s_ij * (1 + 1e-4) + prune_skin
-// on the fixed-point records (s_ij the pair diameter of the potential, FP32),
-// (LJ: |r_ij| <= r_cut * (1 + 1e-4) + prune_skin, r_cut the larger of the
-// force and energy cutoffs) in the outer list's order.  A pair within the
-// force cutoff at a later
-// step was within sqrt(rc2)*s_ij + prune_skin at the prune (each particle
-// moved at most prune_skin/2), and the 1e-4 slack covers the FP32 roundings
-// of the test, so the inner list holds every pair the force pass finds in
-// range; the pairs it drops were out of range and add exactly zero.
-// One thread per particle, whole tiles of the pruning replicas.
-// ---------------------------------------------------------------------------
-constexpr int PRUNE_UNROLL = 4;
-
-__global__ void __launch_bounds__(TILE) k_prune(Batch b)
-{
-    for (int t = blockIdx.x; t < b.ntiles; t += gridDim.x) {
-        const int r = b.tile_rep[t];
-        if (r < 0) continue;
-        const RepDesc& d = b.desc[r];
-        if (!d.active || !need_prune(b.state[r], d)) continue;
-        const long long i = (long long)t * TILE + threadIdx.x;
-        const Slots& S = b.s;
-        int m = 0;
-        if (i < d.slot0 + d.n) {
-            const FixRec ri = S.rec[i];
-            S.recp[i] = ri;
-            const int cnt = S.ncnt[i], K = b.K, T = b.tpp;
-            const float u2 = d.fix_u2, sk = d.prune_skin_f, rcf = d.prune_rcut_f;
-            const bool ber = d.pot == POT_BERTHIER;
-            auto keep = [&](const FixRec& rj) {
-                const float r2 = __ull2float_rn(fix_dist2(ri, rj)) * u2;
-                float tt = rcf + sk;  // LJ: one cutoff radius
-                if (ber) {
-                    const float sij = (ri.d + rj.d) * 0.5f * (1.0f - d.zetaf * fabsf(ri.d - rj.d));
-                    tt = fmaf(rcf, sij, sk);
-                }
-                return r2 <= tt * tt;
-            };
-            // PRUNE_UNROLL entries and their records loaded before the tests
-            int n = 0;
-            for (; n + PRUNE_UNROLL <= cnt; n += PRUNE_UNROLL) {
-                unsigned e[PRUNE_UNROLL];
-                FixRec q[PRUNE_UNROLL];
-#pragma unroll
-                for (int u = 0; u < PRUNE_UNROLL; u++) e[u] = __ldg(S.nbr + nbr_addr(n + u, i, T, K));
-#pragma unroll
-                for (int u = 0; u < PRUNE_UNROLL; u++) q[u] = rec_get(S.rec + (e[u] & IDX_MASK));
-#pragma unroll
-                for (int u = 0; u < PRUNE_UNROLL; u++)
-                    if (keep(q[u])) S.nbr_in[nbr_addr(m++, i, T, K)] = e[u];
-            }
-            for (; n < cnt; n++) {
-                const unsigned e = __ldg(S.nbr + nbr_addr(n, i, T, K));
-                if (keep(rec_get(S.rec + (e & IDX_MASK)))) S.nbr_in[nbr_addr(m++, i, T, K)] = e;
-            }
-        }
-        S.ncnt_in[i] = m;
-        // the replica's inner-list size: one atomic per warp (the whole
-        // block takes this branch: one replica per tile)
-        unsigned long long sum = (unsigned long long)m;
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
-        if ((threadIdx.x & 31) == 0 && sum) atomicAdd(&b.state[r].entries_in_acc, sum);
-    }
-}
-
-// after the prune: the pruned replicas' triggers reset, inner-list sizes
-__global__ void k_prune_done(Batch b)
-{
-    const int r = blockIdx.x * blockDim.x + threadIdx.x;
-    if (r >= b.nreps) return;
-    const RepDesc& d = b.desc[r];
-    RepState& st = b.state[r];
-    if (!d.active || !need_prune(st, d)) return;
-    st.maxdisp_in = 0ull;
-    st.force_prune = 0;
-    st.prunes += 1;
-    st.list_entries_in = (long long)st.entries_in_acc;
-    st.entries_in_acc = 0ull;
-}
-
-void launch_prune_impl(const Batch& b, const LaunchCfg& lc)
-{
-    k_prune<<<lc.grid_stream, TILE, 0, lc.stream>>>(b);
-    k_prune_done<<<(b.nreps + 127) / 128, 128, 0, lc.stream>>>(b);
-    if (lc.launches) *lc.launches += 2;
 }
 
 // the host's requests: one thread per entry rep * 4 + flags (1 rebuild,

@@ -72,6 +72,10 @@ struct RepDesc {
     long long noise_step0;
     int noise_nsteps;
     float dmaxf;               // max(D) rounded to FP32: bounds every pair threshold of the build
+    double fix_ud;             // u = L / 2^32 (exact)
+    // split precision: the skin trigger on the fixed-point displacement
+    // since the last rebuild, |X - X_rebuild|^2 > skin_thr (units^2)
+    unsigned long long skin_thr;
     // pruned (inner) list of the force pass: the outer-list pairs within
     // rc_ij + prune_skin at the last prune, valid while no particle has moved
     // prune_skin / 2 since (the pairs it drops add exactly zero to the sums)
@@ -83,7 +87,8 @@ struct RepDesc {
 };
 
 struct RepState {
-    unsigned long long maxdisp2;  // bits of the max |disp|^2 (non-negative double)
+    unsigned long long maxdisp2;  // max |disp|^2: FP64 replicas its bits (a non-negative double), split
+                                  // replicas the fixed-point |X - X_rebuild|^2
     int force_rebuild;
     int overflow;
     int nonfinite;
@@ -145,6 +150,7 @@ struct Slots {
     unsigned* nbr_in;             // inner (pruned) list, the same layout; null when not kept
     int* ncnt_in;
     FixRec* recp;                 // the record at the last prune (displacement since)
+    FixRec* recb;                 // split precision: the record at the last rebuild (displacement since)
     // rebuild scratch
     int* bin_cell;
     int* bin_rank;
@@ -294,7 +300,9 @@ __device__ __forceinline__ FixRec rec_get(const FixRec* __restrict__ r)
 
 __device__ __forceinline__ bool need_rebuild(const RepState& st, const RepDesc& d)
 {
-    return st.force_rebuild || (__longlong_as_double((long long)st.maxdisp2) > d.skin_half2);
+    if (st.force_rebuild) return true;
+    if (d.prec == PREC_FP32) return st.maxdisp2 > d.skin_thr;
+    return __longlong_as_double((long long)st.maxdisp2) > d.skin_half2;
 }
 
 __device__ __forceinline__ bool need_prune(const RepState& st, const RepDesc& d)

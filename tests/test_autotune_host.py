@@ -1,7 +1,7 @@
 """Autotuner selection logic against a fake batch (no device): it picks the
 fastest (tpp, skin) and tile shape (particles per work item), skips skins
 whose predicted lists overflow max_neighbors, and tunes each replica group's
-skin in a second pass."""
+skin in a second pass, and the inner skin of the filtered lists."""
 import numpy as np
 
 from simulationcode_gb300.autotune import autotune
@@ -17,7 +17,7 @@ class FakeBatch:
     """step time = sum over replicas of a cost that depends on its skin and
     the batch's threads per particle; lists grow with the skin"""
 
-    def __init__(self, specs, best2d, best3d, max_count=40):
+    def __init__(self, specs, best2d, best3d, max_count=40, best_tpp=2, best_inner=None):
         self.specs = dict(enumerate(specs))
         self.skin = {r: s.skin for r, s in self.specs.items()}
         self.tpp = 1
@@ -27,6 +27,13 @@ class FakeBatch:
         self.calls = []
         self.item = 0
         self.best_item = 0
+        self.best_tpp = best_tpp
+        self.best_inner = best_inner  # None: filtered lists never pay
+        self.inner_skin = 0.0
+
+    def set_prune(self, inner_skin, rid=-1):
+        assert self.tpp == 1 or inner_skin == 0
+        self.inner_skin = inner_skin
 
     def set_skin(self, skin, rid=-1):
         for r in self.specs:
@@ -44,7 +51,11 @@ class FakeBatch:
         ms = 0.0
         for r, s in self.specs.items():
             ms += 1.0 + 5.0 * (self.skin[r] - self.best[s.dims]) ** 2
-        return ms * (1.0 + 0.1 * abs(np.log2(self.tpp) - 1)) * (1.0 if self.item == self.best_item else 1.05)
+        ms *= (1.0 + 0.1 * abs(np.log2(self.tpp) - np.log2(self.best_tpp)))
+        ms *= 1.0 if self.item == self.best_item else 1.05
+        if self.inner_skin > 0:
+            ms *= 0.9 if self.inner_skin == self.best_inner else 1.03
+        return ms
 
     def step(self, n):
         self.t += n * self._ms()
@@ -94,3 +105,20 @@ def test_overflowing_skins_are_skipped():
     assert res.skin == 0.3
     assert any("skipped" in m for m in seen)
     assert all(t["skin"] == 0.3 for t in res.trials)
+
+
+def test_inner_skin_axis_with_one_thread_per_particle():
+    """with one thread per particle the inner skin of the filtered lists is
+    tuned and kept only when it beats no filtering"""
+    from simulationcode_gb300.autotune import as_tuned
+    b = FakeBatch([spec(3), spec(2)], best2d=0.3, best3d=0.3, best_tpp=1, best_inner=0.3)
+    res = autotune(b, tpps=(1, 2), skins=[0.3], warmup=1, steps=2, work_items=(0,), inner_skins=(0.2, 0.3, 0.4))
+    assert res.tpp == 1 and res.inner_skin == 0.3 and b.inner_skin == 0.3
+    assert as_tuned(res, b)["inner_skin"] == 0.3
+    b2 = FakeBatch([spec(3), spec(2)], best2d=0.3, best3d=0.3, best_tpp=1, best_inner=None)
+    res2 = autotune(b2, tpps=(1, 2), skins=[0.3], warmup=1, steps=2, work_items=(0,), inner_skins=(0.2, 0.3))
+    assert res2.inner_skin == 0.0 and b2.inner_skin == 0.0
+    # more threads per particle: no filtered lists tried
+    b3 = FakeBatch([spec(3)], best2d=0.3, best3d=0.3, best_tpp=2, best_inner=0.3)
+    res3 = autotune(b3, tpps=(1, 2), skins=[0.3], warmup=1, steps=2, work_items=(0,))
+    assert res3.tpp == 2 and res3.inner_skin == 0.0

@@ -33,7 +33,7 @@ def _pair(specs, graphs, inner):
     for prune in (False, True):
         b = ReplicaBatch(0, graphs=graphs, graph_steps=8)
         ids = [b.add(copy.copy(s)) for s in specs]
-        if prune:
+        if prune and inner > 0:
             b.set_prune(inner)
         b.rebuild()
         out.append((b, ids))
@@ -96,10 +96,11 @@ def test_pruned_lists_on_the_replica_workload(simlib):
     from simulationcode_gb300 import autotune as AT
     specs = W.c4(indices=list(range(24)))
     W.relax_on_device(specs, 0)
-    tuned = AT.load_tuned("c4")
-    (a, ia), (b, ib) = _pair(specs, True, 0.15)
+    tuned = dict(AT.load_tuned("c4"), inner_skin=0.0)
+    (a, ia), (b, ib) = _pair(specs, True, 0.0)
     AT.apply_tuned(a, tuned)
-    AT.apply_tuned(b, tuned)
+    AT.apply_tuned(b, dict(tuned, inner_skin=0.15))
+    assert b.inner_skin == 0.15 and a.inner_skin == 0.0
     a.step(100)
     b.step(100)
     _same(a, b, ia, ib)
