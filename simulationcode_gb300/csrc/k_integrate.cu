@@ -69,11 +69,8 @@ __device__ __forceinline__ unsigned long long drift_slot(const Batch& b, const R
     const double y = wrap_coord(dadd(p.y, dry), d);
     const double z = (d.dims == 3) ? wrap_coord(dadd(p.z, drz), d) : p.z;
     S.posD[i] = make_double4_32a(x, y, z, p.w);
-    if (d.prec == PREC_FP32 || d.prune) {  // the record's fixed-point position (D kept)
-        FixRec q = S.rec[i];
-        q.x = fix32(x, d);
-        q.y = fix32(y, d);
-        if (d.dims == 3) q.z = fix32(z, d);
+    if (d.prec == PREC_FP32 || d.prune) {  // the record, rebuilt from the position (no read)
+        const FixRec q = fix_rec(x, y, z, p.w, d);
         S.rec[i] = q;
         if (d.prec == PREC_FP32) {
             key = fix_dist2(q, S.recb[i]);
@@ -180,6 +177,28 @@ __global__ void __launch_bounds__(TILE, SIMMD_UPD_MINB) k_kick_drift(Batch b)
     }
 }
 
+// set-up relaxation: |dr| <= cap per particle (out of line: it runs only
+// during the relaxation and would otherwise hold registers of the hot path)
+__device__ __noinline__ void relax_clamp(double& drx, double& dry, double& drz, double cap)
+{
+    double m = fmax(fabs(drx), fmax(fabs(dry), fabs(drz)));
+    if (m > 0.0) {
+        double qx = drx / m, qy = dry / m, qz = drz / m;
+        double len = m * sqrt(qx * qx + qy * qy + qz * qz);
+        if (!(len <= cap)) {
+            double sc = cap / len;
+            drx = isfinite(sc) ? drx * sc : 0.0;
+            dry = isfinite(sc) ? dry * sc : 0.0;
+            drz = isfinite(sc) ? drz * sc : 0.0;
+            if (!isfinite(len)) {
+                drx = qx * cap;
+                dry = qy * cap;
+                drz = qz * cap;
+            }
+        }
+    }
+}
+
 // Brownian position update (src/MD.jl:444-467 as intended): dr = (dt/gamma)
 // (F - <F>), displacement, wrap.  F itself is left as computed (the mean
 // subtraction is applied again when F is downloaded), saving a store.
@@ -210,24 +229,7 @@ __global__ void __launch_bounds__(TILE, SIMMD_UPD_MINB) k_brownian_update(Batch 
                 dry = fma(c, S.fy[i], st.cfmean[1]);
                 if (d.dims == 3) drz = fma(c, S.fz[i], st.cfmean[2]);
             }
-            if (d.relax_cap > 0.0) {  // set-up relaxation: |dr| <= relax_cap per particle
-                double m = fmax(fabs(drx), fmax(fabs(dry), fabs(drz)));
-                if (m > 0.0) {
-                    double qx = drx / m, qy = dry / m, qz = drz / m;
-                    double len = m * sqrt(qx * qx + qy * qy + qz * qz);
-                    if (!(len <= d.relax_cap)) {
-                        double sc = d.relax_cap / len;
-                        drx = isfinite(sc) ? drx * sc : 0.0;
-                        dry = isfinite(sc) ? dry * sc : 0.0;
-                        drz = isfinite(sc) ? drz * sc : 0.0;
-                        if (!isfinite(len)) {
-                            drx = qx * d.relax_cap;
-                            dry = qy * d.relax_cap;
-                            drz = qz * d.relax_cap;
-                        }
-                    }
-                }
-            }
+            if (d.relax_cap > 0.0) relax_clamp(drx, dry, drz, d.relax_cap);
             u2 = drift_slot(b, d, i, drx, dry, drz, d2in, bad);
         }
         block_max_to_state(u2, bad, d2in, d, st, s_max);
