@@ -56,8 +56,9 @@ def autotune(batch: ReplicaBatch, *, tpps: Iterable[int] = (1, 2, 4, 8), skins: 
     overflow max_neighbors is skipped (skins are tried in increasing order).
     ``group_by(spec)``: a second pass tunes the skin of each group of
     replicas separately (the rebuild cadence that suits 2D replicas differs
-    from 3D).  Last, with one thread per particle, the inner skin of the
-    force pass's filtered lists (kept only when it beats no filtering)."""
+    from 3D).  Last, the inner skin of the force pass's filtered lists with
+    one thread per particle (kept only when it beats every configuration
+    without them)."""
     base_skin = next(iter(batch.specs.values())).skin if batch.specs else 0.3
     skins = [base_skin] if skins is None else sorted(skins)
     skin_seen = base_skin
@@ -132,23 +133,28 @@ def autotune(batch: ReplicaBatch, *, tpps: Iterable[int] = (1, 2, 4, 8), skins: 
                     batch.set_skin(gbest[0], rid)
                 group_skins[str(key)] = gbest[0]
                 ms = min(ms, gbest[1])
-    # inner skin of the force pass's filtered lists (one thread per particle)
+    # inner skin of the force pass's filtered lists (one thread per particle:
+    # tried also when more threads per particle won without them)
     inner = 0.0
-    if tpp == 1:
-        inner_ms = ms
+    if 1 in tuple(tpps) and inner_skins:
+        best_tpp, inner_ms = tpp, ms
+        if tpp != 1:
+            batch.set_tuning(1, True, gs)
         for si in inner_skins:
             batch.set_prune(si)
             batch.step(warmup)
             batch.timer_start()
             batch.step(steps)
             t = batch.timer_stop() / steps
-            trials.append({"tpp": tpp, "skin": skin, "inner_skin": si, "graph_steps": gs, "ms_per_step": t})
+            trials.append({"tpp": 1, "skin": skin, "inner_skin": si, "graph_steps": gs, "ms_per_step": t})
             if log:
-                log("autotune: inner skin %.2f -> %.4f ms/step" % (si, t))
+                log("autotune: tpp=1 inner skin %.2f -> %.4f ms/step" % (si, t))
             if t < inner_ms:
-                inner, inner_ms = si, t
+                inner, inner_ms, best_tpp = si, t, 1
         batch.set_prune(inner)
-        ms = inner_ms
+        if best_tpp != 1:
+            batch.set_tuning(best_tpp, True, gs)
+        tpp, ms = best_tpp, inner_ms
     return TuneResult(tpp=tpp, skin=skin, graph_steps=gs, ms_per_step=ms, trials=trials, group_skins=group_skins,
                       work_item=item, inner_skin=inner)
 

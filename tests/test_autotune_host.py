@@ -118,7 +118,11 @@ def test_inner_skin_axis_with_one_thread_per_particle():
     b2 = FakeBatch([spec(3), spec(2)], best2d=0.3, best3d=0.3, best_tpp=1, best_inner=None)
     res2 = autotune(b2, tpps=(1, 2), skins=[0.3], warmup=1, steps=2, work_items=(0,), inner_skins=(0.2, 0.3))
     assert res2.inner_skin == 0.0 and b2.inner_skin == 0.0
-    # more threads per particle: no filtered lists tried
+    # more threads per particle won without filtered lists: one thread per
+    # particle with them is tried and kept only if faster
     b3 = FakeBatch([spec(3)], best2d=0.3, best3d=0.3, best_tpp=2, best_inner=0.3)
     res3 = autotune(b3, tpps=(1, 2), skins=[0.3], warmup=1, steps=2, work_items=(0,))
-    assert res3.tpp == 2 and res3.inner_skin == 0.0
+    assert res3.tpp == 1 and res3.inner_skin == 0.3 and b3.tpp == 1   # 1.1 * 0.9 < 1.0
+    b4 = FakeBatch([spec(3)], best2d=0.3, best3d=0.3, best_tpp=4, best_inner=0.3)
+    res4 = autotune(b4, tpps=(1, 2, 4), skins=[0.3], warmup=1, steps=2, work_items=(0,))
+    assert res4.tpp == 4 and res4.inner_skin == 0.0 and b4.tpp == 4 and b4.inner_skin == 0.0
