@@ -41,7 +41,7 @@ import SimulationCode: initialize_neighbor_struct, update_neighbor_lists!, calcu
 using SimulationCode: Newtonian, Langevin, Brownian
 
 export GPU, GPUNeighborList, nocallback, gpu_dump_async, gpu_dump_wait, gpu_check_conversions,
-       gpu_energy_virial_noalloc!
+       gpu_energy_virial_noalloc!, gpu_set_prune!
 
 const libsimmd = get(ENV, "SIMMD_LIB", "libsimmd.so")
 
@@ -394,6 +394,13 @@ function gpu_dump_async(nl::GPUNeighborList, r::Matrix{Float64}, v::Matrix{Float
 end
 
 gpu_dump_wait(nl::GPUNeighborList) = check(ccall((:simmd_dump_wait, libsimmd), Cint, (Ptr{Cvoid},), nl.ctx))
+
+"""filtered force lists: the force pass reads the pairs within rc_ij +
+inner_skin and re-filters when a particle has moved inner_skin / 2
+(bit-identical results; one thread per particle); 0 turns them off"""
+gpu_set_prune!(nl::GPUNeighborList, inner_skin::Real) =
+    check(ccall((:simmd_set_prune, libsimmd), Cint, (Ptr{Cvoid}, Int32, Float64), nl.ctx, Int32(-1),
+                Float64(inner_skin)))
 
 """device self-check: mismatches of the split kernels' bit-level float <->
 double conversions against the hardware converter (0 expected)"""
