@@ -1158,9 +1158,9 @@ int simmd_engine_create(int32_t device, simmd_ctx** out)
     }
     int st = dalloc(c, &c->d_queue, 4);
     if (st == SIMMD_OK) st = cudaMemsetAsync(c->d_queue, 0, 4 * sizeof(int), c->stream) == cudaSuccess ? 0 : SIMMD_ERR_CUDA;
-    if (st == SIMMD_OK) st = dalloc(c, &c->d_plan_cnt, 4);
+    if (st == SIMMD_OK) st = dalloc(c, &c->d_plan_cnt, 8);
     if (st == SIMMD_OK)
-        st = cudaMemsetAsync(c->d_plan_cnt, 0, 4 * sizeof(int), c->stream) == cudaSuccess ? 0 : SIMMD_ERR_CUDA;
+        st = cudaMemsetAsync(c->d_plan_cnt, 0, 8 * sizeof(int), c->stream) == cudaSuccess ? 0 : SIMMD_ERR_CUDA;
     if (st != SIMMD_OK) {
         delete c;
         return st;
@@ -1751,7 +1751,7 @@ int simmd_timer_stop(simmd_ctx* c, float* ms)
     return SIMMD_OK;
 }
 
-// rebuild bodies executed so far (device counter of k_rb_done); bodies that a
+// rebuild bodies executed so far (device counter of k_rb_copyback); bodies that a
 // conditional graph node skipped are enqueued but not run
 static long long bodies_executed(simmd_ctx* c)
 {

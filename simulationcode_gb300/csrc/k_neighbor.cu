@@ -24,9 +24,9 @@
 //             d2 from dx - round(dx/L)*L in the reference's operation order.
 //             The list stores each pair in both directions (no atomics in
 //             the force pass)
-//   copyback  staging to the main arrays
-//   done      reset displacement max / request flag, count the rebuild,
-//             clear the plan
+//   copyback  staging to the main arrays; its last block resets the
+//             displacement max / request flags, counts the rebuild and
+//             clears the plan
 #include "simmd_internal.cuh"
 
 namespace simmd {
@@ -43,7 +43,7 @@ __device__ __forceinline__ int plan_count(const Batch& b, int which)
 // its cell counters are zeroed
 // Inside a captured step loop the rest of the sequence is the body of a
 // conditional graph node: a planning block sets the node's condition, so a
-// step in which no replica's trigger fired skips the eight other launches.
+// step in which no replica's trigger fired skips the seven other launches.
 __global__ void k_rb_plan(Batch b, cudaGraphConditionalHandle cond, int use_cond)
 {
     const int r = blockIdx.x;
@@ -275,7 +275,6 @@ struct BuildSmem {
     float4 o[BLD_CHUNK];  // position relative to the home cell's reference point (FP32), D
     int slot[BLD_CHUNK];  // slot of the candidate (-1: padding of the last round)
     int ca[27];
-    int cn[27];
     int pre[28];
     unsigned rf[3];  // the home cell's centre in fixed point
     int nst;
@@ -354,32 +353,38 @@ __device__ void build_cell(const Batch& b, const RepDesc& d, RepState& st, int c
     const int rng = (nc >= 3) ? 1 : 0;
     const int w = 2 * rng + 1;
     const int nst = (DIM == 3) ? w * w * w : w * w;
-    if (tid < nst) {
-        int ox = tid % w - rng, oy = (tid / w) % w - rng, oz = (DIM == 3) ? tid / (w * w) - rng : 0;
-        int x = (cx + ox + nc) % nc, y = (cy + oy + nc) % nc, z = (DIM == 3) ? (cz + oz + nc) % nc : 0;
-        int lin = x + nc * (y + nc * z);
-        int a = S.cell_start[d.cell0 + lin];
-        sm.ca[tid] = a;
-        sm.cn[tid] = S.cell_start[d.cell0 + lin + 1] - a;
-    }
-    // reference point at the home cell centre (fixed point, (2c+1) 2^31 / nc):
-    // candidate coordinates relative to it are small, exact integer
-    // differences (minimum image by the int32 wraparound) turned into FP32,
-    // so a pair difference is one FP32 subtract
-    if (tid == 32) {
-        sm.rf[0] = (unsigned)(((2ull * (unsigned long long)cx + 1ull) << 31) / (unsigned long long)nc);
-        sm.rf[1] = (unsigned)(((2ull * (unsigned long long)cy + 1ull) << 31) / (unsigned long long)nc);
-        sm.rf[2] = (DIM == 3) ? (unsigned)(((2ull * (unsigned long long)cz + 1ull) << 31) / (unsigned long long)nc)
-                              : 0u;
-    }
-    __syncthreads();
-    if (tid == 0) {
-        int acc = 0;
-        for (int k = 0; k < nst; k++) {
-            sm.pre[k] = acc;
-            acc += sm.cn[k];
+    if (tid < 32) {
+        // warp 0: stencil cell `tid`'s first slot and count, the candidates
+        // before it by a warp scan
+        int a = 0, n = 0;
+        if (tid < nst) {
+            const int ox = tid % w - rng, oy = (tid / w) % w - rng, oz = (DIM == 3) ? tid / (w * w) - rng : 0;
+            const int x = (cx + ox + nc) % nc, y = (cy + oy + nc) % nc, z = (DIM == 3) ? (cz + oz + nc) % nc : 0;
+            const int lin = x + nc * (y + nc * z);
+            a = S.cell_start[d.cell0 + lin];
+            n = S.cell_start[d.cell0 + lin + 1] - a;
         }
-        sm.pre[nst] = acc;
+        int incl = n;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, incl, o);
+            if (tid >= o) incl += y;
+        }
+        if (tid < nst) {
+            sm.ca[tid] = a;
+            sm.pre[tid] = incl - n;
+        }
+        if (tid == 31) sm.pre[nst] = incl;  // lanes past the stencil add nothing
+    } else if (tid < 35) {
+        // reference point at the home cell centre (fixed point, (2c+1) 2^31 /
+        // nc), one axis per lane of warp 1: candidate coordinates relative to
+        // it are small, exact integer differences (minimum image by the int32
+        // wraparound) turned into FP32, so a pair difference is one FP32
+        // subtract
+        const int k = tid - 32;
+        const int cc = k == 0 ? cx : (k == 1 ? cy : cz);
+        sm.rf[k] = (k < DIM) ? (unsigned)(((2ull * (unsigned long long)cc + 1ull) << 31) / (unsigned long long)nc)
+                             : 0u;
     }
     __syncthreads();
     const int M = sm.pre[nst];
@@ -554,6 +559,10 @@ __global__ void __launch_bounds__(BLD_THREADS, 8) k_rb_build(Batch b, unsigned* 
 
 // copy the staged (re-ordered) state back; separate kernel because the build
 // reads neighbours' staged positions
+// the end of the sequence: the staged (re-ordered) state copied back
+// (a separate kernel because the build reads neighbours' staged positions);
+// the last block to finish then closes the rebuild of every planned replica
+// (displacement max, request flags, counters) and clears the plan
 __global__ void k_rb_copyback(Batch b)
 {
     const int ntask = plan_count(b, 0);
@@ -570,25 +579,31 @@ __global__ void k_rb_copyback(Batch b)
         S.fz[i] = S.t_fz[i];
         S.orig[i] = S.t_orig[i];
     }
-}
-
-__global__ void k_rb_done(Batch b)
-{
-    int r = blockIdx.x * blockDim.x + threadIdx.x;
-    if (r == 0) {  // every rebuild kernel of this sequence has run: the plan is spent
+    __shared__ int s_last;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        s_last = atomicAdd(&b.plan_cnt[4], 1) == (int)gridDim.x - 1;
+    }
+    __syncthreads();
+    if (!s_last) return;
+    __threadfence();
+    if (threadIdx.x == 0) {  // every block has read the plan: it is spent
+        b.plan_cnt[4] = 0;
         b.plan_cnt[0] = 0;
         b.plan_cnt[1] = 0;
         *reinterpret_cast<unsigned long long*>(b.plan_cnt + 2) += 1ull;  // bodies executed
     }
-    if (r >= b.nreps) return;
-    const RepDesc& d = b.desc[r];
-    RepState& st = b.state[r];
-    if (!d.active || !st.in_plan) return;
-    st.in_plan = 0;
-    st.maxdisp2 = 0ull;
-    st.force_rebuild = 0;
-    st.rebuilds += 1;
-    st.force_prune = 1;  // the slots were re-ordered: the inner list follows
+    for (int r = threadIdx.x; r < b.nreps; r += blockDim.x) {
+        const RepDesc& d = b.desc[r];
+        RepState& st = b.state[r];
+        if (!d.active || !st.in_plan) continue;
+        st.in_plan = 0;
+        st.maxdisp2 = 0ull;
+        st.force_rebuild = 0;
+        st.rebuilds += 1;
+        st.force_prune = 1;  // the slots were re-ordered: the inner list follows
+    }
 }
 
 // the host's requests: one thread per entry rep * 4 + flags (1 rebuild,
@@ -625,8 +640,7 @@ void launch_rebuild_body_impl(const Batch& b, const LaunchCfg& lc, unsigned* nbr
     if (nbr_full) k_rb_build<true><<<g, BLD_THREADS, 0, lc.stream>>>(b, nbr_full, ncnt_full, Kfull);
     else k_rb_build<false><<<g, BLD_THREADS, 0, lc.stream>>>(b, nullptr, nullptr, 0);
     k_rb_copyback<<<g, TILE, 0, lc.stream>>>(b);
-    k_rb_done<<<(b.nreps + 127) / 128, 128, 0, lc.stream>>>(b);
-    if (lc.launches) *lc.launches += 8;
+    if (lc.launches) *lc.launches += 7;
 }
 
 // ---------------------------------------------------------------------------

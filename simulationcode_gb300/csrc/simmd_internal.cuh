@@ -181,7 +181,7 @@ struct Batch {
     // rebuild plan: tiles and cells of the replicas rebuilding this step
     int* plan_tiles;              // [ntiles]
     int2* plan_cells;             // [cell capacity] (replica, cell)
-    int* plan_cnt;                // [0] tiles, [1] cells
+    int* plan_cnt;                // [0] tiles, [1] cells, [2..3] bodies run (64-bit), [4] copy-back blocks done
 };
 
 // ---------------------------------------------------------------------------
