@@ -464,6 +464,7 @@ static LaunchCfg make_lc(simmd_ctx* c, int mode)
     lc.stream = c->stream;
     long long nt = c->S_cap / TILE;
     lc.grid_stream = (int)std::max(1LL, std::min(nt, (long long)c->sm_count * 16));
+    lc.grid_copy = std::max(1, c->sm_count * 4);
     const int parts = force_parts(c);
     lc.grid_force64 = c->sm_count * force_blocks_per_sm(c->T, mode, PREC_FP64, parts);
     lc.grid_force32 = c->sm_count * force_blocks_per_sm(c->T, mode, PREC_FP32, parts);

@@ -639,7 +639,9 @@ void launch_rebuild_body_impl(const Batch& b, const LaunchCfg& lc, unsigned* nbr
     k_rb_gather<<<g, TILE, 0, lc.stream>>>(b, ncnt_full);
     if (nbr_full) k_rb_build<true><<<g, BLD_THREADS, 0, lc.stream>>>(b, nbr_full, ncnt_full, Kfull);
     else k_rb_build<false><<<g, BLD_THREADS, 0, lc.stream>>>(b, nullptr, nullptr, 0);
-    k_rb_copyback<<<g, TILE, 0, lc.stream>>>(b);
+    // fewer blocks for the copy-back: each block's completion is one atomic on
+    // the closing counter
+    k_rb_copyback<<<min(g, lc.grid_copy), TILE, 0, lc.stream>>>(b);
     if (lc.launches) *lc.launches += 7;
 }
 

@@ -414,6 +414,7 @@ __device__ __forceinline__ void normal_pair_f32(unsigned long long seed, long lo
 struct LaunchCfg {
     cudaStream_t stream;
     int grid_stream;      // blocks for streaming kernels
+    int grid_copy;        // blocks for the rebuild's copy-back (4 per SM)
     int grid_force64;     // blocks for the persistent force kernel, FP64 replicas
     int grid_force32;     // ... split-precision replicas
     long long* launches;  // launch counter
