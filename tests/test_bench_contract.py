@@ -32,3 +32,17 @@ def test_reference_arm_json_line():
     assert cb["value"] == d["value"] and cb["kind"] in ("port", "reference") and cb["cores"] >= 1 and cb["sample"]
     e = d["e2e"]
     assert e["value"] == d["value"] and e["h2d_bytes_per_step"] == 0 and e["d2h_bytes_per_step"] == 0
+
+
+def test_force_bytes_model_follows_the_list_read():
+    """the roofline's algorithmic bytes: per particle its record, count and
+    force (plus the velocity stream for Newtonian/Langevin) and 4 B per list
+    entry the launch reads (the filtered list's count when one is given)"""
+    import bench
+    from types import SimpleNamespace as NS
+    specs = [NS(N=100, dims=3, dynamics=2), NS(N=50, dims=2, dynamics=0)]
+    stats = [NS(list_entries=3000), NS(list_entries=800)]
+    per3 = 8 * 3 + 8 + 4 + 8 * 3
+    per2 = 8 * 2 + 8 + 4 + 8 * 2 + 16 * 2
+    assert bench.force_bytes_per_launch(specs, stats) == 100 * per3 + 50 * per2 + 4 * (3000 + 800)
+    assert bench.force_bytes_per_launch(specs, stats, [1500.0, 400.0]) == 100 * per3 + 50 * per2 + 4 * (1500 + 400)
