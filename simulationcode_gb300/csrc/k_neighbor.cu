@@ -274,10 +274,9 @@ constexpr int BLD_CHUNK = 512;
 struct BuildSmem {
     float4 o[BLD_CHUNK];  // position relative to the home cell's reference point (FP32), D
     int slot[BLD_CHUNK];  // slot of the candidate (-1: padding of the last round)
-    int ca[27];
-    int pre[28];
+    int ca[27];      // first slot of each stencil cell
+    int pre[28];     // candidates before each stencil cell (pre[nst]: all)
     unsigned rf[3];  // the home cell's centre in fixed point
-    int nst;
     unsigned long long entries;
     int maxcnt;
 };
