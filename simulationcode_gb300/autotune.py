@@ -197,7 +197,9 @@ def skin_for(tuned: Optional[dict], spec) -> float:
 
 def apply_tuned(batch: ReplicaBatch, tuned: dict, graphs: bool = True):
     """set a batch to a stored tuning: per-group skins, threads per particle,
-    steps per captured graph"""
+    steps per captured graph, tile shape and the inner skin of the filtered
+    lists (turned off before a threads-per-particle change, since filtered
+    lists need one thread per particle)"""
     for rid, spec in list(batch.specs.items()):
         sk = skin_for(tuned, spec)
         if sk != spec.skin:

@@ -126,3 +126,14 @@ def test_inner_skin_axis_with_one_thread_per_particle():
     b4 = FakeBatch([spec(3)], best2d=0.3, best3d=0.3, best_tpp=4, best_inner=0.3)
     res4 = autotune(b4, tpps=(1, 2, 4), skins=[0.3], warmup=1, steps=2, work_items=(0,))
     assert res4.tpp == 4 and res4.inner_skin == 0.0 and b4.tpp == 4 and b4.inner_skin == 0.0
+
+
+def test_apply_tuned_sets_the_inner_skin_after_threads_per_particle():
+    """a stored tuning with an inner skin turns the filtered lists on after
+    one thread per particle is set; one without turns them off first"""
+    from simulationcode_gb300.autotune import apply_tuned
+    b = FakeBatch([spec(3)], best2d=0.3, best3d=0.3, best_tpp=1, best_inner=0.3)
+    apply_tuned(b, {"tpp": 1, "graph_steps": 16, "skins": {"3D": 0.5}, "inner_skin": 0.3})
+    assert b.tpp == 1 and b.inner_skin == 0.3 and b.skin[0] == 0.5
+    apply_tuned(b, {"tpp": 2, "graph_steps": 16, "skins": {"3D": 0.5}})
+    assert b.tpp == 2 and b.inner_skin == 0.0
