@@ -4,9 +4,11 @@
 Prints ONE JSON line.  A "step" is one MD time step of every particle of the
 workload (all replicas).  ``value`` = particle-steps/s with the state
 resident in HBM (device-timed with CUDA events on the library's stream);
-``e2e`` = the same metric through the C ABI with host buffers: upload of the
-ArrayStruct arrays from page-locked host memory, simmd_step, download of the
-state, all inside the timed region.
+``e2e`` = the same metric through the C ABI with host buffers: the
+ArrayStruct arrays from page-locked host memory to the device
+(simmd_set_state_all: a caller holding the state between segments),
+simmd_step, download of the state, all inside the timed region; a restart
+segment (simmd_upload_all, new lists first) is reported beside it.
 
     python bench.py [--workload c4] [--steps K] [--warmup W] [--gpus N]
     python bench.py --impl reference ...   # the reference algorithm on the host cores
@@ -572,49 +574,62 @@ def run_gpu(args, dist):
             traffic = None
 
     # e2e through the C ABI: host (page-locked) arrays -> device, K steps,
-    # device -> host, every replica at once (simmd_upload_all /
-    # simmd_download_all: one copy per array, one synchronisation)
+    # device -> host, every replica at once (one copy per array, one
+    # synchronisation each way).  The timed segment is that of a caller that
+    # holds the state on the host between calls (the reference's driver
+    # between callbacks): simmd_set_state_all (the lists and skin bookkeeping
+    # stay valid) + simmd_step(K) + simmd_download_all.  A restart segment
+    # (simmd_upload_all: new lists for every replica before the first step)
+    # is timed after it and reported beside it.
     total, offs = batch.transfer_layout()
     any_v = any(s.dynamics != 2 for s in specs)
     r_all = np.zeros(total)
     v_all = np.zeros(total) if any_v else None
     D_all = np.zeros(sum(s.N for s in specs))
-    outs = [np.zeros(total), np.zeros(total) if any_v else None, np.zeros(total)]
+    F_all = np.zeros(total)
     doff = 0
     for rid, s in sorted(zip(ids, specs), key=lambda t: t[0]):
-        o = offs[rid]
-        r_all[o:o + s.N * s.dims] = np.asarray(s.r, dtype=np.float64).reshape(-1)
-        if any_v and s.v is not None:
-            v_all[o:o + s.N * s.dims] = np.asarray(s.v, dtype=np.float64).reshape(-1)
         D_all[doff:doff + s.N] = s.D
         doff += s.N
-    host = [a for a in [r_all, v_all, D_all] + outs if a is not None]
+    host = [a for a in (r_all, v_all, D_all, F_all) if a is not None]
     for a in host:
         _lib.check(lib.simmd_host_register(C.c_void_p(a.ctypes.data), a.nbytes))
-    h2d = r_all.nbytes + D_all.nbytes + (v_all.nbytes if any_v else 0)
-    d2h = outs[0].nbytes + outs[2].nbytes + (outs[1].nbytes if any_v else 0)
-    e2e_steps = args.steps
-    if not args.no_e2e:
-        # one untimed round: the staging buffers of the batched transfers are
-        # allocated once per context, as in a user's repeated segments
-        batch.upload_all(r_all, D_all, v=v_all)
-        batch.download_all(outs[0], outs[1], outs[2])
+    h2d = r_all.nbytes + (v_all.nbytes if any_v else 0)
+    d2h = r_all.nbytes + F_all.nbytes + (v_all.nbytes if any_v else 0)
+    e2e_steps = 0 if args.no_e2e else args.steps
+    restart = None
+    # one untimed round: the host takes the current state, and the staging
+    # buffers of the batched transfers are allocated once per context, as in
+    # a user's repeated segments
+    batch.download_all(r_all, v_all, F_all)
+    batch.set_state_all(r_all, v_all)
     dist.barrier()
-    if args.no_e2e:
-        e2e_steps = 0
     t0 = time.perf_counter()
-    batch.upload_all(r_all, D_all, v=v_all)
+    batch.set_state_all(r_all, v_all)
     if e2e_steps:
         _lib.check(lib.simmd_step(batch.ctx, e2e_steps, None))
-    batch.download_all(outs[0], outs[1], outs[2])
+    batch.download_all(r_all, v_all, F_all)
     e2e_s = dist.max(time.perf_counter() - t0)
+    if e2e_steps:
+        dist.barrier()
+        t0 = time.perf_counter()
+        batch.upload_all(r_all, D_all, v=v_all)
+        _lib.check(lib.simmd_step(batch.ctx, e2e_steps, None))
+        batch.download_all(r_all, v_all, F_all)
+        rs = dist.max(time.perf_counter() - t0)
+        restart = {"value": n_all * e2e_steps / rs, "unit": "particle-steps/s",
+                   "h2d_bytes_per_step": (h2d + D_all.nbytes) / e2e_steps, "d2h_bytes_per_step": d2h / e2e_steps,
+                   "what": "simmd_upload_all (r, %sD) + simmd_step(K) + simmd_download_all: new lists for every "
+                           "replica before the first step" % ("v, " if any_v else "")}
     for a in host:
         lib.simmd_host_unregister(C.c_void_p(a.ctypes.data))
     e2e_steps = max(e2e_steps, 1)
     e2e = {"value": n_all * e2e_steps / e2e_s, "unit": "particle-steps/s",
            "h2d_bytes_per_step": h2d / e2e_steps, "d2h_bytes_per_step": d2h / e2e_steps,
-           "what": "simmd_upload_all (r, %sD of every replica from page-locked host arrays) + simmd_step(K) + "
-                   "simmd_download_all (r, %sF), wall clock" % ("v, " if any_v else "", "v, " if any_v else "")}
+           "what": "simmd_set_state_all (r%s of every replica from page-locked host arrays; lists kept) + "
+                   "simmd_step(K) + simmd_download_all (r, %sF), wall clock" % (", v" if any_v else "",
+                                                                                 "v, " if any_v else ""),
+           "restart": restart}
 
     # bytes streamed per step: force launch + positions, velocities, forces,
     # displacements of the integrator pass

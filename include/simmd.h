@@ -185,12 +185,16 @@ int simmd_set_state_r(simmd_ctx* ctx, int32_t rep, const double* r, const double
  * dims x N array (-1: NULL context) and, if offsets is not NULL, fills
  * offsets[rep] for rep < n with the replica's first double (-1 for ids not
  * in use).  simmd_upload_all = simmd_upload_r of every
- * replica (r, D required; v, F, disp may be NULL = zeros); simmd_download_all
- * = simmd_download_r of every replica (any pointer may be NULL).  Host
- * arrays page-locked with simmd_host_register transfer at full link speed. */
+ * replica (r, D required; v, F, disp may be NULL = zeros); simmd_set_state_all
+ * = simmd_set_state_r of every replica (any pointer may be NULL: the lists
+ * and the skin bookkeeping are kept, the segment loop of a caller that holds
+ * the state on the host between calls); simmd_download_all =
+ * simmd_download_r of every replica (any pointer may be NULL).  Host arrays
+ * page-locked with simmd_host_register transfer at full link speed. */
 int64_t simmd_transfer_layout(simmd_ctx* ctx, int32_t n, int64_t* offsets);
 int simmd_upload_all(simmd_ctx* ctx, const double* r, const double* v, const double* F, const double* D,
                      const double* disp);
+int simmd_set_state_all(simmd_ctx* ctx, const double* r, const double* v, const double* F, const double* disp);
 int simmd_download_all(simmd_ctx* ctx, double* r, double* v, double* F, double* disp);
 /* find_inherent_structure (src/InherentStructure.jl:5-56) for every replica
    of the context, in FP64 with the reference's arithmetic: steepest descent

@@ -86,6 +86,7 @@ SIGNATURES = {
     "simmd_transfer_layout": (C.c_int64, [_vp, C.c_int32, _vp]),
     "simmd_upload_all": (C.c_int, [_vp, _vp, _vp, _vp, _vp, _vp]),
     "simmd_download_all": (C.c_int, [_vp, _vp, _vp, _vp, _vp]),
+    "simmd_set_state_all": (C.c_int, [_vp, _vp, _vp, _vp, _vp]),
     "simmd_energy_all": (C.c_int, [_vp]),
     "simmd_stats_r": (C.c_int, [_vp, C.c_int32, _P(Stats)]),
     "simmd_replica_bytes": (C.c_int64, [_P(Params), C.c_int32]),

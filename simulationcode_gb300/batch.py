@@ -136,6 +136,13 @@ class ReplicaBatch:
         D: their N diameters in id order)"""
         _lib.check(self.lib.simmd_upload_all(self.ctx, _lib.ptr(r), _lib.ptr(v), _lib.ptr(F), _lib.ptr(D), None))
 
+    def set_state_all(self, r: Optional[np.ndarray] = None, v: Optional[np.ndarray] = None,
+                      F: Optional[np.ndarray] = None, disp: Optional[np.ndarray] = None):
+        """simmd_set_state_all: every replica's state overwritten in place from
+        flat float64 arrays in the batched layout (any may be None), keeping
+        the lists and the skin bookkeeping"""
+        _lib.check(self.lib.simmd_set_state_all(self.ctx, _lib.ptr(r), _lib.ptr(v), _lib.ptr(F), _lib.ptr(disp)))
+
     def download_all(self, r: Optional[np.ndarray] = None, v: Optional[np.ndarray] = None,
                      F: Optional[np.ndarray] = None):
         """simmd_download_all into flat float64 arrays in the batched layout"""

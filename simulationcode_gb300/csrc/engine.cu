@@ -1432,6 +1432,33 @@ int simmd_upload_all(simmd_ctx* c, const double* r, const double* v, const doubl
     return SIMMD_OK;
 }
 
+int simmd_set_state_all(simmd_ctx* c, const double* r, const double* v, const double* F, const double* disp)
+{
+    if (!c) return set_err(SIMMD_ERR_BAD_ARG, "NULL context");
+    CK(cudaSetDevice(c->device));
+    long long nv = 0, ns = 0;
+    xfer_layout(c, &nv, &ns);
+    if (nv == 0) return set_err(SIMMD_ERR_NOT_FOUND, "no replica");
+    std::vector<RepDesc> dstage;
+    if (c->xfer_dirty) TRY(push_all_desc(c, dstage));  // the transfer offsets, read by the kernel below
+    TRY(ensure_stage(c, nv));
+    double* stg = c->d_stage;
+    double *dr = stg, *dv = stg + c->stage_cap, *dF = stg + 2 * c->stage_cap, *du = stg + 4 * c->stage_cap;
+    if (r) CK(cudaMemcpyAsync(dr, r, sizeof(double) * nv, cudaMemcpyHostToDevice, c->stream));
+    if (v) CK(cudaMemcpyAsync(dv, v, sizeof(double) * nv, cudaMemcpyHostToDevice, c->stream));
+    if (F) CK(cudaMemcpyAsync(dF, F, sizeof(double) * nv, cudaMemcpyHostToDevice, c->stream));
+    if (disp) CK(cudaMemcpyAsync(du, disp, sizeof(double) * nv, cudaMemcpyHostToDevice, c->stream));
+    Batch b = make_batch(c);
+    LaunchCfg lc = make_lc(c, FMODE_STEP);
+    launch_set_state_all(b, lc, r ? dr : nullptr, v ? dv : nullptr, F ? dF : nullptr, disp ? du : nullptr);
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(c->stream));
+    if (r)  // the lists are kept; the inner lists are re-pruned
+        for (int rep = 0; rep < c->R_cap; rep++)
+            if (c->reps[rep].active) c->reps[rep].pending_prune = true;
+    return SIMMD_OK;
+}
+
 int simmd_download_all(simmd_ctx* c, double* r, double* v, double* F, double* disp)
 {
     if (!c) return set_err(SIMMD_ERR_BAD_ARG, "NULL context");

@@ -525,15 +525,16 @@ __global__ void k_store_aos(Batch b, int rep, double* r, double* v, double* F, d
 }
 
 // host arrays (original order) -> current slot order; lists and cells kept
-__global__ void k_set_state(Batch b, int rep, const double* r, const double* v, const double* F,
-                            const double* disp)
+// slot s (original id o) of a replica takes the host's values; r, v, F,
+// disp point at the replica's dims x N block (original order) or are NULL.
+// The lists and the skin bookkeeping are kept: an edited position keeps its
+// displacement since the rebuild (split replicas shift the rebuild-time
+// record with it), unless a displacement is given
+__device__ __forceinline__ void set_slot_state(const Batch& b, const RepDesc& d, RepState& st, long long s, int o,
+                                               const double* r, const double* v, const double* F,
+                                               const double* disp)
 {
-    const RepDesc& d = b.desc[rep];
-    long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= d.n) return;
-    long long s = d.slot0 + k;
-    Slots& S = b.s;
-    const int o = S.orig[s];
+    const Slots& S = b.s;
     const int dm = d.dims;
     if (r) {
         double4_32a p = S.posD[s];
@@ -562,7 +563,7 @@ __global__ void k_set_state(Batch b, int rep, const double* r, const double* v, 
         S.fx[s] = F[o * dm];
         S.fy[s] = F[o * dm + 1];
         if (dm == 3) S.fz[s] = F[o * dm + 2];
-        if (k == 0) b.state[rep].fmean_pending = 0;  // the host's F is final
+        if (s == d.slot0) st.fmean_pending = 0;  // the host's F is final
     }
     if (disp) {
         S.ux[s] = disp[o * dm];
@@ -573,6 +574,33 @@ __global__ void k_set_state(Batch b, int rep, const double* r, const double* v, 
             S.recb[s] = fix_rec(dsub(p.x, disp[o * dm]), dsub(p.y, disp[o * dm + 1]),
                                 dm == 3 ? dsub(p.z, disp[o * dm + 2]) : 0.0, p.w, d);
         }
+    }
+}
+
+__global__ void k_set_state(Batch b, int rep, const double* r, const double* v, const double* F,
+                            const double* disp)
+{
+    const RepDesc& d = b.desc[rep];
+    long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= d.n) return;
+    const long long s = d.slot0 + k;
+    set_slot_state(b, d, b.state[rep], s, b.s.orig[s], r, v, F, disp);
+}
+
+// every active replica at once, batched host layout (replica r's dims x N
+// block at xfer_off, replicas in id order); one thread per slot
+__global__ void k_set_state_all(Batch b, const double* r, const double* v, const double* F, const double* disp)
+{
+    for (int t = blockIdx.x; t < b.ntiles; t += gridDim.x) {
+        const int rep = b.tile_rep[t];
+        if (rep < 0) continue;
+        const RepDesc& d = b.desc[rep];
+        if (!d.active) continue;
+        const long long s = (long long)t * TILE + threadIdx.x;
+        if (s - d.slot0 >= d.n) continue;
+        const long long o = d.xfer_off;
+        set_slot_state(b, d, b.state[rep], s, b.s.orig[s], r ? r + o : nullptr, v ? v + o : nullptr,
+                       F ? F + o : nullptr, disp ? disp + o : nullptr);
     }
 }
 
@@ -695,6 +723,13 @@ void launch_load_all(const Batch& b, const LaunchCfg& lc, const double* r, const
                      const double* D, const double* disp)
 {
     k_load_all<<<lc.grid_stream, TILE, 0, lc.stream>>>(b, r, v, F, D, disp);
+    if (lc.launches) *lc.launches += 1;
+}
+
+void launch_set_state_all(const Batch& b, const LaunchCfg& lc, const double* r, const double* v, const double* F,
+                          const double* disp)
+{
+    k_set_state_all<<<lc.grid_stream, TILE, 0, lc.stream>>>(b, r, v, F, disp);
     if (lc.launches) *lc.launches += 1;
 }
 

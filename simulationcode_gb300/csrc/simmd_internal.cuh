@@ -433,6 +433,8 @@ void launch_kinetic(const Batch& b, const LaunchCfg& lc);
 void launch_load_all(const Batch& b, const LaunchCfg& lc, const double* r, const double* v, const double* F,
                      const double* D, const double* disp);
 void launch_store_all(const Batch& b, const LaunchCfg& lc, double* r, double* v, double* F, double* disp);
+void launch_set_state_all(const Batch& b, const LaunchCfg& lc, const double* r, const double* v, const double* F,
+                          const double* disp);
 void launch_export_list(const Batch& b, const LaunchCfg& lc, int rep, const RepDesc& hd,
                         long long* counts, long long* list, long long maxK, int half_only);
 

@@ -191,3 +191,55 @@ def test_download_all_after_layout_query_and_skin_change(simlib):
     b.step(3)
     check()
     b.close()
+
+
+def test_set_state_all_equals_per_replica_set_state(simlib):
+    """simmd_set_state_all (every replica in one call, lists and skin
+    bookkeeping kept) equals simmd_set_state_r replica by replica, bit for
+    bit; handing back the state just downloaded leaves the trajectory and the
+    rebuild count as if the call had not been made (the segment loop of a
+    caller that holds the state on the host)."""
+    specs = _relaxed(_mixed_specs(seed=6))
+    a, b, c = ReplicaBatch(0), ReplicaBatch(0), ReplicaBatch(0)
+    ia = [a.add(s) for s in specs]
+    ib = [b.add(s) for s in specs]
+    ic = [c.add(s) for s in specs]
+    for batch in (a, b, c):
+        batch.rebuild()
+        batch.step(9)
+    # c: the state goes to the host and back between two segments
+    total, offs = c.transfer_layout()
+    r_h, v_h = np.zeros(total), np.zeros(total)
+    c.download_all(r_h, v_h)
+    c.set_state_all(r_h, v_h)
+    rebuilds_before = [c.stats(i).rebuilds for i in ic]
+    # a per replica, b at once: positions moved within the skin, new velocities
+    rng = np.random.default_rng(7)
+    new = {}
+    for k, s in enumerate(specs):
+        r0 = a.state(ia[k])[0]
+        new[k] = (np.mod(r0 + rng.uniform(-0.004, 0.004, r0.shape), s.box_size), rng.standard_normal(r0.shape) * 0.3)
+        _lib.check(a.lib.simmd_set_state_r(a.ctx, ia[k], _lib.ptr(new[k][0]), _lib.ptr(new[k][1]), None, None))
+    total_b, offs_b = b.transfer_layout()
+    r_all, v_all = np.zeros(total_b), np.zeros(total_b)
+    for k, s in enumerate(specs):
+        o, n = offs_b[ib[k]], s.N * s.dims
+        r_all[o:o + n] = new[k][0].reshape(-1)
+        v_all[o:o + n] = new[k][1].reshape(-1)
+    b.set_state_all(r_all, v_all)
+    for batch in (a, b, c):
+        batch.step(21)
+    ref = ReplicaBatch(0)
+    ir = [ref.add(s) for s in specs]
+    ref.rebuild()
+    ref.step(30)
+    for k in range(len(specs)):
+        for x, y in zip(a.state(ia[k]), b.state(ib[k])):
+            assert np.array_equal(x, y), k
+        assert a.stats(ia[k]).rebuilds == b.stats(ib[k]).rebuilds
+        for x, y in zip(ref.state(ir[k]), c.state(ic[k])):
+            assert np.array_equal(x, y), k
+        assert ref.stats(ir[k]).rebuilds == c.stats(ic[k]).rebuilds
+        assert c.stats(ic[k]).rebuilds >= rebuilds_before[k]
+    for batch in (a, b, c, ref):
+        batch.close()
