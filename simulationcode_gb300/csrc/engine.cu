@@ -1793,7 +1793,7 @@ static long long bodies_executed(simmd_ctx* c)
     return (long long)n;
 }
 
-static const int REBUILD_BODY_LAUNCHES = 8;
+static const int REBUILD_BODY_LAUNCHES = 7;  // the launches of launch_rebuild_body_impl
 
 // kernels run: enqueued launches less the bodies that were skipped
 int64_t simmd_launch_count(simmd_ctx* c)

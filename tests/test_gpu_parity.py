@@ -174,18 +174,24 @@ def test_set_skin_rebuilds_with_new_pair_set(simlib, oracle):
 def test_conditional_rebuild_bodies_counted(simlib, oracle):
     """In a captured step loop a rebuild sequence's body runs only when a
     trigger fired: with one replica, bodies run == the replica's rebuilds,
-    and the trajectory equals direct launches bit for bit."""
+    the kernels counted as run are three a step (kick1+drift, plan, force),
+    seven per body run and the closing COM/rescale pass, and the trajectory
+    equals direct launches bit for bit."""
     import ctypes as C
     p, r, v, D, rc = make_case(0, 3, 0, 1000, seed=12)
     a = GpuSystem(p, r, D, v=v, force_cutoff=rc, graphs=True)
     b = GpuSystem(p, r, D, v=v, force_cutoff=rc, graphs=False)
+    f, rb = C.c_int64(), C.c_int64()
     for g in (a, b):
         g.rebuild()
+    assert simlib.simmd_kernel_counts(a.ctx, C.byref(f), C.byref(rb)) == 0
+    rb0, l0 = rb.value, simlib.simmd_launch_count(a.ctx)
+    for g in (a, b):
         g.step(96)
-    f, rb = C.c_int64(), C.c_int64()
     assert simlib.simmd_kernel_counts(a.ctx, C.byref(f), C.byref(rb)) == 0
     assert rb.value == a.stats().rebuilds
     assert 1 < a.stats().rebuilds < 96
+    assert simlib.simmd_launch_count(a.ctx) - l0 == 3 * 96 + 7 * (rb.value - rb0) + 1
     for x, y in zip(a.state(), b.state()):
         assert np.array_equal(x, y)
 
