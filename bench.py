@@ -212,7 +212,9 @@ def workload_config(workload, specs, n_particles, n_replicas, tuned):
     for s in specs:
         skins[group_key(s)] = skin_for(tuned, s)
     sb = state_bytes(specs)
-    return {"workload": workload, "description": W.DESCRIPTIONS[workload], "particles": int(n_particles),
+    # the configuration's own skin is 0.3; the skins the run uses are `skins`
+    desc = W.DESCRIPTIONS[workload].replace(", skin 0.3", ", skin 0.3 as configured (the run's: skins)")
+    return {"workload": workload, "description": desc, "particles": int(n_particles),
             "replicas": int(n_replicas), "skins": dict(sorted(skins.items())),
             "l2": ("state larger than L2 (%.0f MB of particle state per step), no flush" % (sb / 1e6))
                   if sb > 129e6 else "state fits in L2 (%.0f MB of particle state)" % (sb / 1e6)}
