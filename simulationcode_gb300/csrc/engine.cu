@@ -434,6 +434,23 @@ static int force_parts(const simmd_ctx* c)
     return parts;
 }
 
+// the stepping force pass leaves its replica sums to a pass of their own
+// (k_replica_means) when the batch has many tiles in small replicas: the
+// pass then runs no block barrier or reduction tree inside its persistent
+// loop.  Small batches (an extra launch would show) and large replicas (one
+// block reduces each replica's tiles) keep the reduction in the pass
+static int force_defer(const simmd_ctx* c)
+{
+    long long tiles = 0;
+    int maxt = 0;
+    for (const auto& h : c->reps)
+        if (h.active) {
+            tiles += h.d.ntiles;
+            maxt = std::max(maxt, h.d.ntiles);
+        }
+    return (tiles >= 4LL * c->sm_count && maxt <= 1024 && force_parts(c) == 1) ? 1 : 0;
+}
+
 static Batch make_batch(simmd_ctx* c)
 {
     Batch b{};
@@ -446,6 +463,7 @@ static Batch make_batch(simmd_ctx* c)
     b.K = c->K;
     b.tpp = c->T;
     b.parts = force_parts(c);
+    b.defer = force_defer(c);
     b.s = c->s;
     b.red_val = c->d_red_val;
     b.red_cnt = c->d_red_cnt;
@@ -935,7 +953,7 @@ static int read_states(simmd_ctx* c)
 static int graph_key(const simmd_ctx* c, const Mix& m, int fmode)
 {
     return (m.nl ? 1 : 0) | (m.br ? 2 : 0) | (m.rescale ? 4 : 0) | (m.prec_mask << 3) | (fmode << 5) |
-           (force_parts(c) << 8);
+           (force_parts(c) << 8) | (force_defer(c) << 16);
 }
 
 static int run_steps(simmd_ctx* c, long long nsteps, const double* noise)

@@ -403,7 +403,7 @@ __device__ __forceinline__ void finish_replica(const RepDesc& d, RepState& st, c
         st.entries_in_acc = 0ull;
     }
     constexpr bool EN = (MODE == FMODE_ENERGY || MODE == FMODE_STEP_ENERGY);
-    constexpr bool STEP = (MODE == FMODE_STEP || MODE == FMODE_STEP_ENERGY);
+    constexpr bool STEP = (MODE == FMODE_STEP || MODE == FMODE_STEP_ENERGY || MODE == FMODE_STEP_DEFER);
     const double nd = (double)d.n;
     if (STEP) {
         double* m = (d.dyn == DYN_BROWNIAN) ? st.fmean : st.vmean;
@@ -421,6 +421,20 @@ __device__ __forceinline__ void finish_replica(const RepDesc& d, RepState& st, c
     // and by the download); a plain force evaluation leaves F final
     if (MODE != FMODE_ENERGY && d.dyn == DYN_BROWNIAN) st.fmean_pending = STEP ? 1 : 0;
     if (noise) st.step += 1;
+}
+
+// a stepping pass (no energy) leaves the tile reduction to k_replica_means:
+// lane 0 of each warp stores the warp's sums in the tile's warp slot, with
+// no block barrier and no tree climb inside the persistent loop
+template <int NV>
+__device__ __forceinline__ void step_slot_store(const Batch& b, int t, int part, const double (&pv)[NV])
+{
+    if ((threadIdx.x & 31) == 0) {
+        const int nw = blockDim.x >> 5, wid = threadIdx.x >> 5;
+        double* slot = b.warp_part + ((size_t)t * WARP_SLOTS + (size_t)(part * nw + wid)) * NPART;
+#pragma unroll
+        for (int k = 0; k < NV; k++) slot[k] = pv[k];
+    }
 }
 
 #ifndef SIMMD_F32_MINB
@@ -441,7 +455,7 @@ template <int MODE, int PREC, int T>
 __global__ void __launch_bounds__(TILE * T, force_min_blocks<PREC, T>()) k_force(Batch b, double* epp)
 {
     constexpr bool EN = (MODE == FMODE_ENERGY || MODE == FMODE_STEP_ENERGY);
-    constexpr bool STEP = (MODE == FMODE_STEP || MODE == FMODE_STEP_ENERGY);
+    constexpr bool STEP = (MODE == FMODE_STEP || MODE == FMODE_STEP_ENERGY || MODE == FMODE_STEP_DEFER);
     constexpr int NV = EN ? 5 : 3;
     __shared__ int s_tile;
     __shared__ int s_flag;
@@ -598,7 +612,12 @@ __global__ void __launch_bounds__(TILE * T, force_min_blocks<PREC, T>()) k_force
                 pv[NV - 1] = dw;
             }
             if (prn) count_inner(st, m);
-            last = tile_reduce<NV, true>(b, item, d, st, pv, out, s_part, &s_flag, parts);
+            if (MODE == FMODE_STEP_DEFER) {  // lane 0 holds the warp's sums
+                step_slot_store<NV>(b, t, part, pv);
+                last = false;
+            } else {
+                last = tile_reduce<NV, true>(b, item, d, st, pv, out, s_part, &s_flag, parts);
+            }
         } else {
             // ---- FP64: the reference's arithmetic
             double fx = 0.0, fy = 0.0, fz = 0.0, e = 0.0, w = 0.0;
@@ -665,7 +684,13 @@ __global__ void __launch_bounds__(TILE * T, force_min_blocks<PREC, T>()) k_force
                 }
             }
             if (prn) count_inner(st, m);
-            last = tile_reduce<NV>(b, item, d, st, pv, out, s_part, &s_flag, parts);
+            if (MODE == FMODE_STEP_DEFER) {
+                warp_sum<NV>(pv);
+                step_slot_store<NV>(b, t, part, pv);
+                last = false;
+            } else {
+                last = tile_reduce<NV>(b, item, d, st, pv, out, s_part, &s_flag, parts);
+            }
         }
         if (last && tid == 0) finish_replica<MODE, NV>(d, st, out, noise, prn);
     }
@@ -676,6 +701,103 @@ __global__ void __launch_bounds__(TILE * T, force_min_blocks<PREC, T>()) k_force
             b.queue[1] = 0;
         }
     }
+}
+
+// after a stepping force pass, one block per replica: the replica's sums
+// from the warp slots of its tiles, in the canonical order of the tile
+// reduction (each tile its warp slots added in order; then groups of 32
+// consecutive tiles -- one warp -- reduced with compensation, level by
+// level, a level's group results kept in the reduction tree's records);
+// then what the pass's last tile does in the other modes: the mean force
+// (Brownian) or centre-of-mass velocity, the filtered-list bookkeeping and
+// the noise counter
+constexpr int MEANS_THREADS = 256;
+
+__global__ void __launch_bounds__(MEANS_THREADS) k_replica_means(Batch b)
+{
+    const int r = blockIdx.x, tid = threadIdx.x, lane = tid & 31;
+    const RepDesc& d = b.desc[r];
+    RepState& st = b.state[r];
+    if (!d.active || d.ntiles < 1) return;  // block-uniform
+    const int wpt = (TILE / b.parts) * b.tpp / 32 * b.parts;  // warp slots per tile
+    __shared__ double s_fin[6];
+    int n = d.ntiles;
+    for (int level = 0;; level++) {
+        const int ng = (n + 31) >> 5;
+        // every warp of the block takes whole groups; the block covers
+        // MEANS_THREADS members per round
+        for (int base = 0; base < ng * 32; base += MEANS_THREADS) {
+            const int idx = base + tid;
+            double s[3] = {0.0, 0.0, 0.0}, c[3] = {0.0, 0.0, 0.0};
+            if (idx < n) {
+                if (level == 0) {  // the tile's sum: its warp slots in order
+                    const double* slot = b.warp_part + (size_t)(d.tile0 + idx) * WARP_SLOTS * NPART;
+                    for (int w0 = 0; w0 < wpt; w0 += 8) {
+                        double v[8][3];
+#pragma unroll
+                        for (int w = 0; w < 8; w++)
+#pragma unroll
+                            for (int k = 0; k < 3; k++)
+                                v[w][k] = w0 + w < wpt ? __ldcg(slot + (size_t)(w0 + w) * NPART + k) : 0.0;
+#pragma unroll
+                        for (int w = 0; w < 8; w++)
+                            if (w0 + w < wpt)
+#pragma unroll
+                                for (int k = 0; k < 3; k++) s[k] += v[w][k];
+                    }
+                } else {
+                    const double* src = b.red_val + ((size_t)level * b.ntiles + d.tile0 + idx) * RED_REC;
+#pragma unroll
+                    for (int k = 0; k < 3; k++) {
+                        s[k] = __ldcg(src + k);
+                        c[k] = __ldcg(src + 3 + k);
+                    }
+                }
+            }
+            if (base + (tid & ~31) < ng * 32) {  // a warp of this level's groups
+                warp_sum_comp<3>(s, c);
+                const int g = (base + tid) >> 5;
+                if (lane == 0) {
+                    if (ng > 1) {
+                        double* dst = b.red_val + ((size_t)(level + 1) * b.ntiles + d.tile0 + g) * RED_REC;
+#pragma unroll
+                        for (int k = 0; k < 3; k++) {
+                            dst[k] = s[k];
+                            dst[3 + k] = c[k];
+                        }
+                    } else {
+#pragma unroll
+                        for (int k = 0; k < 3; k++) {
+                            s_fin[k] = s[k];
+                            s_fin[3 + k] = c[k];
+                        }
+                    }
+                }
+            }
+        }
+        __threadfence_block();
+        __syncthreads();
+        if (ng == 1) break;
+        n = ng;
+    }
+    if (tid != 0) return;
+    const bool pruned = b.tpp == 1 && need_prune(st, d);
+    if (pruned) {  // every tile of the replica wrote its inner list in this pass
+        st.maxdisp_in = 0ull;
+        st.force_prune = 0;
+        st.prunes += 1;
+        st.list_entries_in = (long long)st.entries_in_acc;
+        st.entries_in_acc = 0ull;
+    }
+    const double nd = (double)d.n;
+    double* m = (d.dyn == DYN_BROWNIAN) ? st.fmean : st.vmean;
+#pragma unroll
+    for (int k = 0; k < 3; k++) m[k] = ddiv(s_fin[k] + s_fin[3 + k], nd);
+    if (d.dyn == DYN_BROWNIAN) {
+        for (int k = 0; k < 3; k++) st.cfmean[k] = -(d.dt_over_gamma * m[k]);
+        st.fmean_pending = 1;
+    }
+    if (d.dyn != DYN_NEWTONIAN && d.relax_cap == 0.0) st.step += 1;
 }
 
 // ---------------------------------------------------------------------------
@@ -697,6 +819,7 @@ static void* kernel_for(int mode, int T)
 {
     switch (mode) {
         case FMODE_STEP: return kernel_ptr<FMODE_STEP, PREC>(T);
+        case FMODE_STEP_DEFER: return kernel_ptr<FMODE_STEP_DEFER, PREC>(T);
         case FMODE_FORCES: return kernel_ptr<FMODE_FORCES, PREC>(T);
         case FMODE_ENERGY: return kernel_ptr<FMODE_ENERGY, PREC>(T);
         default: return kernel_ptr<FMODE_STEP_ENERGY, PREC>(T);
@@ -714,6 +837,7 @@ int force_blocks_per_sm(int T, int mode, int prec, int parts)
 // one launch per precision present in the batch (prec_mask bit 0: FP64, bit 1: FP32 split)
 void launch_force_impl(const Batch& b, const LaunchCfg& lc, int mode, int prec_mask, double* epp)
 {
+    if (mode == FMODE_STEP && b.defer) mode = FMODE_STEP_DEFER;
     for (int prec = 0; prec < 2; prec++) {
         if (!(prec_mask & (1 << prec))) continue;
         void* k = prec == PREC_FP64 ? kernel_for<PREC_FP64>(mode, b.tpp) : kernel_for<PREC_FP32>(mode, b.tpp);
@@ -722,6 +846,10 @@ void launch_force_impl(const Batch& b, const LaunchCfg& lc, int mode, int prec_m
         void* args[] = {(void*)&bb, (void*)&ep};
         cudaLaunchKernel(k, dim3(prec == PREC_FP64 ? lc.grid_force64 : lc.grid_force32),
                          dim3((TILE / b.parts) * b.tpp), args, 0, lc.stream);
+        if (lc.launches) *lc.launches += 1;
+    }
+    if (mode == FMODE_STEP_DEFER) {
+        k_replica_means<<<b.nreps, MEANS_THREADS, 0, lc.stream>>>(b);
         if (lc.launches) *lc.launches += 1;
     }
 }

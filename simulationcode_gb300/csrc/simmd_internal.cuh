@@ -172,6 +172,7 @@ struct Batch {
     int K;                        // list rows
     int tpp;                      // threads per particle (list interleave)
     int parts;                    // force pass: work items per tile (power of two, <= MAX_PARTS)
+    int defer;                    // stepping force pass: replica sums reduced after the pass
     Slots s;
     double* red_val;              // [RED_LEVELS][ntiles][RED_REC] reduction tree values (sum, error)
     int* red_cnt;                 // [RED_LEVELS][ntiles] members of a tree group done (reset by the last)
@@ -438,6 +439,8 @@ void launch_set_state_all(const Batch& b, const LaunchCfg& lc, const double* r, 
 void launch_export_list(const Batch& b, const LaunchCfg& lc, int rep, const RepDesc& hd,
                         long long* counts, long long* list, long long maxK, int half_only);
 
-enum { FMODE_STEP = 0, FMODE_FORCES = 1, FMODE_ENERGY = 2, FMODE_STEP_ENERGY = 3 };
+// FMODE_STEP_DEFER: FMODE_STEP whose replica sums are reduced after the pass
+// (k_replica_means), chosen by the launch for batches of many small replicas
+enum { FMODE_STEP = 0, FMODE_FORCES = 1, FMODE_ENERGY = 2, FMODE_STEP_ENERGY = 3, FMODE_STEP_DEFER = 4 };
 
 }  // namespace simmd

@@ -243,3 +243,44 @@ def test_set_state_all_equals_per_replica_set_state(simlib):
         assert c.stats(ic[k]).rebuilds >= rebuilds_before[k]
     for batch in (a, b, c, ref):
         batch.close()
+
+
+def test_deferred_replica_sums_equal_the_in_pass_reduction(simlib):
+    """A batch of many small replicas leaves the stepping force pass's replica
+    sums (mean force, centre-of-mass velocity) to a pass of their own, which
+    adds the tiles' warp partials in the order of the in-pass tile reduction:
+    every replica's trajectory equals its run alone (in-pass reduction) bit
+    for bit, and the batch runs the extra pass each step."""
+    import ctypes as C
+    rng = np.random.default_rng(8)
+    specs = []
+    for k in range(200):
+        dims = 2 if k % 2 else 3
+        dyn = (_lib.BROWNIAN, _lib.LANGEVIN, _lib.NEWTONIAN)[k % 3]
+        prec = _lib.FP32_SPLIT if k % 4 else _lib.FP64
+        specs.append(W.berthier_spec(int(rng.integers(450, 600)), dims, dyn, rng, dt=1e-3, precision=prec,
+                                     seed=100 + k))
+    specs = _relaxed(specs)
+    mix = ReplicaBatch(0, graphs=True, graph_steps=8)
+    ids = [mix.add(s) for s in specs]
+    mix.rebuild()
+    f, rb = C.c_int64(), C.c_int64()
+    assert simlib.simmd_kernel_counts(mix.ctx, C.byref(f), C.byref(rb)) == 0
+    l0, rb0 = mix.launches(), rb.value
+    mix.step(24)
+    assert simlib.simmd_kernel_counts(mix.ctx, C.byref(f), C.byref(rb)) == 0
+    # a step: kick1+drift and a rebuild plan (Newtonian/Langevin), the force
+    # pass (one launch per precision), the replica sums, the position update
+    # and a rebuild plan (Brownian); seven per rebuild body run; the closing
+    # COM pass
+    assert mix.launches() - l0 == 24 * (1 + 1 + 2 + 1 + 1 + 1) + 7 * (rb.value - rb0) + 1
+    for k in (0, 1, 2, 3, 4, 5, 101, 199):
+        alone = ReplicaBatch(0, graphs=False)
+        a = alone.add(specs[k])
+        alone.rebuild()
+        alone.step(24)
+        for x, y in zip(alone.state(a), mix.state(ids[k])):
+            assert np.array_equal(x, y), k
+        assert alone.stats(a).rebuilds == mix.stats(ids[k]).rebuilds
+        alone.close()
+    mix.close()
