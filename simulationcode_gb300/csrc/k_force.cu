@@ -616,7 +616,7 @@ __global__ void __launch_bounds__(TILE * T, force_min_blocks<PREC, T>()) k_force
                 step_slot_store<NV>(b, t, part, pv);
                 last = false;
             } else {
-                last = tile_reduce<NV, true>(b, item, d, st, pv, out, s_part, &s_flag, parts);
+                last = tile_reduce<NV, true, 3>(b, item, d, st, pv, out, s_part, &s_flag, parts);
             }
         } else {
             // ---- FP64: the reference's arithmetic
@@ -689,7 +689,7 @@ __global__ void __launch_bounds__(TILE * T, force_min_blocks<PREC, T>()) k_force
                 step_slot_store<NV>(b, t, part, pv);
                 last = false;
             } else {
-                last = tile_reduce<NV>(b, item, d, st, pv, out, s_part, &s_flag, parts);
+                last = tile_reduce<NV, false, 3>(b, item, d, st, pv, out, s_part, &s_flag, parts);
             }
         }
         if (last && tid == 0) finish_replica<MODE, NV>(d, st, out, noise, prn);
@@ -755,7 +755,7 @@ __global__ void __launch_bounds__(MEANS_THREADS) k_replica_means(Batch b)
                 }
             }
             if (base + (tid & ~31) < ng * 32) {  // a warp of this level's groups
-                warp_sum_comp<3>(s, c);
+                warp_sum_comp<3, 3>(s, c);
                 const int g = (base + tid) >> 5;
                 if (lane == 0) {
                     if (ng > 1) {

@@ -6,8 +6,9 @@
 // adds them in that order).  Tile sums are then combined in a fixed tree:
 // groups of 32 consecutive tiles, then groups of 32 group sums, ...; the
 // block that completes a group's last member reduces the group with one
-// warp (compensated: (sum, error) pairs combined with TwoSum in a fixed
-// shuffle tree) and climbs one level.  Every level is one round trip, so a
+// warp (a fixed shuffle tree; energies and virial compensated -- (sum,
+// error) pairs combined with TwoSum -- the mean force / velocity plain) and
+// climbs one level.  Every level is one round trip, so a
 // replica of thousands of tiles finishes in a few, not in one warp's walk
 // over all tiles.  The result depends only on the replica's own particles,
 // slot layout and threads per particle -- not on the split, on which block
@@ -34,8 +35,11 @@ __device__ __forceinline__ void two_sum(double a, double b, double& s, double& e
     e = (a - (s - bp)) + (b - bp);
 }
 
-// compensated warp reduction of (s, c) pairs, every lane gets the total
-template <int NV>
+// compensated warp reduction of (s, c) pairs, every lane gets the total.
+// The first NPLAIN values (a replica's mean force or velocity) are summed
+// plainly in the same tree (their c stays 0): GB300's FP64 pipe is narrow,
+// and the error-free sums are kept for the energy-like values
+template <int NV, int NPLAIN = 0>
 __device__ __forceinline__ void warp_sum_comp(double (&s)[NV], double (&c)[NV])
 {
 #pragma unroll
@@ -43,6 +47,10 @@ __device__ __forceinline__ void warp_sum_comp(double (&s)[NV], double (&c)[NV])
 #pragma unroll
         for (int k = 0; k < NV; k++) {
             const double s2 = __shfl_xor_sync(0xffffffffu, s[k], o);
+            if (k < NPLAIN) {
+                s[k] += s2;
+                continue;
+            }
             const double c2 = __shfl_xor_sync(0xffffffffu, c[k], o);
             double t, e;
             two_sum(s[k], s2, t, e);
@@ -57,7 +65,7 @@ __device__ __forceinline__ void warp_sum_comp(double (&s)[NV], double (&c)[NV])
 // used).  s_part: 32*NV shared doubles; s_flag: one shared int.  Must be
 // called by every thread of the block (contains __syncthreads); blockDim a
 // multiple of 32.
-template <int NV, bool WARP_DONE = false>
+template <int NV, bool WARP_DONE = false, int NPLAIN = 0>
 __device__ bool tile_reduce(const Batch& b, int item, const RepDesc& d, RepState& st, double (&v)[NV],
                             double (&out)[NV], double* s_part, int* s_flag, int parts = 1)
 {
@@ -148,7 +156,7 @@ __device__ bool tile_reduce(const Batch& b, int item, const RepDesc& d, RepState
                 s[k] = lane < m ? __ldcg(src + (size_t)lane * RED_REC + k) : 0.0;
                 c[k] = lane < m ? __ldcg(src + (size_t)lane * RED_REC + NV + k) : 0.0;
             }
-            warp_sum_comp<NV>(s, c);
+            warp_sum_comp<NV, NPLAIN>(s, c);
             if (lane == 0) b.red_cnt[(size_t)level * b.ntiles + d.tile0 + g] = 0;
             idx = g;
             n = (n + 31) >> 5;
