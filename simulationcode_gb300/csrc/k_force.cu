@@ -706,8 +706,10 @@ __global__ void __launch_bounds__(TILE * T, force_min_blocks<PREC, T>()) k_force
 // after a stepping force pass, one block per replica: the replica's sums
 // from the warp slots of its tiles, in the canonical order of the tile
 // reduction (each tile its warp slots added in order; then groups of 32
-// consecutive tiles -- one warp -- reduced with compensation, level by
-// level, a level's group results kept in the reduction tree's records);
+// consecutive tiles -- one warp -- reduced in the tree's fixed shuffle
+// order, the mean force / velocity summed plainly as the tile reduction
+// sums them, level by level, a level's group results kept in the
+// reduction tree's records);
 // then what the pass's last tile does in the other modes: the mean force
 // (Brownian) or centre-of-mass velocity, the filtered-list bookkeeping and
 // the noise counter
