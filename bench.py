@@ -176,6 +176,22 @@ def peaks():
         return 6800.0, "fallback"
 
 
+def issue_bound(profile, force_ms, sm_mhz):
+    """The force kernel against the SMs' instruction-issue rate: its warp
+    instructions per launch and the GPU's SM count (ncu, ``profile``) at one
+    instruction per scheduler per cycle (4 per SM) at ``sm_mhz`` take
+    ``floor_ms``; ``frac`` is that floor over the measured launch time.
+    None without a profile."""
+    try:
+        w = float(profile["warp_instructions_per_launch"])
+        sms = int(profile["sm_count"])
+        floor_ms = w / (4.0 * sms * float(sm_mhz) * 1e6) * 1e3
+        return {"warp_instructions_per_launch": w, "sm_count": sms, "sm_mhz": float(sm_mhz),
+                "floor_ms": floor_ms, "frac": floor_ms / force_ms}
+    except (KeyError, TypeError, ValueError, ZeroDivisionError):
+        return None
+
+
 def force_bytes_per_launch(specs, stats, entries=None):
     """Algorithmic HBM bytes of one force-kernel launch, independent of the
     kernel's own representation: per particle its position (8 B per
@@ -567,11 +583,13 @@ def run_gpu(args, dist):
     peak, peak_kind = peaks()
     achieved = fbytes / (force_ms / 1000.0) / 1e9
     traffic = None
+    fprof = {}
     tfile = os.path.join(ROOT, "profiles", "force_traffic_%s.json" % args.workload)
     if os.path.exists(tfile):
         try:
             with open(tfile) as f:
-                traffic = json.load(f).get("dram_bytes_per_launch")
+                fprof = json.load(f)
+            traffic = fprof.get("dram_bytes_per_launch")
         except Exception:
             traffic = None
 
@@ -654,7 +672,8 @@ def run_gpu(args, dist):
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
                          "kernel": "k_force", "force_ms_per_launch": force_ms,
-                         "alg_bytes_per_launch": fbytes},
+                         "alg_bytes_per_launch": fbytes,
+                         "issue": issue_bound(fprof, force_ms, clk.get("sm_mhz") or clk.get("sm_max_mhz") or 2070.0)},
             "step_breakdown_ms": {k: prof[k] / max(prof["steps"], 1) for k in ("force_ms", "kick_ms", "rebuild_ms",
                                                                                "update_ms")},
             "e2e": e2e, "gpu_launches": int(launches), "clocks": clk}

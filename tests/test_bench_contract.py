@@ -46,3 +46,17 @@ def test_force_bytes_model_follows_the_list_read():
     per2 = 8 * 2 + 8 + 4 + 8 * 2 + 16 * 2
     assert bench.force_bytes_per_launch(specs, stats) == 100 * per3 + 50 * per2 + 4 * (3000 + 800)
     assert bench.force_bytes_per_launch(specs, stats, [1500.0, 400.0]) == 100 * per3 + 50 * per2 + 4 * (1500 + 400)
+
+
+def test_issue_bound_from_the_profile():
+    """the force kernel's issue-rate floor: warp instructions per launch over
+    4 schedulers x SMs x clock, as a fraction of the measured launch time"""
+    import bench
+    prof = {"warp_instructions_per_launch": 4 * 152 * 2070e6 * 1e-4, "sm_count": 152}
+    ib = bench.issue_bound(prof, 0.2, 2070.0)
+    assert abs(ib["floor_ms"] - 0.1) < 1e-12 and abs(ib["frac"] - 0.5) < 1e-12
+    assert bench.issue_bound({}, 0.2, 2070.0) is None
+    assert bench.issue_bound({"dram_bytes_per_launch": 1}, 0.2, 2070.0) is None
+    # the committed profile of the batch workload carries the figures
+    with open(os.path.join(ROOT, "profiles", "force_traffic_c4.json")) as f:
+        assert bench.issue_bound(json.load(f), 0.238, 2070.0)["frac"] > 0.3
