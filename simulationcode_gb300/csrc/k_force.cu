@@ -251,6 +251,23 @@ __device__ __forceinline__ void pairs_f32(const Batch& b, const RepDesc& d, long
     const FixRec* __restrict__ rec = b.s.rec;
     float r2, sd;
     int n = sub;
+    if constexpr (T == 1 && !PR) {
+        // the rows staged in shared memory first, by a pointer walk with no
+        // per-entry test of where the entry lives; the rest below (pairs in
+        // list order either way)
+        const int ns = min(cnt, nrows);
+        const unsigned* q = s_rows + pl;
+        for (; n + PAIR_UNROLL - 1 < ns; n += PAIR_UNROLL, q += PAIR_UNROLL * ppb) {
+            unsigned j[PAIR_UNROLL];
+            FixRec o[PAIR_UNROLL];
+#pragma unroll
+            for (int u = 0; u < PAIR_UNROLL; u++) j[u] = q[u * ppb] & IDX_MASK;
+#pragma unroll
+            for (int u = 0; u < PAIR_UNROLL; u++) o[u] = rec_get(rec + j[u]);
+#pragma unroll
+            for (int u = 0; u < PAIR_UNROLL; u++) pair_f32<DIM, POT, EN>(d, ri, o[u], fx, fy, fz, e, w, r2, sd);
+        }
+    }
     for (; n + (PAIR_UNROLL - 1) * T < cnt; n += PAIR_UNROLL * T) {
         unsigned j[PAIR_UNROLL];
         FixRec o[PAIR_UNROLL];
