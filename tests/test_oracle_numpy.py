@@ -13,8 +13,14 @@ oracle.  Each expression follows the reference line it cites:
     src/AuxiliaryFunctions.jl:22-34); virial = sum over pairs of
     (F/r) r^2 (the build's definition).
 
+and the time step written out the same way (Newtonian / Langevin velocity
+Verlet with the centre-of-mass removal, src/MD.jl:499-542; Brownian as
+intended by src/MD.jl:429-471), 10 steps beside the oracle's with the same
+noise.
+
 Tolerance: forces max|dF| <= 1e-12 max|F|; energy and virial relative
-1e-12 (the two differ only in summation order).
+1e-12 (the two differ only in summation order); positions and velocities
+after 10 steps within 1e-11.
 """
 import numpy as np
 import pytest
@@ -70,3 +76,51 @@ def test_oracle_matches_numpy_restatement(oracle, pot, dims, N):
     assert s.full_energy() == pytest.approx(V.sum() / 2.0, rel=1e-12)
     assert s.virial() == pytest.approx((Fr * r2).sum() / 2.0, rel=1e-12)
     assert np.abs(F_np).max() > 1.0 and (Fr != 0).sum() > N  # the case exercises the potential
+
+
+def _forces(p, r, D):
+    Fr, V, dx, r2 = _pair_terms(p, r, D)
+    return (Fr[:, :, None] * dx).sum(1)
+
+
+def _numpy_step(p, r, v, F, D, xi):
+    """one do_time_step of the reference written out in numpy: Newtonian /
+    Langevin src/MD.jl:499-542 (add_new_random_force! :30-45), Brownian as
+    intended by src/MD.jl:429-471 (forces + noise :62-74, the mean force
+    removed, r += (dt/gamma) F, wrapped).  Returns (r, v, F)."""
+    L, dt, m = p.box_size, p.dt, p.m
+    if p.dynamics == 2:  # Brownian
+        F = _forces(p, r, D) + np.sqrt(2 * p.kBT * p.gamma / dt) * xi
+        F = F - F.sum(0) / p.N
+        rn = r + (dt / p.gamma) * F
+        rn -= np.floor(rn / L) * L
+        return rn, v, F
+    v = v + dt * F / (2.0 * m)
+    rn = r + dt * v
+    rn -= np.floor(rn / L) * L
+    F = _forces(p, rn, D)
+    if p.dynamics == 1:  # Langevin
+        F = F + (-p.gamma * v + np.sqrt(2 * p.kBT * p.gamma / dt) * xi)
+    v = v + dt * F / (2.0 * m)
+    v = v - v.sum(0) / p.N
+    return rn, v, F
+
+
+@pytest.mark.parametrize("pot,dims,dyn", [(1, 3, 0), (0, 3, 1), (1, 2, 1), (1, 3, 2), (1, 2, 2)])
+def test_oracle_time_step_matches_numpy_restatement(oracle, pot, dims, dyn):
+    N, nsteps = (343 if dims == 3 else 400), 10
+    dt = 2e-5 if dyn == 2 else 0.005
+    p, r, v, D, rc = make_case(pot, dims, dyn, N, seed=13, dt=dt)
+    s = oracle.OracleSystem(p, r, D, v=v, force_cutoff=rc)
+    s.update_neighbor_lists()
+    s.calculate_new_forces(np.zeros((N, dims)))
+    rn, vn, Fn = s.r.copy(), s.v.copy(), s.F.copy()
+    noise = np.random.default_rng(17).standard_normal((nsteps, N, dims))
+    for k in range(nsteps):
+        s.step(noise[k] if dyn else None)
+        rn, vn, Fn = _numpy_step(p, rn, vn, Fn, np.asarray(D, float), noise[k])
+    d = s.r - rn
+    d -= np.round(d / p.box_size) * p.box_size
+    assert np.abs(d).max() <= 1e-11
+    if dyn != 2:
+        assert np.abs(s.v - vn).max() <= 1e-11 * max(1.0, np.abs(vn).max())
