@@ -16,7 +16,8 @@ oracle.  Each expression follows the reference line it cites:
 and the time step written out the same way (Newtonian / Langevin velocity
 Verlet with the centre-of-mass removal, src/MD.jl:499-542; Brownian as
 intended by src/MD.jl:429-471), 10 steps beside the oracle's with the same
-noise.
+noise; and the inherent-structure descent (src/InherentStructure.jl:5-56),
+200 iterations.
 
 Tolerance: forces max|dF| <= 1e-12 max|F|; energy and virial relative
 1e-12 (the two differ only in summation order); positions and velocities
@@ -124,3 +125,26 @@ def test_oracle_time_step_matches_numpy_restatement(oracle, pot, dims, dyn):
     assert np.abs(d).max() <= 1e-11
     if dyn != 2:
         assert np.abs(s.v - vn).max() <= 1e-11 * max(1.0, np.abs(vn).max())
+
+
+@pytest.mark.parametrize("pot,dims,N,dt", [(1, 3, 216, 0.005), (1, 2, 256, 1e-3), (0, 3, 216, 1e-3)])
+def test_oracle_minimiser_matches_numpy_restatement(oracle, pot, dims, N, dt):
+    """find_inherent_structure (src/InherentStructure.jl:5-56) written out in
+    numpy: v = F dt, capped so that max |v| <= max_step_size, r += v
+    wrapped; 200 iterations of it beside the oracle's stopped at
+    max_iterations = 200"""
+    p, r, v, D, rc = make_case(pot, dims, 0, N, seed=21)
+    s = oracle.OracleSystem(p, r, D, v=v, force_cutoff=rc)
+    st, it = oracle.find_inherent_structure(s, tolerance=1e-12, max_iterations=200, max_step_size=0.001, dt=dt)
+    assert st == 2  # stopped by max_iterations, after exactly 200 iterations
+    rn, L, Dn = np.array(r, float), p.box_size, np.asarray(D, float)
+    for _ in range(200):
+        step = _forces(p, rn, Dn) * dt
+        size = np.sqrt((step * step).sum(1)).max()
+        if size > 0.001:
+            step *= 0.001 / size
+        rn = rn + step
+        rn -= np.floor(rn / L) * L
+    d = s.r - rn
+    d -= np.round(d / L) * L
+    assert np.abs(d).max() <= 1e-10
