@@ -16,8 +16,9 @@ oracle.  Each expression follows the reference line it cites:
 and the time step written out the same way (Newtonian / Langevin velocity
 Verlet with the centre-of-mass removal, src/MD.jl:499-542; Brownian as
 intended by src/MD.jl:429-471), 10 steps beside the oracle's with the same
-noise; and the inherent-structure descent (src/InherentStructure.jl:5-56),
-200 iterations.
+noise; the inherent-structure descent (src/InherentStructure.jl:5-56),
+200 iterations; and swap Monte Carlo sweeps (src/MC.jl:21-156) with the
+oracle's keyed draws.
 
 Tolerance: forces max|dF| <= 1e-12 max|F|; energy and virial relative
 1e-12 (the two differ only in summation order); positions and velocities
@@ -148,3 +149,74 @@ def test_oracle_minimiser_matches_numpy_restatement(oracle, pot, dims, N, dt):
     d = s.r - rn
     d -= np.round(d / L) * L
     assert np.abs(d).max() <= 1e-10
+
+
+def _particle_energy(p, i, ri, Di, r, D):
+    """find_energy (src/AuxiliaryFunctions.jl:546-584, berthier_inner_loop3/2)
+    over all other particles"""
+    d = ri[None, :] - r
+    d -= np.round(d / p.box_size) * p.box_size
+    r2 = (d * d).sum(1)
+    r2[i] = np.inf
+    mean_d = (Di + D) * 0.5 * (1.0 - p.b_zeta * np.abs(Di - D))
+    s2 = mean_d * mean_d
+    with np.errstate(divide="ignore", over="ignore", invalid="ignore"):
+        ix2 = r2 / s2
+        ix4 = ix2 * ix2
+        xi12 = 1.0 / (ix4 * ix4 * ix4)
+        V = np.where(p.force_cutoff2 * s2 < r2, 0.0, xi12 + p.b_c4 * ix4 + p.b_c2 * ix2 + p.b_c0)
+    return V.sum()
+
+
+@pytest.mark.parametrize("dims,N", [(3, 216), (2, 256)])
+def test_oracle_mc_matches_numpy_restatement(oracle, dims, N):
+    """do_MC_step! (src/MC.jl:139-156) with do_translation_step! (:21-47) and
+    do_swap_step! (:67-110) written out in numpy over all pairs, with the
+    oracle's keyed draws (u[0] move kind, u[1] acceptance, u[2..] the
+    displacement, u[5] the swap partner, drawn uniformly: the evident intent
+    of src/MC.jl:152, whose ceil(rand()/N) always gives particle 1): the
+    same moves accepted, the same positions and diameters, the same summed
+    dE"""
+    p, r, v, D, rc = make_case(1, dims, 0, N, seed=4, skin=0.6)
+    p.kBT = 0.5
+    s = oracle.OracleSystem(p, r, D, force_cutoff=rc)
+    s.update_neighbor_lists()
+    nsweeps, max_disp, swap_prob, seed = 3, 0.08, 0.3, 77
+    counts, de = s.mc_sweeps(nsweeps, max_disp, swap_prob, seed)
+    rn, Dn, L = np.array(r, float), np.array(D, float), p.box_size
+    cn, den = np.zeros(4, np.int64), 0.0
+    for sw in range(nsweeps):
+        for i in range(N):
+            u = oracle.mc_uniforms(seed, sw, i)
+            if u[0] > swap_prob:  # translation
+                dr = u[2:2 + dims] * 2.0 * max_disp - max_disp
+                e_old = _particle_energy(p, i, rn[i], Dn[i], rn, Dn)
+                rnew = rn[i] + dr
+                rnew -= np.floor(rnew / L) * L
+                dE = _particle_energy(p, i, rnew, Dn[i], rn, Dn) - e_old
+                cn[1] += 1
+                if min(1.0, np.exp(-dE / p.kBT)) > u[1]:
+                    cn[0] += 1
+                    rn[i] = rnew
+                    den += dE
+            else:  # swap
+                j = min(int(u[5] * N), N - 1)
+                if j == i or abs(Dn[i] - Dn[j]) > 0.2:
+                    continue
+                Di, Dj = Dn[i], Dn[j]
+                old = _particle_energy(p, i, rn[i], Di, rn, Dn) + _particle_energy(p, j, rn[j], Dj, rn, Dn)
+                Dn[i], Dn[j] = Dj, Di
+                new = _particle_energy(p, i, rn[i], Dj, rn, Dn) + _particle_energy(p, j, rn[j], Di, rn, Dn)
+                dE = new - old
+                cn[3] += 1
+                if min(1.0, np.exp(-dE / p.kBT)) > u[1]:
+                    cn[2] += 1
+                    den += dE
+                else:
+                    Dn[i], Dn[j] = Di, Dj
+    assert np.array_equal(counts, cn) and cn[0] > 0 and cn[2] > 0
+    assert np.array_equal(s.D, Dn)
+    d = s.r - rn
+    d -= np.round(d / L) * L
+    assert np.abs(d).max() <= 1e-12
+    assert de == pytest.approx(den, rel=1e-9, abs=1e-9)
