@@ -19,7 +19,11 @@
 // particle's T lanes adjacent) and combine with __shfl_xor; the split
 // pass stages the first list rows of its particles in shared memory and
 // gathers PAIR_UNROLL neighbour records at a time.  Every pair is visited
-// from both sides (no atomics, deterministic sums).
+// from both sides (no atomics, deterministic sums).  Per-replica sums (mean
+// force or centre-of-mass velocity, energy, virial) go through the fixed
+// reduction tree of simmd_reduce.cuh; a stepping pass over a batch of many
+// small replicas only stores its warps' partials and leaves the tree to
+// k_replica_means, launched after it.
 //
 // FP64 path: the reference's per-pair operation order with explicit
 // round-to-nearest intrinsics, so each pair force is bit-identical to the
