@@ -97,3 +97,43 @@ def test_julia_ccalls_match_the_header(path):
     assert len(calls) >= (25 if path.endswith(".jl") else 8)
     bad = [(n, r, a, protos.get(n)) for n, r, a in calls if protos.get(n) != (r, a)]
     assert not bad, bad
+
+
+def header_struct(name):
+    """[(field, kind)] of `typedef struct name { ... } name;` in the header"""
+    src = open(os.path.join(ROOT, "include", "simmd.h")).read()
+    src = re.sub(r"/\*.*?\*/", " ", src, flags=re.S)
+    body = re.search(r"typedef struct %s\s*\{(.*?)\}\s*%s;" % (name, name), src, flags=re.S).group(1)
+    fields = []
+    for decl in body.split(";"):
+        decl = decl.strip()
+        if not decl:
+            continue
+        typ, names = decl.split(None, 1)
+        fields += [(n.strip(), C_SCALARS[typ]) for n in names.split(",")]
+    return fields
+
+
+def julia_struct(name):
+    src = open(os.path.join(ROOT, "julia", "SimulationCodeGPU.jl")).read()
+    body = re.search(r"\nstruct %s\n(.*?)\nend" % name, src, flags=re.S).group(1)
+    fields = []
+    for decl in re.split(r"[;\n]", body):
+        decl = decl.strip()
+        if decl:
+            n, t = decl.split("::")
+            fields.append((n.strip(), JULIA_SCALARS[t.strip()]))
+    return fields
+
+
+@pytest.mark.parametrize("cname,pyname,jlname", [("simmd_params", "Params", "SimmdParams"),
+                                                 ("simmd_stats", "Stats", "SimmdStats")])
+def test_structs_match_the_header(cname, pyname, jlname):
+    """the parameter and statistics structs: the same fields, in the same
+    order, of the same widths in the header, the ctypes mirror and the Julia
+    module (isbits structs laid out as C's)"""
+    from simulationcode_gb300 import _lib
+    want = header_struct(cname)
+    py = [(n, _ctypes_kind(t)) for n, t in getattr(_lib, pyname)._fields_]
+    assert py == want
+    assert julia_struct(jlname) == want
