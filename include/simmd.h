@@ -259,7 +259,8 @@ int simmd_set_budget(simmd_ctx* ctx, int64_t bytes);
  * caller owns: r (dims x N AoS), D (N), the full neighbour list as in the
  * reference (counts[N], list[maxK*N] column-major, 1-based) and out[3].
  * Scratch is a fixed array inside the library, shared by every call on a
- * GPU: N must be <= SIMMD_NOALLOC_MAX_N (else SIMMD_ERR_BUDGET), and calls
+ * GPU: N must be <= SIMMD_NOALLOC_MAX_N (else SIMMD_ERR_BUDGET, checked
+ * before any device work; simmd_last_error says why), and calls
  * that run concurrently on the same GPU race.  The first call on a device
  * performs a one-time symbol lookup, which may load the library's device
  * code onto that GPU (lazy module loading) and so reserve its memory; make

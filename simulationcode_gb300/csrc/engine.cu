@@ -64,6 +64,9 @@ static int set_err(int code, const std::string& msg)
     return code;
 }
 
+// the same record for entry points defined in other translation units
+int simmd::record_error(int code, const char* msg) { return set_err(code, msg); }
+
 #define CK(call)                                                                                   \
     do {                                                                                           \
         cudaError_t e_ = (call);                                                                   \

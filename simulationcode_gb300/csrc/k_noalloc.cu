@@ -235,15 +235,21 @@ extern "C" int simmd_energy_virial_noalloc(const simmd_params* prm, const double
                                            const int64_t* counts, const int64_t* list, int64_t maxK, double* out,
                                            void* stream)
 {
-    if (!prm || !r || !D || !counts || !list || !out) return SIMMD_ERR_BAD_ARG;
-    if (prm->dims != 2 && prm->dims != 3) return SIMMD_ERR_BAD_ARG;
-    if (prm->potential != SIMMD_POT_LJ && prm->potential != SIMMD_POT_BERTHIER) return SIMMD_ERR_BAD_ARG;
-    if (prm->N < 1 || prm->N > SIMMD_NOALLOC_MAX_N) return SIMMD_ERR_BUDGET;  // beyond the scratch size
-    if (maxK < 1) return SIMMD_ERR_BAD_ARG;
+    using simmd::record_error;
+    if (!prm || !r || !D || !counts || !list || !out) return record_error(SIMMD_ERR_BAD_ARG, "NULL argument");
+    if (prm->dims != 2 && prm->dims != 3) return record_error(SIMMD_ERR_BAD_ARG, "dims must be 2 or 3");
+    if (prm->potential != SIMMD_POT_LJ && prm->potential != SIMMD_POT_BERTHIER)
+        return record_error(SIMMD_ERR_BAD_ARG, "unknown potential");
+    if (prm->N < 1) return record_error(SIMMD_ERR_BAD_ARG, "N must be >= 1");
+    if (prm->N > SIMMD_NOALLOC_MAX_N)  // beyond the fixed scratch
+        return record_error(SIMMD_ERR_BUDGET,
+                            "N is beyond SIMMD_NOALLOC_MAX_N (1048576 particles), the size of the fixed scratch "
+                            "of simmd_energy_virial_noalloc: use simmd_energy on a context instead");
+    if (maxK < 1) return record_error(SIMMD_ERR_BAD_ARG, "maxK must be >= 1");
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= NA_MAX_DEVICES) {
         cudaGetLastError();
-        return SIMMD_ERR_NO_DEVICE;
+        return record_error(SIMMD_ERR_NO_DEVICE, "no CUDA device current");
     }
     double* scratch = nullptr;
     {
@@ -257,7 +263,7 @@ extern "C" int simmd_energy_virial_noalloc(const simmd_params* prm, const double
             if (e != cudaSuccess || !ptr) {
                 cudaGetLastError();
                 g_na_ptr[dev] = nullptr;
-                return SIMMD_ERR_CUDA;
+                return record_error(SIMMD_ERR_CUDA, "cudaGetSymbolAddress of the fixed scratch failed");
             }
             g_na_ptr[dev] = static_cast<double*>(ptr);
             g_na_ctx[dev] = current_ctx_id();  // the lookup has made the context current
@@ -268,7 +274,7 @@ extern "C" int simmd_energy_virial_noalloc(const simmd_params* prm, const double
     // counter and invalid-entry count must start at zero for every call
     if (cudaMemsetAsync(scratch, 0, 2 * sizeof(double), s) != cudaSuccess) {
         cudaGetLastError();
-        return SIMMD_ERR_CUDA;
+        return record_error(SIMMD_ERR_CUDA, "clearing the fixed scratch failed");
     }
     NAParams p;
     p.L = prm->box_size;
@@ -299,6 +305,6 @@ extern "C" int simmd_energy_virial_noalloc(const simmd_params* prm, const double
         else
             k_energy_noalloc<2, simmd::POT_LJ><<<grid, NA_BLOCK, 0, s>>>(p, N, r, D, c, l, maxK, scratch, out);
     }
-    if (cudaGetLastError() != cudaSuccess) return SIMMD_ERR_CUDA;
+    if (cudaGetLastError() != cudaSuccess) return record_error(SIMMD_ERR_CUDA, "kernel launch failed");
     return SIMMD_OK;
 }

@@ -162,6 +162,9 @@ struct Slots {
     int* cell_start;              // per cell (+ pad cell + end)
 };
 
+// sets simmd_last_error's message and returns code (host code)
+int record_error(int code, const char* msg);
+
 struct Batch {
     const RepDesc* desc;
     RepState* state;

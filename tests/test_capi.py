@@ -67,3 +67,23 @@ def test_replica_bytes_estimate(simlib):
     p.N = 4096
     b = simlib.simmd_replica_bytes(C.byref(p), 64)
     assert 4096 * 256 < b < 4096 * 2048
+
+
+def test_noalloc_entry_rejects_before_any_device_work(simlib):
+    """the no-allocation entry point checks its sizes before it touches a
+    device: N beyond its fixed scratch is SIMMD_ERR_BUDGET, with the limit
+    named in simmd_last_error"""
+    from simulationcode_gb300 import _lib
+    buf = (C.c_double * 8)()
+    ptrs = [C.cast(buf, C.c_void_p)] * 5
+    p = _lib.Params()
+    p.dims, p.potential = 3, 1
+    p.N = 1048576 + 1
+    st = simlib.simmd_energy_virial_noalloc(C.byref(p), *ptrs[:4], 1, ptrs[4], None)
+    assert st == _lib.ERR_BUDGET
+    assert b"SIMMD_NOALLOC_MAX_N" in simlib.simmd_last_error()
+    p.N = 0
+    assert simlib.simmd_energy_virial_noalloc(C.byref(p), *ptrs[:4], 1, ptrs[4], None) == _lib.ERR_BAD_ARG
+    p.N, p.dims = 10, 4
+    assert simlib.simmd_energy_virial_noalloc(C.byref(p), *ptrs[:4], 1, ptrs[4], None) == _lib.ERR_BAD_ARG
+    assert b"dims" in simlib.simmd_last_error()
