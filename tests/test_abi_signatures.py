@@ -139,3 +139,61 @@ def test_structs_match_the_header(cname, pyname, jlname):
     assert julia_struct(jlname) == want
     if cname == "simmd_params":  # the copy in the binding examples
         assert julia_struct(jlname, "INTEGRATION.md") == want
+
+
+# the reference's generic functions on the hot path: positional arity and the
+# position (1-based) of the neighbour-list argument, from their definitions
+REFERENCE_GENERICS = {
+    "update_neighbor_lists!": (4, 4),        # src/NeighborLists.jl:24
+    "calculate_new_forces!": (3, 3),         # src/MD.jl:262
+    "do_time_step": (5, 4),                  # src/MD.jl:429, 499
+    "run_short_MD_equilibration!": (4, 4),   # src/MD.jl:579
+    "calculate_full_energy": (3, 3),         # src/AuxiliaryFunctions.jl:22
+    "compute_potential_energy!": (4, 4),     # src/AuxiliaryFunctions.jl:186
+    "print_log_data": (5, 4),                # src/MD.jl:610
+    "find_inherent_structure": (5, 4),       # src/InherentStructure.jl:5
+    "do_MC_step!": (5, 4),                   # src/MC.jl:139
+}
+
+
+def _split_args(s):
+    out, depth, cur = [], 0, ""
+    for ch in s:
+        if ch in "({[":
+            depth += 1
+        elif ch in ")}]":
+            depth -= 1
+        if ch == "," and depth == 0:
+            out.append(cur)
+            cur = ""
+        else:
+            cur += ch
+    if cur.strip():
+        out.append(cur)
+    return [a.strip() for a in out]
+
+
+def test_julia_methods_extend_the_reference_generics():
+    """every hot-path generic function of the reference gets a method for the
+    device neighbour list with the reference's positional arity and the list
+    in the reference's position, and the module imports the name from
+    SimulationCode (so the method extends the reference's function, which
+    the reference's own driver then dispatches to)"""
+    src = open(os.path.join(ROOT, "julia", "SimulationCodeGPU.jl")).read()
+    imports = re.search(r"import SimulationCode:(.*?)\n\s*using", src, flags=re.S).group(1)
+    imported = {x.strip() for x in imports.replace("\n", " ").split(",")}
+    found = {}
+    for name, args in re.findall(r"(?:^function |^)([A-Za-z_!]+)\(([^;)]*(?:\([^)]*\)[^;)]*)*)[;)]", src,
+                                 flags=re.M):
+        parts = _split_args(args)
+        pos = [k + 1 for k, a in enumerate(parts) if a.endswith("::GPUNeighborList")]
+        if pos:
+            found.setdefault(name, set()).add((len(parts), pos[0]))
+    for name, sig in REFERENCE_GENERICS.items():
+        assert name in imported, name
+        assert sig in found.get(name, set()), (name, found.get(name))
+    # initialize_neighbor_struct(skin, box_size, force_cutoff, N, D_array, dims;
+    # maxneighbours) (src/DataStructs.jl:349) plus the trailing device marker
+    assert "initialize_neighbor_struct" in imported
+    assert re.search(r"function initialize_neighbor_struct\(skin_distance, box_size, force_cutoff, N, D_array, dims, "
+                     r"dev::GPU;", src)
