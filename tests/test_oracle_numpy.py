@@ -9,6 +9,8 @@ oracle.  Each expression follows the reference line it cites:
     src/AuxiliaryFunctions.jl:381-444;
   * LJ 3D force over r: compute_forces_lj_3d, src/MD.jl:140-191;
   * LJ 3D energy: LJ_inner_loop, src/AuxiliaryFunctions.jl:477-507;
+  * LJ 2D force and energy: the generic loops, src/MD.jl:291-309 and
+    src/AuxiliaryFunctions.jl:571-581 (find_mean_D(LJ) = sigma^2, squared);
   * energy = half the sum over ordered pairs (calculate_full_energy,
     src/AuxiliaryFunctions.jl:22-34); virial = sum over pairs of
     (F/r) r^2 (the build's definition).
@@ -54,6 +56,21 @@ def _pair_terms(p, r, D):
             ix4 = ix2 * ix2
             xi12 = 1.0 / (ix4 * ix4 * ix4)
             V = np.where(out, 0.0, xi12 + p.b_c4 * ix4 + p.b_c2 * ix2 + p.b_c0)
+        elif dims == 2:  # LJ 2D: the generic loop, src/MD.jl:291-309, and find_energy's
+            # generic branch, src/AuxiliaryFunctions.jl:571-581; find_mean_D(LJ) = sigma^2
+            # (src/InteractionPotential.jl:5-7), squared again; strict '>' cut
+            mds = (p.lj_sigma ** 2) * (p.lj_sigma ** 2)
+            inside = rc2 * mds > r2
+            inv = 1.0 / r2
+            xi2 = mds * inv
+            xi6 = xi2 * xi2 * xi2
+            xi12 = xi6 * xi6
+            Fr = np.where(inside, p.lj_eps * (48.0 * xi12 - 24.0 * xi6) * inv, 0.0)
+            y2 = mds / r2
+            y4 = y2 * y2
+            y6 = y2 * y4
+            y12 = y6 * y6
+            V = np.where(inside, 4.0 * p.lj_eps * (y12 - y6) - p.lj_Uc, 0.0)
         else:  # LJ, 3D
             s2 = p.lj_sigma * p.lj_sigma
             xi2 = s2 / r2
@@ -66,7 +83,7 @@ def _pair_terms(p, r, D):
     return Fr, V, dx, np.where(np.isfinite(r2), r2, 0.0)
 
 
-@pytest.mark.parametrize("pot,dims,N", [(1, 3, 343), (1, 2, 400), (0, 3, 343)])
+@pytest.mark.parametrize("pot,dims,N", [(1, 3, 343), (1, 2, 400), (0, 3, 343), (0, 2, 400)])
 def test_oracle_matches_numpy_restatement(oracle, pot, dims, N):
     p, r, v, D, rc = make_case(pot, dims, oracle.NEWTONIAN, N, seed=9, mc_sweeps=10)
     s = oracle.OracleSystem(p, r, D, force_cutoff=rc)
