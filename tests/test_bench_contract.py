@@ -60,3 +60,23 @@ def test_issue_bound_from_the_profile():
     # the committed profile of the batch workload carries the figures
     with open(os.path.join(ROOT, "profiles", "force_traffic_c4.json")) as f:
         assert bench.issue_bound(json.load(f), 0.238, 2070.0)["frac"] > 0.3
+
+
+def test_reference_arm_under_torchrun_prints_one_line():
+    """--impl reference launched as the driver launches a multi-GPU run (two
+    ranks, gloo on the CPU): rank 0 alone runs and prints the line, the
+    other rank exits 0 without work"""
+    import socket
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        port = s.getsockname()[1]
+    env = dict(os.environ, OMP_NUM_THREADS="1")
+    r = subprocess.run([sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", "2",
+                        "--master-addr", "127.0.0.1", "--master-port", str(port), "bench.py", "--impl", "reference",
+                        "--gpus", "2", "--workload", "c1", "--steps", "3", "--warmup", "3", "--relax-steps", "0"],
+                       cwd=ROOT, capture_output=True, text=True, timeout=300, env=env)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [l for l in r.stdout.splitlines() if l.strip().startswith("{")]
+    assert len(lines) == 1
+    d = json.loads(lines[0])
+    assert d["impl"] == "reference" and d["n_gpus"] == 2 and d["value"] > 0
